@@ -1,0 +1,1267 @@
+// GB300 PC-stable CI-testing engine: device kernels and the C ABI.
+//
+// Batched mode (the product path) keeps the whole skeleton on the device:
+//   * the adjacency is an n x n bitset; each level snapshots it into sorted
+//     per-node neighbour lists (PCStable.cpp:272, FindAdjacencies :500-515);
+//   * every remaining edge x<y owns the ranked sequence of its candidate
+//     conditioning sets: C(|adj(x)\y|, d) x-side sets, then C(|adj(y)\x|, d)
+//     y-side sets, each in the lexicographic order of ChoiceGenerator
+//     (CheckEdge :399-494, ChoiceGenerator.cpp:55-85);
+//   * a level runs in waves; a wave gives each unresolved edge the next q
+//     ranks (q grows geometrically), one persistent kernel drains all tests
+//     of the wave from a work counter, and a reduction keeps, per edge, the
+//     FIRST independent rank -- the reference's sepset (Testing :526-614);
+//   * removals are applied to the bitset at the end of the level and the
+//     FreeDegree stop rule (:620-626, :387) is evaluated on the device.
+// Plain mode is the reference's control flow on the host with one kernel
+// launch (whole GPU) per CI test; it is the comparison baseline.
+#include <cuda_runtime.h>
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ci_device.cuh"
+#include "fastpgm_gb300.h"
+#include "engine_internal.h"
+
+using namespace fpgm;
+
+// ------------------------------------------------------------------ errors
+namespace {
+thread_local std::string g_last_error;
+}
+
+namespace fpgm {
+int set_error(int code, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+}  // namespace fpgm
+
+extern "C" const char *fpgm_last_error(void) { return g_last_error.c_str(); }
+
+#define CK(call)                                                                                    \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return set_error(e_ == cudaErrorMemoryAllocation ? FPGM_ERR_OOM : FPGM_ERR_CUDA,       \
+                             "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+#define RET(call)                    \
+    do {                             \
+        int r_ = (call);             \
+        if (r_ != FPGM_OK) return r_; \
+    } while (0)
+
+// ------------------------------------------------------------------ device buffers
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t need, bool keep = false, cudaStream_t st = nullptr) {
+        if (need <= bytes) return FPGM_OK;
+        size_t nb = std::max(need, bytes + bytes / 2);
+        void *q = nullptr;
+        cudaError_t e = cudaMalloc(&q, nb);
+        if (e != cudaSuccess)
+            return set_error(FPGM_ERR_OOM, "cudaMalloc(%zu) failed: %s", nb, cudaGetErrorString(e));
+        if (keep && p && bytes) {
+            e = cudaMemcpyAsync(q, p, bytes, cudaMemcpyDeviceToDevice, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) {
+                cudaFree(q);
+                return set_error(FPGM_ERR_CUDA, "buffer grow copy failed: %s", cudaGetErrorString(e));
+            }
+        }
+        if (p) cudaFree(p);
+        p = q;
+        bytes = nb;
+        return FPGM_OK;
+    }
+    template <class T> T *as() const { return static_cast<T *>(p); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+constexpr int kStatusActive = 0, kStatusRemoved = 1, kStatusKept = 2;
+// device statistics slots
+enum { ST_RECHECK = 0, ST_NEARTIE, ST_LARGE, ST_MAXDP, ST_UNSUPPORTED, ST_DET, ST_EXEC, ST_UNRESOLVED,
+       ST_REMOVED, ST_MAXDEG, ST_NACTIVE, ST_COUNT };
+
+constexpr int kSmemBytes = 96 * 1024;
+constexpr int64_t kSmemBudgetInts = (kSmemBytes / 4);
+constexpr int64_t kLargeIntsPerSlot = (int64_t)1 << 25;  // 128 MB per global-memory slot
+constexpr int kLargeSlots = 16;
+
+}  // namespace
+
+struct fpgm_engine {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0, ci_blocks = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // data
+    int n = 0;
+    int64_t S = 0, S_pad = 0;
+    DevBuf cols, card;
+    std::vector<uint8_t> h_card;
+    DevBuf btab;
+    // level workspace
+    DevBuf bits, deg, adjl, edges_x, edges_y, pxy, pyx, cntx, total, next, status, seprank, g, off, flag,
+        large_list, counters, stats, scan_tmp, log_pair, log_vars, log_meta, node_cnt, node_off;
+    DevBuf large_ws, plain_ws, tests_buf, detail_buf;
+    // result
+    bool has_result = false;
+    std::vector<uint8_t> res_adj;
+    std::vector<int32_t> res_removed, res_off, res_vars;
+};
+
+// ------------------------------------------------------------------ kernels
+namespace {
+
+struct WaveArgs {
+    const uint8_t *cols;
+    int64_t S, S_pad;
+    const uint8_t *card;
+    int d;
+    // wave source
+    const int32_t *adjl;
+    int32_t adj_stride;
+    const int32_t *deg;
+    const int32_t *ex, *ey, *pxy, *pyx;
+    const uint64_t *cntx, *next;
+    const int32_t *off;
+    int32_t n_edges;
+    const uint64_t *btab;
+    // explicit source
+    const int32_t *tests;
+    int32_t n_tests;
+    // outputs
+    uint8_t *flag;
+    fpgm_ci_result *detail;
+    int32_t want_hash;
+    int32_t *large_list;
+    int32_t *counters;  // [0] work, [1] large count, [2] large work
+    unsigned long long *stats;
+    double alpha;
+    int32_t *large_ws;
+    int64_t large_stride;
+};
+
+enum { SRC_WAVE = 0, SRC_EXPLICIT = 1 };
+
+__device__ inline int upper_bound_i32(const int32_t *a, int n, int v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] <= v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// thread-0 prologue: item -> descriptor
+template <int kSource>
+__device__ inline void build_desc(const WaveArgs &a, int item, TestDesc &t) {
+    if (kSource == SRC_EXPLICIT) {
+        const int32_t *tt = a.tests + (int64_t)item * (2 + a.d);
+        t.x = tt[0];
+        t.y = tt[1];
+        t.d = a.d;
+        for (int k = 0; k < a.d; ++k) t.z[k] = tt[2 + k];
+    } else {
+        const int e = upper_bound_i32(a.off, a.n_edges + 1, item) - 1;
+        uint64_t rank = a.next[e] + (uint64_t)(item - a.off[e]);
+        t.x = a.ex[e];
+        t.y = a.ey[e];
+        t.d = a.d;
+        if (a.d > 0) {
+            int side_node, skip;
+            if (rank < a.cntx[e]) {
+                side_node = t.x;
+                skip = a.pxy[e];
+            } else {
+                rank -= a.cntx[e];
+                side_node = t.y;
+                skip = a.pyx[e];
+            }
+            int c[kMaxCond];
+            unrank_lex(a.btab, a.deg[side_node] - 1, a.d, rank, c);
+            const int32_t *L = a.adjl + (int64_t)side_node * a.adj_stride;
+            for (int k = 0; k < a.d; ++k) t.z[k] = L[c[k] < skip ? c[k] : c[k] + 1];
+        }
+    }
+    desc_finish(t, a.cols, a.S_pad, a.card, kSmemBudgetInts, kLargeIntsPerSlot);
+}
+
+__device__ inline void record_verdict(const WaveArgs &a, int item, const TestDesc &t, const Verdict &v,
+                                      const int *ct, int path) {
+    a.flag[item] = (uint8_t)v.indep;
+    if (v.rechecked) {
+        atomicAdd(&a.stats[ST_RECHECK], 1ull);
+        if (fabs(v.p - a.alpha) < 1e-12) atomicAdd(&a.stats[ST_NEARTIE], 1ull);
+        atomicMax(&a.stats[ST_MAXDP], (unsigned long long)__double_as_longlong(v.dp));
+    }
+    if (a.detail) {
+        fpgm_ci_result r;
+        r.table_hash = a.want_hash ? table_hash(ct, t.cells) : 0;
+        r.cells = t.cells;
+        r.df = (int32_t)v.df;
+        r.independent = v.indep;
+        r.g2 = v.g2;
+        r.p_value = v.p;
+        r.rechecked = v.rechecked;
+        r.path = path;
+        a.detail[item] = r;
+    }
+}
+
+// Persistent count+score kernel: one CTA per test at a time, shared-memory tables.
+template <int kSource>
+__global__ void __launch_bounds__(kThreads, 2) ci_kernel(WaveArgs a) {
+    extern __shared__ int smem[];
+    __shared__ TestDesc td;
+    __shared__ int s_item;
+    __shared__ Partial scratch[kWarps];
+    const int tid = threadIdx.x;
+    const int T = kSource == SRC_EXPLICIT ? a.n_tests : a.off[a.n_edges];
+    const int64_t nvec = a.S >> 4;
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(&a.counters[0], 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= T) break;
+        if (tid == 0) build_desc<kSource>(a, item, td);
+        __syncthreads();
+        if (td.path != 0) {
+            if (tid == 0) {
+                if (td.path == 1) {
+                    int slot = atomicAdd(&a.counters[1], 1);
+                    a.large_list[slot] = item;
+                    atomicAdd(&a.stats[ST_LARGE], 1ull);
+                } else {
+                    a.flag[item] = 2;
+                    atomicAdd(&a.stats[ST_UNSUPPORTED], 1ull);
+                }
+            }
+            __syncthreads();
+            continue;
+        }
+        const int64_t tabn = td.cells * td.R;
+        int *tab = smem;
+        int *ct = td.R > 1 ? smem + tabn : smem;
+        int *ni = ct + td.cells;
+        int *nj = ni + td.dz * td.dx;
+        int *nk = nj + td.dz * td.dy;
+        for (int64_t i = tid; i < tabn; i += kThreads) tab[i] = 0;
+        __syncthreads();
+        count_range<false>(td, 0, nvec, true, a.S, tab, tid, kThreads);
+        __syncthreads();
+        if (td.R > 1) {
+            const int R = td.R, Rm = R - 1;
+            for (int64_t c = tid; c < td.cells; c += kThreads) {
+                int s = 0;
+                for (int r = 0; r < R; ++r) s += tab[c * R + ((r + (int)c) & Rm)];
+                ct[c] = s;
+            }
+            __syncthreads();
+        }
+        Verdict v = score_table(td, ct, ni, nj, nk, a.alpha, scratch, tid, kThreads);
+        if (tid == 0) record_verdict(a, item, td, v, ct, 0);
+        __syncthreads();
+    }
+}
+
+// Global-memory tables for tests too large for shared memory: one slot per CTA.
+template <int kSource>
+__global__ void __launch_bounds__(kThreads) ci_large_kernel(WaveArgs a) {
+    __shared__ TestDesc td;
+    __shared__ int s_idx;
+    __shared__ Partial scratch[kWarps];
+    const int tid = threadIdx.x;
+    int *ws = a.large_ws + (int64_t)blockIdx.x * a.large_stride;
+    const int64_t nvec = a.S >> 4;
+    for (;;) {
+        if (tid == 0) s_idx = atomicAdd(&a.counters[2], 1);
+        __syncthreads();
+        const int idx = s_idx;
+        if (idx >= a.counters[1]) break;
+        const int item = a.large_list[idx];
+        if (tid == 0) build_desc<kSource>(a, item, td);
+        __syncthreads();
+        int *tab = ws;
+        int *ni = tab + td.cells;
+        int *nj = ni + td.dz * td.dx;
+        int *nk = nj + td.dz * td.dy;
+        const int64_t tot = td.cells + td.dz * (td.dx + td.dy + 1);
+        for (int64_t i = tid; i < tot; i += kThreads) tab[i] = 0;
+        __syncthreads();
+        count_range<true>(td, 0, nvec, true, a.S, tab, tid, kThreads);
+        __threadfence_block();
+        __syncthreads();
+        Verdict v = score_table(td, tab, ni, nj, nk, a.alpha, scratch, tid, kThreads);
+        if (tid == 0) record_verdict(a, item, td, v, tab, 1);
+        __syncthreads();
+    }
+}
+
+// ---- plain: one test, whole grid, one launch
+struct PlainArgs {
+    const uint8_t *cols;
+    int64_t S, S_pad;
+    const uint8_t *card;
+    int32_t x, y, d;
+    int32_t z[kMaxCond];
+    double alpha;
+    int32_t want_hash;
+    int32_t *gtab;         // zeroed table + marginals (large_stride ints)
+    int32_t *done;         // ticket counter, reset by the last CTA
+    fpgm_ci_result *out;
+    unsigned long long *stats;
+};
+
+__global__ void __launch_bounds__(kThreads) ci_plain_kernel(PlainArgs p) {
+    extern __shared__ int smem[];
+    __shared__ TestDesc td;
+    __shared__ Partial scratch[kWarps];
+    __shared__ int s_last;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        td.x = p.x;
+        td.y = p.y;
+        td.d = p.d;
+        for (int k = 0; k < p.d; ++k) td.z[k] = p.z[k];
+        desc_finish(td, p.cols, p.S_pad, p.card, kSmemBudgetInts, kLargeIntsPerSlot);
+    }
+    __syncthreads();
+    if (td.path == 2) {
+        if (blockIdx.x == 0 && tid == 0) {
+            p.out->independent = 0;
+            p.out->path = 2;
+            p.out->cells = td.cells;
+        }
+        return;
+    }
+    const int64_t nvec = p.S >> 4;
+    const int64_t per = (nvec + gridDim.x - 1) / gridDim.x;
+    const int64_t v0 = min(nvec, per * blockIdx.x), v1 = min(nvec, v0 + per);
+    if (td.path == 0) {
+        const int64_t tabn = td.cells * td.R;
+        for (int64_t i = tid; i < tabn; i += kThreads) smem[i] = 0;
+        __syncthreads();
+        count_range<false>(td, v0, v1, blockIdx.x == 0, p.S, smem, tid, kThreads);
+        __syncthreads();
+        const int R = td.R, Rm = R - 1;
+        for (int64_t c = tid; c < td.cells; c += kThreads) {
+            int s = 0;
+            for (int r = 0; r < R; ++r) s += smem[c * R + ((r + (int)c) & Rm)];
+            if (s) atomicAdd(&p.gtab[c], s);
+        }
+    } else {
+        count_range<true>(td, v0, v1, blockIdx.x == 0, p.S, p.gtab, tid, kThreads);
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(p.done, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    int *ct = p.gtab;
+    int *ni = ct + td.cells;
+    int *nj = ni + td.dz * td.dx;
+    int *nk = nj + td.dz * td.dy;
+    Verdict v = score_table(td, ct, ni, nj, nk, p.alpha, scratch, tid, kThreads);
+    if (tid == 0) {
+        fpgm_ci_result r;
+        r.table_hash = p.want_hash ? table_hash(ct, td.cells) : 0;
+        r.cells = td.cells;
+        r.df = (int32_t)v.df;
+        r.independent = v.indep;
+        r.g2 = v.g2;
+        r.p_value = v.p;
+        r.rechecked = v.rechecked;
+        r.path = td.path;
+        *p.out = r;
+        if (v.rechecked) {
+            atomicAdd(&p.stats[ST_RECHECK], 1ull);
+            if (fabs(v.p - p.alpha) < 1e-12) atomicAdd(&p.stats[ST_NEARTIE], 1ull);
+            atomicMax(&p.stats[ST_MAXDP], (unsigned long long)__double_as_longlong(v.dp));
+        }
+    }
+    __syncthreads();
+    const int64_t tot = td.cells + td.dz * (td.dx + td.dy + 1);
+    for (int64_t i = tid; i < tot; i += kThreads) ct[i] = 0;
+    if (tid == 0) *p.done = 0;
+}
+
+// ---- data preparation
+// First-appearance ids per column (Dataset.cpp:459-467) and observed cardinality.
+__global__ void relabel_kernel(uint8_t *cols, int64_t S, int64_t S_pad, uint8_t *card, int relabel) {
+    __shared__ unsigned first[256];
+    __shared__ uint8_t map[256];
+    __shared__ unsigned s_max;
+    uint8_t *c = cols + (int64_t)blockIdx.x * S_pad;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) first[i] = 0xffffffffu;
+    if (threadIdx.x == 0) s_max = 0;
+    __syncthreads();
+    if (relabel) {
+        for (int64_t s = threadIdx.x; s < S; s += blockDim.x) {
+            unsigned v = c[s];
+            if ((unsigned)s < first[v]) atomicMin(&first[v], (unsigned)s);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int next = 0;
+            // values sorted by first appearance: repeated min-selection over <= 256 values
+            bool used[256];
+            for (int i = 0; i < 256; ++i) used[i] = first[i] == 0xffffffffu;
+            for (;;) {
+                int best = -1;
+                unsigned bp = 0xffffffffu;
+                for (int i = 0; i < 256; ++i)
+                    if (!used[i] && first[i] < bp) { bp = first[i]; best = i; }
+                if (best < 0) break;
+                used[best] = true;
+                map[best] = (uint8_t)next++;
+            }
+            card[blockIdx.x] = (uint8_t)next;
+        }
+        __syncthreads();
+        for (int64_t s = threadIdx.x; s < S; s += blockDim.x) c[s] = map[c[s]];
+    } else {
+        for (int64_t s = threadIdx.x; s < S; s += blockDim.x) atomicMax(&s_max, (unsigned)c[s]);
+        __syncthreads();
+        if (threadIdx.x == 0) card[blockIdx.x] = (uint8_t)(s_max + 1);
+    }
+}
+
+// ---- level machinery
+__global__ void init_bits_kernel(uint32_t *bits, int n, int W) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= (int64_t)n * W) return;
+    int v = (int)(i / W), w = (int)(i % W);
+    uint32_t m = 0xffffffffu;
+    int lo = w * 32;
+    if (lo + 32 > n) m = (n - lo) >= 32 ? 0xffffffffu : ((1u << (n - lo)) - 1u);
+    if (v >= lo && v < lo + 32) m &= ~(1u << (v - lo));
+    bits[i] = m;
+}
+
+// all pairs i<j in complete-graph order (Network.cpp:270-283)
+__global__ void level0_edges_kernel(int n, int32_t *ex, int32_t *ey, int32_t *pxy, int32_t *pyx, uint64_t *cntx,
+                                    uint64_t *total, uint64_t *next, uint8_t *status) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t E = (int64_t)n * (n - 1) / 2;
+    if (e >= E) return;
+    // row i: first index base(i) = i*(2n-i-1)/2
+    double nn = 2.0 * n - 1.0;
+    int i = (int)floor((nn - sqrt(nn * nn - 8.0 * (double)e)) / 2.0);
+    if (i < 0) i = 0;
+    while (i > 0 && (int64_t)i * (2 * n - i - 1) / 2 > e) --i;
+    while ((int64_t)(i + 1) * (2 * n - i - 2) / 2 <= e) ++i;
+    int64_t base = (int64_t)i * (2 * n - i - 1) / 2;
+    int j = (int)(e - base) + i + 1;
+    ex[e] = i;
+    ey[e] = j;
+    pxy[e] = 0;
+    pyx[e] = 0;
+    cntx[e] = 1;
+    total[e] = 1;
+    next[e] = 0;
+    status[e] = kStatusActive;
+}
+
+// sorted neighbour lists from the bitset (the level snapshot)
+__global__ void csr_kernel(const uint32_t *bits, int n, int W, int32_t *adjl, int stride, int32_t *deg,
+                           int32_t *node_cnt) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    int k = 0, higher = 0;
+    const uint32_t *row = bits + (int64_t)v * W;
+    int32_t *L = adjl + (int64_t)v * stride;
+    for (int w = 0; w < W; ++w) {
+        uint32_t m = row[w];
+        while (m) {
+            int b = __ffs(m) - 1;
+            m &= m - 1;
+            int u = w * 32 + b;
+            L[k++] = u;
+            higher += u > v;
+        }
+    }
+    deg[v] = k;
+    node_cnt[v] = higher;
+}
+
+__device__ inline int find_pos(const int32_t *L, int len, int u) {
+    int lo = 0, hi = len;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (L[mid] < u) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ inline uint64_t sat_binom(const uint64_t *btab, int na, int d, unsigned long long *unsup) {
+    if (na < d) return 0;
+    if (na >= kBinomN) {
+        atomicAdd(unsup, 1ull);
+        return 0;
+    }
+    uint64_t c = btab[(int64_t)na * kBinomK + d];
+    if (c == ~0ull) {
+        atomicAdd(unsup, 1ull);
+        return 0;
+    }
+    return c;
+}
+
+__global__ void level_edges_kernel(int n, int d, const int32_t *adjl, int stride, const int32_t *deg,
+                                   const int32_t *node_off, const uint64_t *btab, int32_t *ex, int32_t *ey,
+                                   int32_t *pxy, int32_t *pyx, uint64_t *cntx, uint64_t *total, uint64_t *next,
+                                   uint8_t *status, unsigned long long *stats) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const int32_t *L = adjl + (int64_t)v * stride;
+    int dv = deg[v];
+    int64_t o = node_off[v];
+    int start = find_pos(L, dv, v + 1);
+    for (int k = start; k < dv; ++k, ++o) {
+        int u = L[k];
+        const int32_t *Lu = adjl + (int64_t)u * stride;
+        ex[o] = v;
+        ey[o] = u;
+        pxy[o] = k;
+        pyx[o] = find_pos(Lu, deg[u], v);
+        uint64_t cx = sat_binom(btab, dv - 1, d, &stats[ST_UNSUPPORTED]);
+        uint64_t cy = sat_binom(btab, deg[u] - 1, d, &stats[ST_UNSUPPORTED]);
+        cntx[o] = cx;
+        total[o] = cx + cy;
+        next[o] = 0;
+        status[o] = (cx + cy) == 0 ? kStatusKept : kStatusActive;
+    }
+}
+
+__global__ void wave_plan_kernel(int n_edges, const uint8_t *status, const uint64_t *total, const uint64_t *next,
+                                 int q, int32_t *g) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e > n_edges) return;
+    if (e == n_edges) {
+        g[e] = 0;
+        return;
+    }
+    int v = 0;
+    if (status[e] == kStatusActive) {
+        uint64_t rem = total[e] - next[e];
+        v = rem < (uint64_t)q ? (int)rem : q;
+    }
+    g[e] = v;
+}
+
+__global__ void wave_reduce_kernel(int n_edges, const int32_t *off, const uint8_t *flag, uint8_t *status,
+                                   uint64_t *next, const uint64_t *total, uint64_t *seprank,
+                                   unsigned long long *stats) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_edges) return;
+    const int o = off[e], g = off[e + 1] - o;
+    if (g == 0) return;
+    int first = -1;
+    bool bad = false;
+    for (int k = 0; k < g; ++k) {
+        uint8_t f = flag[o + k];
+        if (f == 2) bad = true;
+        if (f == 1) {
+            first = k;
+            break;
+        }
+    }
+    if (bad) atomicAdd(&stats[ST_UNSUPPORTED], 1ull);
+    atomicAdd(&stats[ST_EXEC], (unsigned long long)g);
+    if (first >= 0) {
+        status[e] = kStatusRemoved;
+        seprank[e] = next[e] + first;
+        atomicAdd(&stats[ST_DET], (unsigned long long)(first + 1));
+    } else {
+        uint64_t nx = next[e] + g;
+        next[e] = nx;
+        atomicAdd(&stats[ST_DET], (unsigned long long)g);
+        if (nx == total[e]) status[e] = kStatusKept;
+        else atomicAdd(&stats[ST_UNRESOLVED], 1ull);
+    }
+}
+
+// apply removals, log (pair, sepset) -- sepset rebuilt from its rank
+__global__ void level_finalize_kernel(int n_edges, int d, int W, const int32_t *ex, const int32_t *ey,
+                                      const int32_t *pxy, const int32_t *pyx, const uint64_t *cntx,
+                                      const uint64_t *seprank, const uint8_t *status, const int32_t *adjl,
+                                      int stride, const int32_t *deg, const uint64_t *btab, uint32_t *bits,
+                                      int32_t *log_pair, int32_t *log_meta, int32_t *log_vars, int64_t log_base,
+                                      int64_t var_base, unsigned long long *stats) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_edges) return;
+    if (status[e] != kStatusRemoved) return;
+    const int x = ex[e], y = ey[e];
+    atomicAnd(&bits[(int64_t)x * W + (y >> 5)], ~(1u << (y & 31)));
+    atomicAnd(&bits[(int64_t)y * W + (x >> 5)], ~(1u << (x & 31)));
+    const int64_t slot = (int64_t)atomicAdd(&stats[ST_REMOVED], 1ull);
+    log_pair[2 * (log_base + slot)] = x;
+    log_pair[2 * (log_base + slot) + 1] = y;
+    log_meta[2 * (log_base + slot)] = d;
+    log_meta[2 * (log_base + slot) + 1] = (int32_t)(var_base + slot * d);  // fits: checked by host
+    if (d == 0) return;
+    uint64_t rank = seprank[e];
+    int side_node, skip;
+    if (rank < cntx[e]) {
+        side_node = x;
+        skip = pxy[e];
+    } else {
+        rank -= cntx[e];
+        side_node = y;
+        skip = pyx[e];
+    }
+    int c[kMaxCond];
+    unrank_lex(btab, deg[side_node] - 1, d, rank, c);
+    const int32_t *L = adjl + (int64_t)side_node * stride;
+    for (int k = 0; k < d; ++k) log_vars[var_base + slot * d + k] = L[c[k] < skip ? c[k] : c[k] + 1];
+}
+
+__global__ void degree_kernel(const uint32_t *bits, int n, int W, unsigned long long *stats) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    int dg = 0;
+    for (int w = 0; w < W; ++w) dg += __popc(bits[(int64_t)v * W + w]);
+    atomicMax(&stats[ST_MAXDEG], (unsigned long long)dg);
+}
+
+inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+// ------------------------------------------------------------------ engine setup
+extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
+    if (!out) return set_error(FPGM_ERR_INVALID, "fpgm_engine_create: out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    CK(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev)
+        return set_error(FPGM_ERR_INVALID, "fpgm_engine_create: device %d out of range (%d devices)", device, ndev);
+    CK(cudaSetDevice(device));
+    fpgm_engine *e = new fpgm_engine();
+    e->device = device;
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, device));
+    e->num_sms = prop.multiProcessorCount;
+    CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&e->ev0));
+    CK(cudaEventCreate(&e->ev1));
+    CK(cudaFuncSetAttribute(ci_kernel<SRC_WAVE>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    CK(cudaFuncSetAttribute(ci_kernel<SRC_EXPLICIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    CK(cudaFuncSetAttribute(ci_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    int occ = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ci_kernel<SRC_WAVE>, kThreads, kSmemBytes));
+    e->ci_blocks = e->num_sms * std::max(1, occ);
+    // binomial table, saturating
+    std::vector<uint64_t> bt((size_t)kBinomN * kBinomK, 0);
+    for (int n = 0; n < kBinomN; ++n) {
+        bt[(size_t)n * kBinomK] = 1;
+        for (int k = 1; k < kBinomK; ++k) {
+            if (n == 0) continue;
+            uint64_t a = bt[(size_t)(n - 1) * kBinomK + k - 1], b = bt[(size_t)(n - 1) * kBinomK + k];
+            uint64_t s = a + b;
+            bt[(size_t)n * kBinomK + k] = (s < a || a == ~0ull || b == ~0ull) ? ~0ull : s;
+        }
+    }
+    RET(e->btab.ensure(bt.size() * 8));
+    CK(cudaMemcpy(e->btab.p, bt.data(), bt.size() * 8, cudaMemcpyHostToDevice));
+    RET(e->counters.ensure(64));
+    RET(e->stats.ensure(ST_COUNT * 8));
+    *out = e;
+    return FPGM_OK;
+}
+
+extern "C" int fpgm_engine_destroy(fpgm_engine *e) {
+    if (!e) return FPGM_OK;
+    cudaSetDevice(e->device);
+    DevBuf *bufs[] = {&e->cols, &e->card, &e->btab, &e->bits, &e->deg, &e->adjl, &e->edges_x, &e->edges_y,
+                      &e->pxy, &e->pyx, &e->cntx, &e->total, &e->next, &e->status, &e->seprank, &e->g,
+                      &e->off, &e->flag, &e->large_list, &e->counters, &e->stats, &e->scan_tmp, &e->log_pair,
+                      &e->log_vars, &e->log_meta, &e->node_cnt, &e->node_off, &e->large_ws, &e->plain_ws,
+                      &e->tests_buf, &e->detail_buf};
+    for (DevBuf *b : bufs) b->release();
+    if (e->ev0) cudaEventDestroy(e->ev0);
+    if (e->ev1) cudaEventDestroy(e->ev1);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return FPGM_OK;
+}
+
+extern "C" int fpgm_dataset_upload(fpgm_engine *e, const uint8_t *columns, int32_t n_vars, int64_t n_samples,
+                                   int32_t relabel, uint8_t *out_card) {
+    if (!e || !columns) return set_error(FPGM_ERR_INVALID, "fpgm_dataset_upload: NULL argument");
+    if (n_vars < 2 || n_vars > 65535)
+        return set_error(FPGM_ERR_INVALID, "fpgm_dataset_upload: n_vars %d outside [2, 65535]", n_vars);
+    if (n_samples < 1 || n_samples > ((int64_t)1 << 31) - 16)
+        return set_error(FPGM_ERR_INVALID, "fpgm_dataset_upload: n_samples %lld outside [1, 2^31-16]",
+                         (long long)n_samples);
+    CK(cudaSetDevice(e->device));
+    e->n = n_vars;
+    e->S = n_samples;
+    e->S_pad = (n_samples + 63) & ~(int64_t)63;
+    e->has_result = false;
+    RET(e->cols.ensure((size_t)e->n * e->S_pad));
+    RET(e->card.ensure(std::max<size_t>(256, (size_t)n_vars)));
+    CK(cudaMemsetAsync(e->cols.p, 0, (size_t)e->n * e->S_pad, e->stream));
+    CK(cudaMemcpy2DAsync(e->cols.p, (size_t)e->S_pad, columns, (size_t)n_samples, (size_t)n_samples, (size_t)n_vars,
+                         cudaMemcpyHostToDevice, e->stream));
+    relabel_kernel<<<n_vars, 256, 0, e->stream>>>(e->cols.as<uint8_t>(), e->S, e->S_pad, e->card.as<uint8_t>(),
+                                                  relabel);
+    CK(cudaGetLastError());
+    e->h_card.resize(n_vars);
+    CK(cudaMemcpyAsync(e->h_card.data(), e->card.p, n_vars, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    if (out_card) memcpy(out_card, e->h_card.data(), n_vars);
+    return FPGM_OK;
+}
+
+extern "C" int fpgm_dataset_download(fpgm_engine *e, uint8_t *columns) {
+    if (!e || !columns) return set_error(FPGM_ERR_INVALID, "fpgm_dataset_download: NULL argument");
+    if (!e->n) return set_error(FPGM_ERR_STATE, "fpgm_dataset_download: no dataset uploaded");
+    CK(cudaSetDevice(e->device));
+    CK(cudaMemcpy2DAsync(columns, (size_t)e->S, e->cols.p, (size_t)e->S_pad, (size_t)e->S, (size_t)e->n,
+                         cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return FPGM_OK;
+}
+
+// ------------------------------------------------------------------ batched skeleton
+namespace {
+
+int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d) {
+    memset(&a, 0, sizeof a);
+    a.cols = e->cols.as<uint8_t>();
+    a.S = e->S;
+    a.S_pad = e->S_pad;
+    a.card = e->card.as<uint8_t>();
+    a.d = d;
+    a.btab = e->btab.as<uint64_t>();
+    a.counters = e->counters.as<int32_t>();
+    a.stats = e->stats.as<unsigned long long>();
+    a.alpha = alpha;
+    a.large_stride = kLargeIntsPerSlot;
+    return FPGM_OK;
+}
+
+// Largest table a level-d test can need, from the largest cardinality.
+int64_t max_table_ints(const std::vector<uint8_t> &card, int d) {
+    int64_t m = 1;
+    for (uint8_t c : card) m = std::max<int64_t>(m, c);
+    int64_t cells = 1;
+    for (int k = 0; k < d + 2; ++k) {
+        cells *= m;
+        if (cells > ((int64_t)1 << 40)) return (int64_t)1 << 40;
+    }
+    return cells + cells / 2 + cells / m * 2;
+}
+
+int run_waves_and_count(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t n_active, fpgm_pc_stats *st,
+                        int level_idx) {
+    (void)alpha;
+    unsigned long long *dstat = e->stats.as<unsigned long long>();
+    // global-memory slots only when a table of this level can outgrow shared memory
+    if (max_table_ints(e->h_card, d) > kSmemBudgetInts) {
+        RET(e->large_ws.ensure((size_t)kLargeSlots * kLargeIntsPerSlot * 4));
+        a.large_ws = e->large_ws.as<int32_t>();
+    }
+    int wave = 0;
+    int64_t unresolved = n_active;
+    size_t scan_bytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, e->g.as<int32_t>(), e->off.as<int32_t>(),
+                                  (int)(n_active + 1), e->stream);
+    RET(e->scan_tmp.ensure(scan_bytes + 16));
+    const int64_t kMaxItems = (int64_t)1 << 24;
+    while (unresolved > 0) {
+        int64_t q = (int64_t)1 << std::min(wave, 12);
+        int64_t target = (int64_t)e->ci_blocks * 8;
+        if (q * unresolved < target) q = std::min<int64_t>(4096, (target + unresolved - 1) / unresolved);
+        if (d == 0) q = 1;
+        q = std::max<int64_t>(1, std::min<int64_t>(q, kMaxItems / std::max<int64_t>(1, n_active)));
+        RET(e->flag.ensure((size_t)std::min<int64_t>(kMaxItems, q * n_active) + 16));
+        wave_plan_kernel<<<blocks_for(n_active + 1, 256), 256, 0, e->stream>>>(
+            (int)n_active, e->status.as<uint8_t>(), e->total.as<uint64_t>(), e->next.as<uint64_t>(), (int)q,
+            e->g.as<int32_t>());
+        CK(cudaGetLastError());
+        size_t sb = e->scan_tmp.bytes;
+        CK(cub::DeviceScan::ExclusiveSum(e->scan_tmp.p, sb, e->g.as<int32_t>(), e->off.as<int32_t>(),
+                                         (int)(n_active + 1), e->stream));
+        CK(cudaMemsetAsync(e->counters.p, 0, 64, e->stream));
+        a.off = e->off.as<int32_t>();
+        a.n_edges = (int32_t)n_active;
+        a.flag = e->flag.as<uint8_t>();
+        a.large_list = e->large_list.as<int32_t>();
+        CK(cudaEventRecord(e->ev0, e->stream));
+        ci_kernel<SRC_WAVE><<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+        CK(cudaGetLastError());
+        if (a.large_ws) {
+            ci_large_kernel<SRC_WAVE><<<kLargeSlots, kThreads, 0, e->stream>>>(a);
+            CK(cudaGetLastError());
+        }
+        CK(cudaEventRecord(e->ev1, e->stream));
+        CK(cudaMemsetAsync(dstat + ST_UNRESOLVED, 0, 8, e->stream));
+        wave_reduce_kernel<<<blocks_for(n_active, 256), 256, 0, e->stream>>>(
+            (int)n_active, e->off.as<int32_t>(), e->flag.as<uint8_t>(), e->status.as<uint8_t>(),
+            e->next.as<uint64_t>(), e->total.as<uint64_t>(), e->seprank.as<uint64_t>(), dstat);
+        CK(cudaGetLastError());
+        unsigned long long hs[ST_COUNT];
+        int32_t T = 0;
+        CK(cudaMemcpyAsync(hs, dstat, sizeof hs, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaMemcpyAsync(&T, e->off.as<int32_t>() + n_active, 4, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+        st->count_ms += ms;
+        st->count_bytes += (double)T * (2.0 + d) * (double)e->S;
+        st->count_launches += 1;
+        if (hs[ST_UNSUPPORTED])
+            return set_error(FPGM_ERR_UNSUPPORTED,
+                             "level %d: %llu CI test(s) need a joint table beyond %lld cells or a candidate "
+                             "count beyond 2^64 (node degree >= %d)",
+                             d, hs[ST_UNSUPPORTED], (long long)kLargeIntsPerSlot, kBinomN);
+        unresolved = (int64_t)hs[ST_UNRESOLVED];
+        ++wave;
+    }
+    st->waves[level_idx] = wave;
+    return FPGM_OK;
+}
+
+int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
+    const int n = e->n;
+    const int W = (n + 31) / 32;
+    const int64_t E = (int64_t)n * (n - 1) / 2;
+    unsigned long long *dstat = e->stats.as<unsigned long long>();
+    CK(cudaMemsetAsync(dstat, 0, ST_COUNT * 8, e->stream));
+    RET(e->bits.ensure((size_t)n * W * 4));
+    init_bits_kernel<<<blocks_for((int64_t)n * W, 256), 256, 0, e->stream>>>(e->bits.as<uint32_t>(), n, W);
+    CK(cudaGetLastError());
+    RET(e->log_pair.ensure((size_t)E * 8 + 16));
+    RET(e->log_meta.ensure((size_t)E * 8 + 16));
+    RET(e->log_vars.ensure((size_t)1 << 20));
+    RET(e->deg.ensure((size_t)n * 4 + 16));
+    RET(e->node_cnt.ensure((size_t)(n + 1) * 4));
+    RET(e->node_off.ensure((size_t)(n + 1) * 4));
+    int64_t log_count = 0, var_count = 0;
+    int max_deg = n - 1;
+    bool more = true;
+    st->n_levels = 0;
+    for (int d = 0; d < depth && d < 64; ++d) {
+        if (d >= 2 && !more) break;
+        auto t0 = std::chrono::steady_clock::now();
+        if (d > kMaxCond)
+            return set_error(FPGM_ERR_UNSUPPORTED, "conditioning sets beyond %d variables are not supported",
+                             kMaxCond);
+        int64_t n_active;
+        int stride = 1;
+        if (d == 0) {
+            n_active = E;
+        } else {
+            stride = std::max(1, max_deg);
+            RET(e->adjl.ensure((size_t)n * stride * 4));
+            csr_kernel<<<blocks_for(n, 128), 128, 0, e->stream>>>(e->bits.as<uint32_t>(), n, W, e->adjl.as<int32_t>(),
+                                                                 stride, e->deg.as<int32_t>(),
+                                                                 e->node_cnt.as<int32_t>());
+            CK(cudaGetLastError());
+            CK(cudaMemsetAsync(e->node_cnt.as<int32_t>() + n, 0, 4, e->stream));
+            size_t sb = 0;
+            cub::DeviceScan::ExclusiveSum(nullptr, sb, e->node_cnt.as<int32_t>(), e->node_off.as<int32_t>(), n + 1,
+                                          e->stream);
+            RET(e->scan_tmp.ensure(sb + 16));
+            sb = e->scan_tmp.bytes;
+            CK(cub::DeviceScan::ExclusiveSum(e->scan_tmp.p, sb, e->node_cnt.as<int32_t>(), e->node_off.as<int32_t>(),
+                                             n + 1, e->stream));
+            int32_t na = 0;
+            CK(cudaMemcpyAsync(&na, e->node_off.as<int32_t>() + n, 4, cudaMemcpyDeviceToHost, e->stream));
+            CK(cudaStreamSynchronize(e->stream));
+            n_active = na;
+        }
+        const size_t ne = (size_t)std::max<int64_t>(n_active, 1) + 1;
+        RET(e->edges_x.ensure(ne * 4));
+        RET(e->edges_y.ensure(ne * 4));
+        RET(e->pxy.ensure(ne * 4));
+        RET(e->pyx.ensure(ne * 4));
+        RET(e->cntx.ensure(ne * 8));
+        RET(e->total.ensure(ne * 8));
+        RET(e->next.ensure(ne * 8));
+        RET(e->seprank.ensure(ne * 8));
+        RET(e->status.ensure(ne));
+        RET(e->g.ensure(ne * 4));
+        RET(e->off.ensure(ne * 4));
+        RET(e->large_list.ensure((size_t)1 << 26));
+        if (n_active > 0) {
+            if (d == 0) {
+                level0_edges_kernel<<<blocks_for(E, 256), 256, 0, e->stream>>>(
+                    n, e->edges_x.as<int32_t>(), e->edges_y.as<int32_t>(), e->pxy.as<int32_t>(),
+                    e->pyx.as<int32_t>(), e->cntx.as<uint64_t>(), e->total.as<uint64_t>(), e->next.as<uint64_t>(),
+                    e->status.as<uint8_t>());
+            } else {
+                level_edges_kernel<<<blocks_for(n, 128), 128, 0, e->stream>>>(
+                    n, d, e->adjl.as<int32_t>(), stride, e->deg.as<int32_t>(), e->node_off.as<int32_t>(),
+                    e->btab.as<uint64_t>(), e->edges_x.as<int32_t>(), e->edges_y.as<int32_t>(), e->pxy.as<int32_t>(),
+                    e->pyx.as<int32_t>(), e->cntx.as<uint64_t>(), e->total.as<uint64_t>(), e->next.as<uint64_t>(),
+                    e->status.as<uint8_t>(), dstat);
+            }
+            CK(cudaGetLastError());
+            CK(cudaMemsetAsync(dstat + ST_DET, 0, 8 * 2, e->stream));
+            WaveArgs a;
+            wave_args_base(e, a, alpha, d);
+            a.adjl = e->adjl.as<int32_t>();
+            a.adj_stride = stride;
+            a.deg = e->deg.as<int32_t>();
+            a.ex = e->edges_x.as<int32_t>();
+            a.ey = e->edges_y.as<int32_t>();
+            a.pxy = e->pxy.as<int32_t>();
+            a.pyx = e->pyx.as<int32_t>();
+            a.cntx = e->cntx.as<uint64_t>();
+            a.next = e->next.as<uint64_t>();
+            RET(run_waves_and_count(e, a, alpha, d, n_active, st, st->n_levels));
+        }
+        // finalize: removals into the bitset and the removal log
+        RET(e->log_vars.ensure((size_t)(var_count + std::max<int64_t>(n_active, 1) * std::max(d, 1)) * 4 + 16, true,
+                               e->stream));
+        if (var_count + n_active * (int64_t)d > INT32_MAX)
+            return set_error(FPGM_ERR_UNSUPPORTED, "separating-set storage beyond 2^31 entries");
+        CK(cudaMemsetAsync(dstat + ST_REMOVED, 0, 16, e->stream));
+        if (n_active > 0) {
+            level_finalize_kernel<<<blocks_for(n_active, 256), 256, 0, e->stream>>>(
+                (int)n_active, d, W, e->edges_x.as<int32_t>(), e->edges_y.as<int32_t>(), e->pxy.as<int32_t>(),
+                e->pyx.as<int32_t>(), e->cntx.as<uint64_t>(), e->seprank.as<uint64_t>(), e->status.as<uint8_t>(),
+                e->adjl.as<int32_t>(), stride, e->deg.as<int32_t>(), e->btab.as<uint64_t>(), e->bits.as<uint32_t>(),
+                e->log_pair.as<int32_t>(), e->log_meta.as<int32_t>(), e->log_vars.as<int32_t>(), log_count, var_count,
+                dstat);
+            CK(cudaGetLastError());
+        }
+        degree_kernel<<<blocks_for(n, 128), 128, 0, e->stream>>>(e->bits.as<uint32_t>(), n, W, dstat);
+        CK(cudaGetLastError());
+        unsigned long long hs[ST_COUNT];
+        CK(cudaMemcpyAsync(hs, dstat, sizeof hs, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        const int64_t removed = (int64_t)hs[ST_REMOVED];
+        log_count += removed;
+        var_count += removed * d;
+        max_deg = (int)hs[ST_MAXDEG];
+        const int li = st->n_levels;
+        st->tests[li] = n_active > 0 ? (int64_t)hs[ST_DET] : 0;
+        st->tests_executed[li] = n_active > 0 ? (int64_t)hs[ST_EXEC] : 0;
+        st->edges_after[li] = (int32_t)(n_active - removed);
+        st->ms[li] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        st->n_levels++;
+        more = (max_deg - 1) > d;  // PCStable.cpp:387 (evaluated after levels >= 1)
+    }
+    // global statistics
+    unsigned long long hs[ST_COUNT];
+    CK(cudaMemcpyAsync(hs, dstat, sizeof hs, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    st->rechecks = (int64_t)hs[ST_RECHECK];
+    st->near_ties = (int64_t)hs[ST_NEARTIE];
+    st->large_tests = (int64_t)hs[ST_LARGE];
+    unsigned long long mdp = hs[ST_MAXDP];
+    double dp;
+    memcpy(&dp, &mdp, 8);
+    st->max_abs_dp = dp;
+    // result: adjacency bitset + removal log
+    std::vector<uint32_t> hb((size_t)n * W);
+    std::vector<int32_t> lp((size_t)log_count * 2 + 2), lm((size_t)log_count * 2 + 2), lv((size_t)var_count + 1);
+    CK(cudaMemcpyAsync(hb.data(), e->bits.p, hb.size() * 4, cudaMemcpyDeviceToHost, e->stream));
+    if (log_count) {
+        CK(cudaMemcpyAsync(lp.data(), e->log_pair.p, (size_t)log_count * 8, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaMemcpyAsync(lm.data(), e->log_meta.p, (size_t)log_count * 8, cudaMemcpyDeviceToHost, e->stream));
+    }
+    if (var_count) CK(cudaMemcpyAsync(lv.data(), e->log_vars.p, (size_t)var_count * 4, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    e->res_adj.assign((size_t)n * n, 0);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) e->res_adj[(size_t)i * n + j] = (hb[(size_t)i * W + (j >> 5)] >> (j & 31)) & 1u;
+    std::vector<int64_t> order((size_t)log_count);
+    for (int64_t i = 0; i < log_count; ++i) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](int64_t p, int64_t q) {
+        return lp[2 * p] != lp[2 * q] ? lp[2 * p] < lp[2 * q] : lp[2 * p + 1] < lp[2 * q + 1];
+    });
+    e->res_removed.resize((size_t)log_count * 2);
+    e->res_off.assign((size_t)log_count + 1, 0);
+    e->res_vars.clear();
+    e->res_vars.reserve((size_t)var_count);
+    for (int64_t k = 0; k < log_count; ++k) {
+        int64_t i = order[k];
+        e->res_removed[2 * k] = lp[2 * i];
+        e->res_removed[2 * k + 1] = lp[2 * i + 1];
+        const int dd = lm[2 * i], vo = lm[2 * i + 1];
+        for (int t = 0; t < dd; ++t) e->res_vars.push_back(lv[(size_t)vo + t]);
+        e->res_off[k + 1] = (int32_t)e->res_vars.size();
+    }
+    return FPGM_OK;
+}
+
+// ------------------------------------------------------------------ plain path
+int plain_grid(const fpgm_engine *e) {
+    int64_t nvec = e->S >> 4;
+    int64_t g = nvec / kThreads;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(g, e->ci_blocks));
+}
+
+int plain_test(fpgm_engine *e, int x, int y, const int *z, int d, double alpha, int want_hash,
+               fpgm_ci_result *out) {
+    if (!e->plain_ws.p) {
+        RET(e->plain_ws.ensure((size_t)kLargeIntsPerSlot * 4 + 64));
+        CK(cudaMemsetAsync(e->plain_ws.p, 0, e->plain_ws.bytes, e->stream));
+        RET(e->detail_buf.ensure(sizeof(fpgm_ci_result) * 64));
+    }
+    PlainArgs p;
+    memset(&p, 0, sizeof p);
+    p.cols = e->cols.as<uint8_t>();
+    p.S = e->S;
+    p.S_pad = e->S_pad;
+    p.card = e->card.as<uint8_t>();
+    p.x = x;
+    p.y = y;
+    p.d = d;
+    for (int k = 0; k < d; ++k) p.z[k] = z[k];
+    p.alpha = alpha;
+    p.want_hash = want_hash;
+    p.gtab = e->plain_ws.as<int32_t>();
+    p.done = reinterpret_cast<int32_t *>(e->plain_ws.as<char>() + (size_t)kLargeIntsPerSlot * 4);
+    p.out = e->detail_buf.as<fpgm_ci_result>();
+    p.stats = e->stats.as<unsigned long long>();
+    ci_plain_kernel<<<plain_grid(e), kThreads, kSmemBytes, e->stream>>>(p);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, p.out, sizeof(fpgm_ci_result), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    if (out->path == 2)
+        return set_error(FPGM_ERR_UNSUPPORTED, "CI test (%d,%d|%d vars) needs a %lld-cell table, beyond %lld", x, y,
+                         d, (long long)out->cells, (long long)kLargeIntsPerSlot);
+    return FPGM_OK;
+}
+
+bool next_combination(std::vector<int> &c, int a, int b) {
+    int i = b - 1;
+    while (i >= 0 && c[i] == a - b + i) --i;
+    if (i < 0) return false;
+    c[i]++;
+    for (int j = i + 1; j < b; ++j) c[j] = c[j - 1] + 1;
+    return true;
+}
+
+int run_plain(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
+    const int n = e->n;
+    unsigned long long *dstat = e->stats.as<unsigned long long>();
+    CK(cudaMemsetAsync(dstat, 0, ST_COUNT * 8, e->stream));
+    std::vector<uint8_t> adj((size_t)n * n, 1);
+    for (int i = 0; i < n; ++i) adj[(size_t)i * n + i] = 0;
+    struct Rem { int a, b; std::vector<int> z; };
+    std::vector<Rem> rem;
+    fpgm_ci_result r;
+    auto t0 = std::chrono::steady_clock::now();
+    int64_t tests = 0;
+    std::vector<std::pair<int, int>> kill;
+    for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j) {
+            RET(plain_test(e, i, j, nullptr, 0, alpha, 0, &r));
+            ++tests;
+            if (r.independent) {
+                kill.push_back({i, j});
+                rem.push_back({i, j, {}});
+            }
+        }
+    for (auto &k : kill) adj[(size_t)k.first * n + k.second] = adj[(size_t)k.second * n + k.first] = 0;
+    int64_t edges = (int64_t)n * (n - 1) / 2 - (int64_t)kill.size();
+    st->n_levels = 1;
+    st->tests[0] = st->tests_executed[0] = tests;
+    st->edges_after[0] = (int32_t)edges;
+    st->ms[0] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    bool more = true;
+    std::vector<uint8_t> snap;
+    std::vector<int> cand, c, z;
+    for (int d = 1; d < depth && d < 64 && more; ++d) {
+        if (d > kMaxCond) return set_error(FPGM_ERR_UNSUPPORTED, "conditioning sets beyond %d variables", kMaxCond);
+        t0 = std::chrono::steady_clock::now();
+        snap = adj;
+        kill.clear();
+        tests = 0;
+        for (int x = 0; x < n; ++x)
+            for (int y = x + 1; y < n; ++y) {
+                if (!snap[(size_t)x * n + y]) continue;
+                bool found = false;
+                for (int side = 0; side < 2 && !found; ++side) {
+                    int a = side == 0 ? x : y, b = side == 0 ? y : x;
+                    cand.clear();
+                    for (int v = 0; v < n; ++v)
+                        if (v != b && snap[(size_t)a * n + v]) cand.push_back(v);
+                    if ((int)cand.size() < d) continue;
+                    c.resize(d);
+                    z.resize(d);
+                    for (int k = 0; k < d; ++k) c[k] = k;
+                    do {
+                        for (int k = 0; k < d; ++k) z[k] = cand[c[k]];
+                        RET(plain_test(e, x, y, z.data(), d, alpha, 0, &r));
+                        ++tests;
+                        if (r.independent) {
+                            found = true;
+                            kill.push_back({x, y});
+                            rem.push_back({x, y, z});
+                            break;
+                        }
+                    } while (next_combination(c, (int)cand.size(), d));
+                }
+            }
+        for (auto &k : kill) adj[(size_t)k.first * n + k.second] = adj[(size_t)k.second * n + k.first] = 0;
+        edges -= (int64_t)kill.size();
+        int maxdeg = 0;
+        for (int i = 0; i < n; ++i) {
+            int dg = 0;
+            for (int j = 0; j < n; ++j) dg += adj[(size_t)i * n + j];
+            maxdeg = std::max(maxdeg, dg);
+        }
+        const int li = st->n_levels;
+        st->tests[li] = st->tests_executed[li] = tests;
+        st->edges_after[li] = (int32_t)edges;
+        st->ms[li] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        st->n_levels++;
+        more = (maxdeg - 1) > d;
+    }
+    unsigned long long hs[ST_COUNT];
+    CK(cudaMemcpyAsync(hs, dstat, sizeof hs, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    st->rechecks = (int64_t)hs[ST_RECHECK];
+    st->near_ties = (int64_t)hs[ST_NEARTIE];
+    unsigned long long mdp = hs[ST_MAXDP];
+    memcpy(&st->max_abs_dp, &mdp, 8);
+    std::sort(rem.begin(), rem.end(), [](const Rem &p, const Rem &q) { return p.a != q.a ? p.a < q.a : p.b < q.b; });
+    e->res_adj = adj;
+    e->res_removed.clear();
+    e->res_off.assign(1, 0);
+    e->res_vars.clear();
+    for (auto &q : rem) {
+        e->res_removed.push_back(q.a);
+        e->res_removed.push_back(q.b);
+        for (int v : q.z) e->res_vars.push_back(v);
+        e->res_off.push_back((int32_t)e->res_vars.size());
+    }
+    return FPGM_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI: tests and skeleton
+extern "C" int fpgm_ci_test(fpgm_engine *e, int32_t x, int32_t y, const int32_t *z, int32_t nz, double alpha,
+                            int32_t want_hash, fpgm_ci_result *out) {
+    if (!e || !out || (nz > 0 && !z)) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test: NULL argument");
+    if (!e->n) return set_error(FPGM_ERR_STATE, "fpgm_ci_test: no dataset uploaded");
+    if (!(alpha >= 0.0 && alpha <= 1.0))
+        return set_error(FPGM_ERR_INVALID, "Error with incorrect significance level alpha!");
+    if (nz < 0 || nz > kMaxCond) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test: |Z| = %d outside [0, %d]", nz, kMaxCond);
+    if (x < 0 || x >= e->n || y < 0 || y >= e->n) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test: variable out of range");
+    for (int k = 0; k < nz; ++k)
+        if (z[k] < 0 || z[k] >= e->n) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test: variable out of range");
+    CK(cudaSetDevice(e->device));
+    return plain_test(e, x, y, z, nz, alpha, want_hash, out);
+}
+
+extern "C" int fpgm_ci_test_batch(fpgm_engine *e, const int32_t *tests, int32_t n_tests, int32_t d, double alpha,
+                                  int32_t want_hash, fpgm_ci_result *out) {
+    if (!e || !out || (n_tests > 0 && !tests)) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_batch: NULL argument");
+    if (!e->n) return set_error(FPGM_ERR_STATE, "fpgm_ci_test_batch: no dataset uploaded");
+    if (!(alpha >= 0.0 && alpha <= 1.0))
+        return set_error(FPGM_ERR_INVALID, "Error with incorrect significance level alpha!");
+    if (d < 0 || d > kMaxCond) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_batch: d = %d outside [0, %d]", d, kMaxCond);
+    if (n_tests < 0 || n_tests > (1 << 26)) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_batch: n_tests out of range");
+    if (n_tests == 0) return FPGM_OK;
+    for (int64_t i = 0; i < (int64_t)n_tests * (2 + d); ++i)
+        if (tests[i] < 0 || tests[i] >= e->n) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_batch: variable out of range");
+    CK(cudaSetDevice(e->device));
+    RET(e->tests_buf.ensure((size_t)n_tests * (2 + d) * 4));
+    RET(e->detail_buf.ensure((size_t)n_tests * sizeof(fpgm_ci_result)));
+    RET(e->flag.ensure((size_t)n_tests + 16));
+    RET(e->large_list.ensure((size_t)n_tests * 4 + 16));
+    CK(cudaMemcpyAsync(e->tests_buf.p, tests, (size_t)n_tests * (2 + d) * 4, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemsetAsync(e->counters.p, 0, 64, e->stream));
+    CK(cudaMemsetAsync(e->stats.p, 0, ST_COUNT * 8, e->stream));
+    WaveArgs a;
+    wave_args_base(e, a, alpha, d);
+    a.tests = e->tests_buf.as<int32_t>();
+    a.n_tests = n_tests;
+    a.flag = e->flag.as<uint8_t>();
+    a.detail = e->detail_buf.as<fpgm_ci_result>();
+    a.want_hash = want_hash;
+    a.large_list = e->large_list.as<int32_t>();
+    if (max_table_ints(e->h_card, d) > kSmemBudgetInts) {
+        RET(e->large_ws.ensure((size_t)kLargeSlots * kLargeIntsPerSlot * 4));
+        a.large_ws = e->large_ws.as<int32_t>();
+    }
+    ci_kernel<SRC_EXPLICIT><<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+    CK(cudaGetLastError());
+    if (a.large_ws) {
+        ci_large_kernel<SRC_EXPLICIT><<<kLargeSlots, kThreads, 0, e->stream>>>(a);
+        CK(cudaGetLastError());
+    }
+    unsigned long long hs[ST_COUNT];
+    CK(cudaMemcpyAsync(out, a.detail, (size_t)n_tests * sizeof(fpgm_ci_result), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaMemcpyAsync(hs, e->stats.p, sizeof hs, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    if (hs[ST_UNSUPPORTED])
+        return set_error(FPGM_ERR_UNSUPPORTED, "%llu CI test(s) need a joint table beyond %lld cells",
+                         hs[ST_UNSUPPORTED], (long long)kLargeIntsPerSlot);
+    return FPGM_OK;
+}
+
+extern "C" int fpgm_pc_skeleton(fpgm_engine *e, double alpha, int32_t depth, int32_t mode, fpgm_pc_stats *stats) {
+    if (!e) return set_error(FPGM_ERR_INVALID, "fpgm_pc_skeleton: NULL engine");
+    if (!e->n) return set_error(FPGM_ERR_STATE, "fpgm_pc_skeleton: no dataset uploaded");
+    if (!(alpha >= 0.0 && alpha <= 1.0))
+        return set_error(FPGM_ERR_INVALID, "Error with incorrect significance level alpha!");
+    if (mode != FPGM_MODE_BATCHED && mode != FPGM_MODE_PLAIN)
+        return set_error(FPGM_ERR_INVALID, "fpgm_pc_skeleton: unknown mode %d", mode);
+    if (e->n > 16384 && mode == FPGM_MODE_BATCHED)
+        return set_error(FPGM_ERR_UNSUPPORTED, "fpgm_pc_skeleton: %d nodes exceed the 16384-node limit", e->n);
+    CK(cudaSetDevice(e->device));
+    fpgm_pc_stats local;
+    fpgm_pc_stats *st = stats ? stats : &local;
+    memset(st, 0, sizeof *st);
+    e->has_result = false;
+    auto t0 = std::chrono::steady_clock::now();
+    int rc = mode == FPGM_MODE_BATCHED ? run_batched(e, alpha, depth, st) : run_plain(e, alpha, depth, st);
+    st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (rc == FPGM_OK) e->has_result = true;
+    return rc;
+}
+
+extern "C" int fpgm_pc_result_sizes(fpgm_engine *e, int32_t *n_nodes, int32_t *n_removed, int64_t *n_sep_vars) {
+    if (!e) return set_error(FPGM_ERR_INVALID, "fpgm_pc_result_sizes: NULL engine");
+    if (!e->has_result) return set_error(FPGM_ERR_STATE, "fpgm_pc_result_sizes: no skeleton result");
+    if (n_nodes) *n_nodes = e->n;
+    if (n_removed) *n_removed = (int32_t)(e->res_removed.size() / 2);
+    if (n_sep_vars) *n_sep_vars = (int64_t)e->res_vars.size();
+    return FPGM_OK;
+}
+
+extern "C" int fpgm_pc_result_fetch(fpgm_engine *e, uint8_t *adj, int32_t *removed, int32_t *sep_offsets,
+                                    int32_t *sep_vars) {
+    if (!e) return set_error(FPGM_ERR_INVALID, "fpgm_pc_result_fetch: NULL engine");
+    if (!e->has_result) return set_error(FPGM_ERR_STATE, "fpgm_pc_result_fetch: no skeleton result");
+    if (adj) memcpy(adj, e->res_adj.data(), e->res_adj.size());
+    if (removed && !e->res_removed.empty()) memcpy(removed, e->res_removed.data(), e->res_removed.size() * 4);
+    if (sep_offsets) memcpy(sep_offsets, e->res_off.data(), e->res_off.size() * 4);
+    if (sep_vars && !e->res_vars.empty()) memcpy(sep_vars, e->res_vars.data(), e->res_vars.size() * 4);
+    return FPGM_OK;
+}

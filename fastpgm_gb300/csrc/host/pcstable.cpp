@@ -1,0 +1,476 @@
+// C++ drop-in for the reference's PC-stable structure-learning classes and
+// the BNSL_PCStable job, driving the GPU engine through the C ABI.
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <mutex>
+#include <queue>
+#include <random>
+
+#include "fastpgm_gb300.h"
+#include "fastpgm_gb300_cxx.h"
+#include "orient.h"
+#include "../engine_internal.h"
+
+using std::cout;
+using std::endl;
+using std::string;
+using std::vector;
+
+// ------------------------------------------------------------------ Node / Edge / Network
+Node::Node(int index) : Node(index, std::to_string(index)) {}
+Node::Node(int index, string name) : node_index(index), node_name(std::move(name)) {}
+
+Edge::Edge(Node *n1, Node *n2, EndPoint e1, EndPoint e2) : node1(n1), node2(n2), end_point1(e1), end_point2(e2) {}
+
+Edge::Edge(Node *n1, Node *n2) {  // Edge.cpp:17-34
+    if (n1->GetNodeIndex() < n2->GetNodeIndex()) {
+        node1 = n1;
+        node2 = n2;
+    } else {
+        node1 = n2;
+        node2 = n1;
+    }
+    end_point1 = end_point2 = TAIL;
+}
+
+Network::Network() : Network(true) {}
+Network::Network(bool pure_disc) : pure_discrete(pure_disc) {}
+Network::~Network() {
+    for (auto &kv : map_idx_node_ptr) delete kv.second;
+}
+
+Node *Network::FindNodePtrByIndex(const int &index) const {
+    if (index < 0 || index >= num_nodes) {
+        fprintf(stderr, "Error in function %s! \nInvalid index [%d]!", __FUNCTION__, index);
+        exit(1);
+    }
+    return map_idx_node_ptr.at(index);
+}
+
+std::set<int> Network::GetParentIdxesOfNode(int node_index) { return FindNodePtrByIndex(node_index)->set_parent_indexes; }
+std::set<int> Network::GetChildrenIdxesOfNode(int node_index) { return FindNodePtrByIndex(node_index)->set_children_indexes; }
+
+std::vector<int> Network::GetTopoOrd() {  // Network.cpp:371-411 + common.cpp TopoSortOfDAGZeroInDegreeFirst
+    if (!topo_ord.empty()) return topo_ord;
+    vector<int> indeg(num_nodes, 0);
+    for (int v = 0; v < num_nodes; ++v)
+        for (int c : FindNodePtrByIndex(v)->set_children_indexes) indeg[c]++;
+    std::queue<int> q;
+    for (int i = 0; i < num_nodes; ++i)
+        if (indeg[i] == 0) q.push(i);
+    while (!q.empty()) {
+        int u = q.front();
+        for (int c : FindNodePtrByIndex(u)->set_children_indexes)
+            if (--indeg[c] == 0) q.push(c);
+        topo_ord.push_back(u);
+        q.pop();
+    }
+    return topo_ord;
+}
+
+void Network::PrintEdges() {
+    for (int i = 0; i < num_edges && i < (int)vec_edges.size(); ++i) {
+        Edge &e = vec_edges[i];
+        cout << i << ": ";
+        if (!e.IsDirected())
+            cout << e.node1->node_name << " (" << e.node1->GetNodeIndex() << ") -- " << e.node2->node_name << " ("
+                 << e.node2->GetNodeIndex() << ")" << endl;
+        else if (e.end_point1 == TAIL)
+            cout << e.node1->node_name << " (" << e.node1->GetNodeIndex() << ") -> " << e.node2->node_name << " ("
+                 << e.node2->GetNodeIndex() << ")" << endl;
+        else
+            cout << e.node2->node_name << " (" << e.node2->GetNodeIndex() << ") -> " << e.node1->node_name << " ("
+                 << e.node1->GetNodeIndex() << ")" << endl;
+    }
+    cout << "num nodes = " << num_nodes << endl << "num edges = " << num_edges << endl;
+}
+
+// ------------------------------------------------------------------ Dataset
+namespace {
+string trim_right(string s) {  // common.cpp TrimRight
+    while (!s.empty() && (unsigned char)s.back() < 33) s.pop_back();
+    return s;
+}
+vector<string> split_commas(const string &s) {  // common.cpp Split
+    vector<string> r;
+    size_t b = 0, e;
+    while ((e = s.find(',', b)) != string::npos) {
+        r.push_back(s.substr(b, e - b));
+        b = e + 1;
+    }
+    r.push_back(s.substr(b));
+    return r;
+}
+}  // namespace
+
+void Dataset::LoadCSVTrainingData(string data_file_path, bool str_val, int cls_var_id, std::set<int> cont_vars) {
+    std::ifstream in(data_file_path);
+    if (!in.is_open()) {
+        fprintf(stderr, "Error in function %s!", __FUNCTION__);
+        fprintf(stderr, "Unable to open file %s!", data_file_path.c_str());
+        exit(1);
+    }
+    if (!cont_vars.empty()) {
+        fprintf(stderr, "Error in function %s!\nContinuous variables are not supported by the GPU PC-stable path.",
+                __FUNCTION__);
+        exit(1);
+    }
+    class_var_index = cls_var_id;
+    string line;
+    std::getline(in, line);
+    line = trim_right(line);
+    vec_var_names = split_commas(line);
+    num_vars = (int)vec_var_names.size();
+    if (std::set<string>(vec_var_names.begin(), vec_var_names.end()).size() != vec_var_names.size()) {
+        fprintf(stderr, "Error in function [%s]\nDuplicate variable names in header!", __FUNCTION__);
+        exit(1);
+    }
+    vars_possible_values_ids.assign(num_vars, {});
+    vector<vector<unsigned char>> cols(num_vars);
+    while (std::getline(in, line)) {
+        line = trim_right(line);
+        if (line.empty()) continue;
+        vector<string> f = split_commas(line);
+        if ((int)f.size() < num_vars) {
+            fprintf(stderr, "Error in function %s!\nRow %zu has %zu fields, expected %d.", __FUNCTION__,
+                    cols[0].size() + 2, f.size(), num_vars);
+            exit(1);
+        }
+        for (int v = 0; v < num_vars; ++v) {
+            int id;
+            if (str_val) {  // ids by first appearance (Dataset.cpp:459-467)
+                auto &m = vars_possible_values_ids[v];
+                auto it = m.find(f[v]);
+                if (it == m.end()) {
+                    id = (int)m.size();
+                    m.emplace(f[v], id);
+                } else {
+                    id = it->second;
+                }
+            } else {
+                id = std::stoi(f[v]);
+                vars_possible_values_ids[v].emplace(f[v], id);
+            }
+            if (id < 0 || id > 254) {
+                fprintf(stderr, "Error in function %s!\nVariable %s has more than 255 states; the GPU engine "
+                        "stores states as uint8.", __FUNCTION__, vec_var_names[v].c_str());
+                exit(1);
+            }
+            cols[v].push_back((unsigned char)id);
+        }
+    }
+    num_instance = num_vars ? (int)cols[0].size() : 0;
+    num_of_possible_values_of_disc_vars.resize(num_vars);
+    columns.resize((size_t)num_vars * num_instance);
+    for (int v = 0; v < num_vars; ++v) {
+        num_of_possible_values_of_disc_vars[v] = (int)vars_possible_values_ids[v].size();
+        std::copy(cols[v].begin(), cols[v].end(), columns.begin() + (size_t)v * num_instance);
+    }
+    cout << "Finish loading training data. Number of instances: " << num_instance
+         << ". Number of variables: " << num_vars << "." << endl;
+}
+
+// ------------------------------------------------------------------ StructureLearning
+void StructureLearning::AssignNodeInformation(Dataset *dts) {  // StructureLearning.cpp:11-34
+    network->num_nodes = dts->num_vars;
+    for (int i = 0; i < network->num_nodes; ++i) {
+        Node *node = new Node(i);
+        if ((int)dts->vec_var_names.size() == network->num_nodes) node->node_name = dts->vec_var_names[i];
+        node->possible_values_ids = dts->vars_possible_values_ids[i];
+        node->SetDomainSize(dts->num_of_possible_values_of_disc_vars[i]);
+        auto it = network->map_idx_node_ptr.find(i);
+        if (it != network->map_idx_node_ptr.end()) delete it->second;
+        network->map_idx_node_ptr[i] = node;
+    }
+}
+
+bool StructureLearning::Direct(int a, int c) {  // StructureLearning.cpp:73-84, on the Network records
+    Node *pa = network->FindNodePtrByIndex(a), *pc = network->FindNodePtrByIndex(c);
+    if (pa->set_children_indexes.count(c) == 0) {
+        // refuse an arc that would close a directed cycle
+        vector<int> st{c};
+        std::set<int> seen{c};
+        while (!st.empty()) {
+            int u = st.back();
+            st.pop_back();
+            if (u == a) return false;
+            for (int w : network->FindNodePtrByIndex(u)->set_children_indexes)
+                if (seen.insert(w).second) st.push_back(w);
+        }
+        pa->set_children_indexes.insert(c);
+        pc->set_parent_indexes.insert(a);
+    }
+    network->vec_edges.push_back(Edge(pa, pc, TAIL, ARROW));
+    Edge und(pa, pc);
+    auto it = std::find(network->vec_edges.begin(), network->vec_edges.end(), und);
+    if (it != network->vec_edges.end()) network->vec_edges.erase(it);
+    return true;
+}
+
+vector<int> StructureLearning::FindRootsInDAGForest() {  // StructureLearning.cpp:151-206
+    vector<int> roots;
+    const int n = network->num_nodes;
+    vector<bool> visited(n, false);
+    vector<int> indeg(n);
+    for (int i = 0; i < n; ++i) indeg[i] = (int)network->GetParentIdxesOfNode(i).size();
+    for (;;) {
+        int best = -1, root = -1;
+        for (int i = 0; i < n; ++i)
+            if (indeg[i] == 0 && !visited[i]) {
+                int nc = (int)network->GetChildrenIdxesOfNode(i).size();
+                if (nc > best) {
+                    best = nc;
+                    root = i;
+                }
+            }
+        if (best == -1) break;
+        visited[root] = true;
+        roots.push_back(root);
+        std::queue<int> q;
+        q.push(root);
+        while (!q.empty()) {
+            int cur = q.front();
+            q.pop();
+            for (int c : network->GetChildrenIdxesOfNode(cur))
+                if (!visited[c]) { visited[c] = true; q.push(c); }
+            for (int p : network->GetParentIdxesOfNode(cur))
+                if (!visited[p]) { visited[p] = true; q.push(p); }
+        }
+    }
+    return roots;
+}
+
+void StructureLearning::AddRootNode(vector<int> &sub_roots) {  // StructureLearning.cpp:217-236
+    Node *root = new Node(network->num_nodes, "ROOT");
+    root->possible_values_ids["0"] = 0;
+    root->possible_values_ids["1"] = 1;
+    root->SetDomainSize(2);
+    for (int c : sub_roots) {
+        Node *cp = network->FindNodePtrByIndex(c);
+        root->set_children_indexes.insert(c);
+        cp->set_parent_indexes.insert(root->node_index);
+        network->vec_edges.push_back(Edge(root, cp, TAIL, ARROW));
+        network->num_edges++;
+    }
+    network->map_idx_node_ptr[network->num_nodes] = root;
+    network->num_nodes++;
+}
+
+void StructureLearning::SaveBNStructure(string struct_file) {  // StructureLearning.cpp:238-292
+    std::ofstream out(struct_file);
+    if (!out.is_open()) {
+        fprintf(stderr, "Error in function %s!", __FUNCTION__);
+        fprintf(stderr, "Unable to open file %s!", struct_file.c_str());
+        exit(1);
+    }
+    out << "number of nodes = " << network->num_nodes << ", number of edges = " << network->num_edges << "\n";
+    if (!network->vec_edges.empty() && network->vec_edges[0].IsDirected()) {
+        vector<int> topo = network->GetTopoOrd();
+        int k = 0;
+        for (int t : topo) {
+            Node *tp = network->FindNodePtrByIndex(t);
+            for (int c : tp->set_children_indexes)
+                out << k++ << ": " << tp->node_name << "/v" << t << " -> " << network->FindNodePtrByIndex(c)->node_name
+                    << "/v" << c << "\n";
+        }
+    } else {
+        for (int i = 0; i < network->num_edges && i < (int)network->vec_edges.size(); ++i) {
+            Edge &e = network->vec_edges[i];
+            Node *a = e.GetNode1(), *b = e.GetNode2();
+            out << i << ": ";
+            if (!e.IsDirected())
+                out << a->node_name << "/v" << a->GetNodeIndex() << " -- " << b->node_name << "/v" << b->GetNodeIndex();
+            else if (e.GetEndPoint1() == TAIL)
+                out << a->node_name << "/v" << a->GetNodeIndex() << " -> " << b->node_name << "/v" << b->GetNodeIndex();
+            else
+                out << b->node_name << "/v" << b->GetNodeIndex() << " -> " << a->node_name << "/v" << a->GetNodeIndex();
+            out << "\n";
+        }
+    }
+    cout << "Learned structure has been saved in " << struct_file << endl;
+}
+
+// ------------------------------------------------------------------ PCStable
+namespace {
+std::mutex g_engine_mu;
+fpgm_engine *g_engines[64] = {nullptr};
+
+int shared_engine(int device, fpgm_engine **out) {
+    if (device < 0 || device >= 64) return fpgm::set_error(FPGM_ERR_INVALID, "device %d out of range", device);
+    std::lock_guard<std::mutex> lk(g_engine_mu);
+    if (!g_engines[device]) {
+        int rc = fpgm_engine_create(device, &g_engines[device]);
+        if (rc != FPGM_OK) return rc;
+    }
+    *out = g_engines[device];
+    return FPGM_OK;
+}
+
+void die_on(int rc) {
+    if (rc != FPGM_OK) {
+        fprintf(stderr, "Error: %s\n", fpgm_last_error());
+        exit(1);
+    }
+}
+}  // namespace
+
+PCStable::PCStable(Network *net, double a, int d) : alpha(a) {  // PCStable.cpp:7-12
+    network = net;
+    num_ci_test = 0;
+    depth = d;
+}
+
+PCStable::~PCStable() {  // PCStable.cpp:14-16
+    delete network;
+    network = nullptr;
+}
+
+int PCStable::Run(Dataset *dts, bool dag, bool add_root, bool save_struct, const string &struct_file, int verbose) {
+    if (!(alpha >= 0.0 && alpha <= 1.0))
+        return fpgm::set_error(FPGM_ERR_INVALID, "Function [IndependenceTest]: Error with incorrect significance level alpha!");
+    if (dts->num_vars < 2 || dts->num_instance < 1)
+        return fpgm::set_error(FPGM_ERR_INVALID, "PCStable: the dataset needs at least 2 variables and 1 sample");
+    const auto t0 = std::chrono::steady_clock::now();
+    AssignNodeInformation(dts);
+    const int n = network->num_nodes;
+    fpgm_engine *eng = nullptr;
+    int rc = shared_engine(device, &eng);
+    if (rc != FPGM_OK) return rc;
+    rc = fpgm_dataset_upload(eng, dts->columns.data(), n, dts->num_instance, 0, nullptr);
+    if (rc != FPGM_OK) return rc;
+    if (verbose > 0)
+        cout << "--------------------------------------------------\n"
+             << "Removing edges level by level..." << endl;
+    rc = fpgm_pc_skeleton(eng, alpha, depth, engine_mode, &stats);
+    if (rc != FPGM_OK) return rc;
+    int32_t nn = 0, nr = 0;
+    int64_t nv = 0;
+    fpgm_pc_result_sizes(eng, &nn, &nr, &nv);
+    vector<uint8_t> adj((size_t)n * n);
+    vector<int32_t> removed((size_t)nr * 2 + 2), off((size_t)nr + 1), vars((size_t)nv + 1);
+    fpgm_pc_result_fetch(eng, adj.data(), removed.data(), off.data(), vars.data());
+    int64_t tests = 0;
+    for (int l = 0; l < stats.n_levels; ++l) {
+        tests += stats.tests[l];
+        if (verbose > 0)
+            cout << "Level " << l << "... " << endl
+                 << "# of CI-tests is " << tests << endl
+                 << "# remaining edges = " << stats.edges_after[l] << ", time = " << stats.ms[l] / 1000.0 << endl;
+    }
+    num_ci_test = (int)tests;
+    sepset.clear();
+    for (int k = 0; k < nr; ++k)
+        sepset[{removed[2 * k], removed[2 * k + 1]}] = std::set<int>(vars.begin() + off[k], vars.begin() + off[k + 1]);
+    const auto t1 = std::chrono::steady_clock::now();
+
+    // orientation (PCStable.cpp:240-255)
+    if (verbose > 0)
+        cout << "--------------------------------------------------\n"
+             << "Orienting v-structure and other undirected edges" << endl;
+    fpgm::Orienter o(n, adj.data());
+    for (int k = 0; k < nr; ++k)
+        o.set_sepset(removed[2 * k], removed[2 * k + 1], vars.data() + off[k], off[k + 1] - off[k]);
+    o.orient();
+    network->vec_edges.clear();
+    for (auto &kv : network->map_idx_node_ptr) {
+        kv.second->set_parent_indexes.clear();
+        kv.second->set_children_indexes.clear();
+    }
+    for (int v = 0; v < n; ++v)
+        for (int c : o.children(v)) {
+            network->FindNodePtrByIndex(v)->set_children_indexes.insert(c);
+            network->FindNodePtrByIndex(c)->set_parent_indexes.insert(v);
+        }
+    for (const fpgm::EdgeRec &r : o.edges()) {
+        Node *a = network->FindNodePtrByIndex(r.n1), *b = network->FindNodePtrByIndex(r.n2);
+        network->vec_edges.push_back(r.directed ? Edge(a, b, TAIL, ARROW) : Edge(a, b));
+    }
+    network->num_edges = o.num_skeleton_edges();
+    if (dag) {  // StructureLearning.cpp:110-144
+        std::mt19937 gen(std::random_device{}());
+        std::uniform_int_distribution<int> coin(0, 1);
+        for (size_t i = 0; i < network->vec_edges.size();) {
+            Edge &e = network->vec_edges[i];
+            if (e.IsDirected()) break;
+            int x = e.node1->GetNodeIndex(), y = e.node2->GetNodeIndex();
+            bool ok = coin(gen) == 0 ? (Direct(x, y) || Direct(y, x)) : (Direct(y, x) || Direct(x, y));
+            if (!ok) return fpgm::set_error(FPGM_ERR_INVALID, "Error: randomly directing causes loop anyway.");
+        }
+    }
+    const auto t2 = std::chrono::steady_clock::now();
+    if (add_root) {
+        cout << "--------------------------------------------------\n"
+             << "Handling multiple independent sub-graphs...\nFinding roots for sub-graphs and adding the ROOT... "
+             << endl;
+        vector<int> roots = FindRootsInDAGForest();
+        AddRootNode(roots);
+        cout << "roots: ";
+        for (int r : roots) cout << r << ", ";
+        cout << endl;
+    }
+    if (save_struct) SaveBNStructure(struct_file);
+    if (verbose > 0) {
+        const double total = std::chrono::duration<double>(t2 - t0).count();
+        const double skel = std::chrono::duration<double>(t1 - t0).count();
+        cout << "--------------------------------------------------\n"
+             << "# of CI-tests = " << num_ci_test << endl
+             << "pc-stable step 1: " << skel << " s " << endl
+             << " (" << skel / total * 100 << "%)" << endl;
+    }
+    cout << "pc-stable: " << std::chrono::duration<double>(t2 - t0).count() << " s " << endl;
+    return FPGM_OK;
+}
+
+void PCStable::StructLearnCompData(Dataset *dts, int group_size, int num_threads, bool dag, bool add_root,
+                                   bool save_struct, string struct_file, int verbose) {
+    (void)group_size;
+    (void)num_threads;
+    if (verbose > 0)
+        cout << "--------------------------------------------------\n"
+             << "Structure learning with PC-Stable..." << endl;
+    die_on(Run(dts, dag, add_root, save_struct, struct_file, verbose));
+}
+
+// ------------------------------------------------------------------ job API
+namespace {
+int bnsl_impl(int verbose, int n_threads, int group_size, double alpha, const string &ref_net, const string &train_set,
+              bool save_struct) {
+    Dataset *trainer = new Dataset();
+    trainer->LoadCSVTrainingData(train_set, true, 0);
+    Network *network = new Network(true);
+    PCStable *bnsl = new PCStable(network, alpha);
+    (void)group_size;
+    (void)n_threads;
+    if (verbose > 0)
+        cout << "--------------------------------------------------\n"
+             << "Structure learning with PC-Stable..." << endl;
+    int rc = bnsl->Run(trainer, false, false, save_struct, train_set + "_struct", verbose);
+    delete trainer;
+    if (rc == FPGM_OK) {
+        if (!ref_net.empty())
+            cout << "The reference BN comparison (SHD) is not part of the GPU PC-stable engine; skipped." << endl;
+        else
+            cout << "There is no reference BN (ground-truth) provided, comparison (showing accuracy) is skipped."
+                 << endl;
+    }
+    bnsl->network = nullptr;  // the reference deletes the network itself and never deletes bnsl
+    delete network;
+    delete bnsl;
+    return rc;
+}
+}  // namespace
+
+void BNSL_PCStable(int verbose, int n_threads, int group_size, double alpha, string ref_net, string train_set,
+                   bool save_struct) {
+    die_on(bnsl_impl(verbose, n_threads, group_size, alpha, ref_net, train_set, save_struct));
+}
+
+extern "C" int fpgm_bnsl_pcstable(int32_t verbose, int32_t n_threads, int32_t group_size, double alpha,
+                                  const char *ref_net, const char *train_set, int32_t save_struct) {
+    if (!train_set) return fpgm::set_error(FPGM_ERR_INVALID, "fpgm_bnsl_pcstable: train_set is NULL");
+    return bnsl_impl(verbose, n_threads, group_size, alpha, ref_net ? ref_net : "", train_set, save_struct != 0);
+}

@@ -1,0 +1,168 @@
+/*
+ * fastpgm_gb300.h -- C ABI of the GB300 PC-stable CI-testing engine.
+ *
+ * Plain pointers and sizes only; every entry point returns an int status
+ * (FPGM_OK or a negative FPGM_ERR_*), and fpgm_last_error() gives the
+ * calling thread's last message.  The library never exits the process; the
+ * C++ drop-in layer (fastpgm_gb300/csrc/host) maps a failure to the
+ * reference's "message + exit(1)" behaviour.
+ *
+ * Reference interfaces each group replaces (paths inside the FastPGM tree):
+ *   fpgm_dataset_upload   Dataset::LoadCSVTrainingData id assignment and
+ *                         RowMajor2ColumnMajor (src/fastpgm/Dataset.cpp:389-503,
+ *                         :459-467, :846-857): column-major data + observed
+ *                         cardinalities (include/fastpgm/Dataset.h:29-32)
+ *   fpgm_ci_test(_batch)  IndependenceTest::IndependenceResult with the
+ *                         "g square" metric (structure_learning/IndependenceTest.cpp:35-58,
+ *                         :65-155, :295-364) over Counts2D/Counts3D tables
+ *                         (structure_learning/CellTable.cpp:23-72, :226-291, :430-455)
+ *   fpgm_pc_skeleton      PCStable::StructLearnByPCStable levels 0..depth-1
+ *                         (structure_learning/PCStable.cpp:84-231) with
+ *                         SearchAtDepth/CheckEdge/Testing/FreeDegree
+ *                         (:265-388, :399-494, :526-614, :620-626)
+ *   fpgm_pc_result_*      PCStable::sepset and the skeleton adjacency the
+ *                         reference keeps in `adjacencies` (PCStable.h:72, PCStable.cpp:118-127)
+ *   fpgm_orient_cpdag     PCStable::OrientVStructure / OrientImplied / Rule1-3
+ *                         (PCStable.cpp:639-847) with Network edge bookkeeping
+ *                         (src/fastpgm/Network.cpp:169-268, :515-545)
+ *   fpgm_bnsl_pcstable    BNSL_PCStable (src/fastpgm/fastpgm_api/fastpgm_api.cpp:18-44,
+ *                         include/fastpgm/fastpgm_api/fastpgm_api.h:23-25)
+ *   fpgm_generate_network SampleSetGenerator forward sampling
+ *                         (src/fastpgm/SampleSetGenerator.cpp), made seedable
+ */
+#ifndef FASTPGM_GB300_H
+#define FASTPGM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    FPGM_OK = 0,
+    FPGM_ERR_INVALID = -1,      /* bad argument (the reference prints and exits) */
+    FPGM_ERR_OOM = -2,          /* device or host allocation failed */
+    FPGM_ERR_CUDA = -3,         /* CUDA runtime error */
+    FPGM_ERR_TIMEOUT = -4,      /* a bounded device wait gave up */
+    FPGM_ERR_IO = -5,           /* file could not be opened / written */
+    FPGM_ERR_UNSUPPORTED = -6,  /* input outside the engine's limits (message says which) */
+    FPGM_ERR_STATE = -7         /* call out of order (e.g. no dataset uploaded) */
+};
+
+enum { FPGM_MODE_BATCHED = 0, FPGM_MODE_PLAIN = 1 };
+
+/* Largest conditioning-set size the engine accepts. */
+#define FPGM_MAX_COND 30
+
+typedef struct fpgm_engine fpgm_engine;
+
+typedef struct {
+    uint64_t table_hash;   /* FNV-1a-64 of the int32 joint table n[z][x][y] in reference cell order (0 if not asked) */
+    int64_t cells;         /* dz * dx * dy */
+    int32_t df;            /* adjusted degrees of freedom (IndependenceTest.cpp:96-111) */
+    int32_t independent;   /* df == 0 or p > alpha */
+    double g2;             /* G^2 the decision used: FP64 when rechecked, else the FP32 compensated sum */
+    double p_value;        /* 1 - P(df/2, G^2/2) */
+    int32_t rechecked;     /* 1 when the FP64 recheck band was entered */
+    int32_t path;          /* 0 shared-memory table, 1 global-memory table */
+} fpgm_ci_result;
+
+typedef struct {
+    int32_t n_levels;
+    int64_t tests[64];           /* tests per level, the reference's sequential group-size-1 count */
+    int64_t tests_executed[64];  /* tests actually run (batched mode includes speculative ones) */
+    int32_t edges_after[64];     /* skeleton edges left after the level */
+    int32_t waves[64];           /* batched waves in the level */
+    double ms[64];               /* wall time of the level, host clock around device work */
+    int64_t rechecks;            /* tests that entered the FP64 band */
+    int64_t near_ties;           /* FP64 |p - alpha| < 1e-12 (decision could differ from any other FP64 order) */
+    int64_t large_tests;         /* tests counted in global memory */
+    double max_abs_dp;           /* max |p32 - p64| over rechecked tests */
+    double count_ms;             /* device time of the counting+scoring kernels (CUDA events) */
+    double count_bytes;          /* algorithmic bytes those kernels had to read: sum (2+d) * n_samples */
+    int64_t count_launches;      /* launches of the counting+scoring kernels */
+    double total_ms;             /* wall time of the whole skeleton call */
+} fpgm_pc_stats;
+
+typedef struct {
+    int32_t n_nodes;
+    int32_t n_edges;         /* exact edge count; <= 0 means round(avg_indegree * n_nodes) */
+    double avg_indegree;
+    int32_t max_indegree;
+    int32_t card_min, card_max;   /* uniform cardinality range */
+    double tail_frac;             /* with this probability draw from [tail_min, tail_max] instead */
+    int32_t tail_min, tail_max;
+    double dirichlet_alpha;       /* CPT rows ~ Dirichlet(alpha) */
+    int64_t n_samples;
+    uint64_t seed;
+} fpgm_gen_spec;
+
+/* ---- errors ---- */
+const char *fpgm_last_error(void);
+
+/* ---- engine lifetime ---- */
+int fpgm_engine_create(int32_t device, fpgm_engine **out);
+int fpgm_engine_destroy(fpgm_engine *eng);
+
+/* ---- data ----
+ * columns: n_vars x n_samples uint8, column-major (column v at columns + v*n_samples).
+ * relabel != 0: ids become first-appearance order per column and cardinality
+ * the number of distinct observed values (Dataset.cpp:459-467, :486-488).
+ * relabel == 0: values are used as given; out_card (if given) then receives max+1.
+ * out_card may be NULL. */
+int fpgm_dataset_upload(fpgm_engine *eng, const uint8_t *columns, int32_t n_vars, int64_t n_samples,
+                        int32_t relabel, uint8_t *out_card);
+/* Copies the (relabelled) device columns back, n_vars*n_samples bytes. */
+int fpgm_dataset_download(fpgm_engine *eng, uint8_t *columns);
+
+/* ---- single / batched CI tests (G^2) ----
+ * fpgm_ci_test: one test, one kernel launch ("plain" path).
+ * fpgm_ci_test_batch: tests[t*(2+d) + 0,1,2..] = x, y, z1..zd; all tests run in one
+ * persistent launch.  want_hash != 0 fills table_hash (slower). */
+int fpgm_ci_test(fpgm_engine *eng, int32_t x, int32_t y, const int32_t *z, int32_t nz, double alpha,
+                 int32_t want_hash, fpgm_ci_result *out);
+int fpgm_ci_test_batch(fpgm_engine *eng, const int32_t *tests, int32_t n_tests, int32_t d, double alpha,
+                       int32_t want_hash, fpgm_ci_result *out);
+
+/* ---- PC-stable skeleton ----
+ * depth follows PCStable(Network*, alpha, depth=1000): levels d = 0 .. depth-1.
+ * mode: FPGM_MODE_BATCHED (device-resident level engine) or FPGM_MODE_PLAIN
+ * (the reference's control flow on the host, one kernel launch per CI test).
+ * The result stays in the engine until the next call; fetch it below. */
+int fpgm_pc_skeleton(fpgm_engine *eng, double alpha, int32_t depth, int32_t mode, fpgm_pc_stats *stats);
+int fpgm_pc_result_sizes(fpgm_engine *eng, int32_t *n_nodes, int32_t *n_removed, int64_t *n_sep_vars);
+/* adj: n*n bytes (1 = edge kept).  removed: 2*n_removed (a < b pairs, ascending).
+ * sep_offsets: n_removed+1.  sep_vars: n_sep_vars (each set ascending, like set<int>). */
+int fpgm_pc_result_fetch(fpgm_engine *eng, uint8_t *adj, int32_t *removed, int32_t *sep_offsets,
+                         int32_t *sep_vars);
+
+/* ---- orientation (host) ----
+ * Reproduces the reference's order-dependent v-structure and Meek-rule pass on
+ * a skeleton.  Output edges in the reference's final vec_edges order:
+ * out_edges[3*i] = a, [3*i+1] = b, [3*i+2] = 1 for a -> b, 0 for a -- b.
+ * out_edges needs room for 3 * (#skeleton edges). */
+int fpgm_orient_cpdag(int32_t n, const uint8_t *adj, int32_t n_removed, const int32_t *removed,
+                      const int32_t *sep_offsets, const int32_t *sep_vars, int32_t *out_edges,
+                      int32_t *out_n_edges);
+/* Writes the reference's _struct text (StructureLearning.cpp:238-292) for the edge records
+ * fpgm_orient_cpdag produced.  names may be NULL (then "<i>").  num_edges_header is the skeleton
+ * edge count the reference prints in the header and iterates over. */
+int fpgm_write_struct(const char *path, int32_t n, const char *const *names, const int32_t *edges,
+                      int32_t n_edges, int32_t num_edges_header);
+
+/* ---- drop-in job ---- */
+int fpgm_bnsl_pcstable(int32_t verbose, int32_t n_threads, int32_t group_size, double alpha,
+                       const char *ref_net, const char *train_set, int32_t save_struct);
+
+/* ---- seeded synthetic data ---- */
+int fpgm_generate_network(const fpgm_gen_spec *spec, uint8_t *out_columns, uint8_t *out_card,
+                          int32_t *out_parents);
+int fpgm_write_csv(const char *path, const uint8_t *columns, int32_t n_vars, int64_t n_samples,
+                   const char *name_prefix);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

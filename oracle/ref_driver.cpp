@@ -1,0 +1,167 @@
+// oracle/ref_driver.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// A small driver linked against the reference's OWN PC-stable sources
+// (compiled in place from the reference tree by oracle/Makefile; nothing of
+// the reference is copied here).  It is the pinned oracle: the shipped golden
+// file dataset/alarm/alarm_s5000_struct is reproduced by `pc` mode.
+//
+//   ref_driver pc <csv> <alpha> <threads> <group_size> <depth> <out_prefix> [verbose]
+//       Runs exactly what BNSL_PCStable does (fastpgm_api.cpp:18-44):
+//       LoadCSVTrainingData(csv, true, 0); PCStable(new Network(true), alpha, depth);
+//       StructLearnCompData(d, gs, T, dag=false, add_root=false, save_struct=true, ...)
+//       and writes <out_prefix>_struct (the reference's own writer) and
+//       <out_prefix>_sepsets ("a b : z1 z2 ..." per removed pair, key order).
+//       Prints one line "ref_pc_seconds <s> num_ci_test <n>".
+//
+//   ref_driver tests <csv> <alpha> <tests_in> <out>
+//       For each input line "x y k z1 .. zk" runs the reference's
+//       IndependenceTest::IndependenceResult (IndependenceTest.cpp:35-58) and
+//       the reference's Counts2D/Counts3D::FillTable (CellTable.cpp:226-291,
+//       430-455), and writes "hash df g2 p indep" where hash is FNV-1a-64 over
+//       the reference's int32 joint table n[] in its own cell order, and df/g2
+//       follow IndependenceTest.cpp:94-138 on that table.
+#include <cstdio>
+#include <cstdint>
+#include <cstdlib>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+#include <omp.h>
+
+#include "fastpgm/Dataset.h"
+#include "fastpgm/Network.h"
+#include "fastpgm/Timer.h"
+#include "fastpgm/structure_learning/PCStable.h"
+#include "fastpgm/structure_learning/IndependenceTest.h"
+#include "fastpgm/structure_learning/CellTable.h"
+
+static uint64_t fnv1a_i32(const int *v, long n) {
+    uint64_t h = 1469598103934665603ull;
+    for (long i = 0; i < n; ++i) {
+        uint32_t w = (uint32_t)v[i];
+        for (int b = 0; b < 4; ++b) {
+            h ^= (w >> (8 * b)) & 0xffu;
+            h *= 1099511628211ull;
+        }
+    }
+    return h;
+}
+
+static int run_pc(int argc, char **argv) {
+    if (argc < 8) { fprintf(stderr, "pc: bad args\n"); return 2; }
+    std::string csv = argv[2];
+    double alpha = atof(argv[3]);
+    int threads = atoi(argv[4]);
+    int gs = atoi(argv[5]);
+    int depth = atoi(argv[6]);
+    std::string prefix = argv[7];
+    int verbose = argc > 8 ? atoi(argv[8]) : 0;
+
+    Dataset *d = new Dataset();
+    d->LoadCSVTrainingData(csv, true, 0);
+    Network *net = new Network(true);
+    PCStable *pc = new PCStable(net, alpha, depth);
+    double t0 = omp_get_wtime();
+    pc->StructLearnCompData(d, gs, threads, false, false, true, prefix + "_struct", verbose);
+    double t1 = omp_get_wtime();
+
+    std::ofstream out(prefix + "_sepsets");
+    for (const auto &kv : pc->sepset) {
+        out << kv.first.first << " " << kv.first.second << " :";
+        for (int z : kv.second) out << " " << z;
+        out << "\n";
+    }
+    out.close();
+    printf("ref_pc_seconds %.6f num_ci_test %d\n", t1 - t0, pc->num_ci_test);
+    return 0;
+}
+
+static int run_tests(int argc, char **argv) {
+    if (argc < 6) { fprintf(stderr, "tests: bad args\n"); return 2; }
+    std::string csv = argv[2];
+    double alpha = atof(argv[3]);
+    Dataset *d = new Dataset();
+    d->LoadCSVTrainingData(csv, true, 0);
+    std::ifstream in(argv[4]);
+    FILE *out = fopen(argv[5], "w");
+    Timer timer;
+    std::string line;
+    while (std::getline(in, line)) {
+        if (line.empty()) continue;
+        std::istringstream ss(line);
+        int x, y, k;
+        ss >> x >> y >> k;
+        std::vector<int> z(k);
+        for (int i = 0; i < k; ++i) ss >> z[i];
+        int dx = d->num_of_possible_values_of_disc_vars[x];
+        int dy = d->num_of_possible_values_of_disc_vars[y];
+
+        uint64_t h;
+        int df = 0;
+        double g2 = 0.0;
+        if (k == 0) {
+            Counts2D t(dx, dy, x, y);
+            t.FillTable(d, &timer);
+            h = fnv1a_i32(t.n, (long)dx * dy);
+            int alx = 0, aly = 0;
+            for (int i = 0; i < dx; ++i) alx += t.ni[i] > 0;
+            for (int j = 0; j < dy; ++j) aly += t.nj[j] > 0;
+            alx = alx >= 1 ? alx : 1;
+            aly = aly >= 1 ? aly : 1;
+            df = (alx - 1) * (aly - 1);
+            long total = d->num_instance;
+            for (int i = 0; i < dx; ++i) {
+                long r = t.ni[i];
+                if (r == 0) continue;
+                for (int j = 0; j < dy; ++j) {
+                    long c = t.nj[j], o = t.n[i * dy + j];
+                    if (c == 0 || o == 0) continue;
+                    double e = (double)c * (double)r / (double)total;
+                    g2 += 2.0 * o * log(o / e);
+                }
+            }
+        } else {
+            std::vector<int> dims;
+            for (int zi : z) dims.push_back(d->num_of_possible_values_of_disc_vars[zi]);
+            Counts3D t(dx, dy, x, y, dims, z);
+            t.FillTable(d, &timer);
+            h = fnv1a_i32(t.n, (long)t.dimz * dx * dy);
+            for (int kk = 0; kk < t.dimz; ++kk) {
+                int alx = 0, aly = 0;
+                for (int i = 0; i < dx; ++i) alx += t.ni[kk * dx + i] > 0;
+                for (int j = 0; j < dy; ++j) aly += t.nj[kk * dy + j] > 0;
+                alx = alx >= 1 ? alx : 1;
+                aly = aly >= 1 ? aly : 1;
+                df += (alx - 1) * (aly - 1);
+                long total = t.nk[kk];
+                if (total == 0) continue;
+                for (int i = 0; i < dx; ++i) {
+                    long r = t.ni[kk * dx + i];
+                    if (r == 0) continue;
+                    for (int j = 0; j < dy; ++j) {
+                        long c = t.nj[kk * dy + j], o = t.n[kk * dx * dy + i * dy + j];
+                        if (c == 0 || o == 0) continue;
+                        double e = (double)c * (double)r / (double)total;
+                        g2 += 2.0 * o * log(o / e);
+                    }
+                }
+            }
+        }
+        IndependenceTest it(d, alpha);
+        IndependenceTest::Result r = it.IndependenceResult(x, y, z, "g square", &timer, 1);
+        fprintf(out, "%016llx %d %.17g %.17g %d\n", (unsigned long long)h, df, g2, r.p_value,
+                r.is_independent ? 1 : 0);
+    }
+    fclose(out);
+    return 0;
+}
+
+int main(int argc, char **argv) {
+    if (argc < 2) { fprintf(stderr, "usage: ref_driver pc|tests ...\n"); return 2; }
+    std::string mode = argv[1];
+    if (mode == "pc") return run_pc(argc, argv);
+    if (mode == "tests") return run_tests(argc, argv);
+    fprintf(stderr, "unknown mode %s\n", mode.c_str());
+    return 2;
+}
