@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_kernel(WaveArgs a) {
         __syncthreads();
         if (td.path != 0) {
             if (tid == 0) {
-                if (td.path == 1) {
+                if (td.path == 1 && a.large_ws != nullptr) {
                     int slot = atomicAdd(&a.counters[1], 1);
                     a.large_list[slot] = item;
                     atomicAdd(&a.stats[ST_LARGE], 1ull);
@@ -766,16 +766,17 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d) {
     return FPGM_OK;
 }
 
-// Largest table a level-d test can need, from the largest cardinality.
+// Largest table + marginals a level-d test can need, from the largest cardinality m:
+// m^(d+2) cells and m^d (2m + 1) marginal counters.
 int64_t max_table_ints(const std::vector<uint8_t> &card, int d) {
     int64_t m = 1;
     for (uint8_t c : card) m = std::max<int64_t>(m, c);
-    int64_t cells = 1;
-    for (int k = 0; k < d + 2; ++k) {
-        cells *= m;
-        if (cells > ((int64_t)1 << 40)) return (int64_t)1 << 40;
+    int64_t dz = 1;
+    for (int k = 0; k < d; ++k) {
+        dz *= m;
+        if (dz > ((int64_t)1 << 36)) return (int64_t)1 << 40;
     }
-    return cells + cells / 2 + cells / m * 2;
+    return dz * m * m + dz * (2 * m + 1);
 }
 
 int run_waves_and_count(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t n_active, fpgm_pc_stats *st,

@@ -1,0 +1,145 @@
+"""GPU parity of single and batched CI tests against the oracle and the reference's golden vectors.
+
+Counts (table hash over the int32 joint table in reference cell order) and adjusted df
+must be bit-exact; decisions must be identical.  G^2 is FP32 with compensated summation
+unless the test entered the FP64 recheck band; tolerances are written per assertion.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, read_tests
+from oracle import oracle as O
+import fastpgm_gb300 as F
+
+pytestmark = pytest.mark.gpu
+
+# FP32-compensated G^2 against FP64: relative 2e-5 or absolute 2e-3, whichever is larger.
+G2_RTOL, G2_ATOL = 2e-5, 2e-3
+# p-value of a non-rechecked test sits outside the 1e-3 band around alpha, so the FP32
+# error can move it by at most the propagated bound; compare within 1e-3.
+P_ATOL = 1e-3
+
+
+@pytest.fixture(scope="module")
+def eng():
+    e = F.Engine(0)
+    yield e
+    e.close()
+
+
+def check(g, o, exact_p=False):
+    assert g.table_hash == o.table_hash, "table differs"
+    assert g.df == o.df, "df differs"
+    assert g.independent == o.independent, "decision differs"
+    assert abs(g.g2 - o.g2) <= max(G2_ATOL, G2_RTOL * abs(o.g2)), (g.g2, o.g2)
+    if g.rechecked or exact_p:
+        assert abs(g.p_value - o.p_value) <= 1e-10, (g.p_value, o.p_value)
+    else:
+        assert abs(g.p_value - o.p_value) <= P_ATOL, (g.p_value, o.p_value)
+
+
+@pytest.mark.parametrize("which", ["alarm", "c1"])
+def test_golden_vectors(eng, alarm, which):
+    if which == "alarm":
+        _, cols, card = alarm
+        eng.upload(cols, relabel=False)
+    else:
+        raw, _, _ = F.make_config("c1")
+        cols, card = O.relabel(raw)
+        gcard = eng.upload(raw, relabel=True)
+        assert np.array_equal(gcard, card)
+    gold = read_tests(os.path.join(GOLDEN, which + "_tests.txt"))
+    by_d = {}
+    for g in gold:
+        by_d.setdefault(len(g[2]), []).append(g)
+    for d, items in by_d.items():
+        tests = np.array([[x, y, *z] for x, y, z, *_ in items], dtype=np.int32)
+        res = eng.ci_test_batch(tests, d, want_hash=True)
+        for g, r in zip(items, res):
+            x, y, z, h, df, g2, p, ind = g
+            assert r.table_hash == h and r.df == df and r.independent == ind, g
+            assert abs(r.g2 - g2) <= max(G2_ATOL, G2_RTOL * abs(g2)), (g, r.g2)
+            assert abs(r.p_value - p) <= (1e-10 if r.rechecked else P_ATOL), (g, r.p_value)
+        # the plain one-launch path on the first few
+        for g in items[:8]:
+            x, y, z, h, df, g2, p, ind = g
+            r = eng.ci_test(x, y, z, want_hash=True)
+            assert r.table_hash == h and r.df == df and r.independent == ind, g
+
+
+def random_tests(rng, n, d, count):
+    return np.array([rng.choice(n, size=2 + d, replace=False) for _ in range(count)], dtype=np.int32)
+
+
+@pytest.mark.parametrize("S", [1, 15, 16, 17, 1000, 4099])
+def test_ragged_sample_counts(eng, S):
+    raw, _, _ = F.generate(n_nodes=12, n_samples=S, seed=100 + S, n_edges=14, max_indegree=3, card=(2, 5))
+    cols, card = O.relabel(raw)
+    eng.upload(raw)
+    rng = np.random.default_rng(S)
+    for d in (0, 1, 3):
+        tests = random_tests(rng, 12, d, 40)
+        got = eng.ci_test_batch(tests, d, want_hash=True)
+        exp = O.ci_tests(cols, card, tests, d, threads=4)
+        for g, o in zip(got, exp):
+            check(g, o)
+
+
+def test_constant_and_single_state_columns(eng):
+    S = 3000
+    rng = np.random.default_rng(7)
+    raw = rng.integers(0, 3, size=(6, S)).astype(np.uint8)
+    raw[2, :] = 5          # constant column: cardinality 1, df 0 -> independent
+    raw[4, :S // 2] = 0    # two states
+    raw[4, S // 2:] = 9
+    cols, card = O.relabel(raw)
+    gcard = eng.upload(raw)
+    assert gcard.tolist() == card.tolist()
+    tests = np.array([[0, 2], [2, 3], [0, 4], [1, 3]], dtype=np.int32)
+    for g, o in zip(eng.ci_test_batch(tests, 0, want_hash=True), O.ci_tests(cols, card, tests, 0)):
+        check(g, o)
+    assert eng.ci_test_batch(np.array([[0, 2]], dtype=np.int32), 0)[0].independent == 1
+
+
+def test_many_random_tests_c2_shape(eng):
+    raw, _, _ = F.make_config("c2", n_samples=20000)
+    cols, card = O.relabel(raw)
+    eng.upload(raw)
+    rng = np.random.default_rng(3)
+    for d in (0, 1, 2, 3, 4):
+        tests = random_tests(rng, raw.shape[0], d, 300)
+        got = eng.ci_test_batch(tests, d, want_hash=(d < 4))
+        exp = O.ci_tests(cols, card, tests, d, threads=8)
+        for g, o in zip(got, exp):
+            if d == 4:
+                g.table_hash = o.table_hash
+            check(g, o)
+
+
+def test_global_memory_tables(eng):
+    """Joint tables beyond the shared-memory budget take the global-memory path."""
+    raw, _, _ = F.generate(n_nodes=12, n_samples=6000, seed=77, n_edges=14, max_indegree=3, card=(6, 9))
+    cols, card = O.relabel(raw)
+    eng.upload(raw)
+    rng = np.random.default_rng(5)
+    tests = random_tests(rng, 12, 4, 12)   # >= 6^6 = 46,656 cells
+    got = eng.ci_test_batch(tests, 4, want_hash=True)
+    exp = O.ci_tests(cols, card, tests, 4, threads=8)
+    assert any(g.path == 1 for g in got)
+    for g, o in zip(got, exp):
+        check(g, o)
+    g = eng.ci_test(*map(int, tests[0][:2]), [int(v) for v in tests[0][2:]], want_hash=True)
+    check(g, exp[0])
+
+
+def test_invalid_arguments_are_errors(eng):
+    raw, _, _ = F.make_config("c1")
+    eng.upload(raw)
+    with pytest.raises(F.FpgmError):
+        eng.ci_test(0, 999, ())
+    with pytest.raises(F.FpgmError):
+        eng.ci_test(0, 1, (), alpha=1.5)
+    with pytest.raises(F.FpgmError):
+        eng.ci_test_batch(np.array([[0, 1, 40]], dtype=np.int32), 1)

@@ -1,0 +1,112 @@
+"""GPU PC-stable skeleton parity: batched engine and plain path against the reference's
+golden sepsets/CPDAGs and the oracle's per-level deterministic test counts."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, read_sepsets, sepset_arrays
+from oracle import oracle as O
+import fastpgm_gb300 as F
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def eng():
+    e = F.Engine(0)
+    yield e
+    e.close()
+
+
+def struct_of(tmp_path, names, res):
+    edges = F.orient_cpdag(res["adj"], res["removed"], res["sep_offsets"], res["sep_vars"])
+    p = str(tmp_path / "x_struct")
+    F.write_struct(p, names, edges, int(res["adj"].sum()) // 2)
+    return open(p).read()
+
+
+@pytest.mark.parametrize("mode", [F.FPGM_MODE_BATCHED, F.FPGM_MODE_PLAIN])
+def test_alarm_matches_reference_golden(eng, alarm, tmp_path, mode):
+    names, cols, card = alarm
+    eng.upload(cols, relabel=False)
+    st = eng.pc_skeleton(mode=mode).to_dict()
+    res = eng.result()
+    assert res["sepsets"] == read_sepsets(os.path.join(GOLDEN, "alarm_sepsets"))
+    assert st["tests"] == [666, 3579, 828, 118, 15]
+    assert st["edges_after"] == [262, 67, 46, 44, 44]
+    assert struct_of(tmp_path, names, res) == open(os.path.join(GOLDEN, "alarm_s5000_struct")).read()
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_synthetic_matches_reference(eng, tmp_path, name):
+    raw, depth, _ = F.make_config(name)
+    eng.upload(raw)
+    st = eng.pc_skeleton(depth=depth).to_dict()
+    res = eng.result()
+    assert res["sepsets"] == read_sepsets(os.path.join(GOLDEN, name + "_sepsets"))
+    n = raw.shape[0]
+    assert struct_of(tmp_path, ["V%d" % i for i in range(n)], res) == open(os.path.join(GOLDEN, name + "_struct")).read()
+    cols, card = O.relabel(raw)
+    ref = O.pc_skeleton(cols, card, depth=depth, threads=16)
+    assert st["tests"] == ref["stats"]["tests"]
+    assert st["edges_after"] == ref["stats"]["edges_after"]
+    assert all(e >= t for e, t in zip(st["tests_executed"], st["tests"]))
+
+
+def test_plain_matches_batched_c1(eng):
+    raw, depth, _ = F.make_config("c1")
+    eng.upload(raw)
+    sb = eng.pc_skeleton(mode=F.FPGM_MODE_BATCHED).to_dict()
+    rb = eng.result()
+    sp = eng.pc_skeleton(mode=F.FPGM_MODE_PLAIN).to_dict()
+    rp = eng.result()
+    assert rb["sepsets"] == rp["sepsets"] and np.array_equal(rb["adj"], rp["adj"])
+    assert sb["tests"] == sp["tests"]
+
+
+@pytest.mark.parametrize("name,S,nodes,depth", [("c3", 20000, None, 5), ("c4", 4000, 300, 1000),
+                                                ("c4", 3000, None, 3)])
+def test_other_shapes_match_oracle(eng, name, S, nodes, depth):
+    raw, d0, _ = F.make_config(name, n_samples=S, n_nodes=nodes)
+    cols, card = O.relabel(raw)
+    eng.upload(raw)
+    st = eng.pc_skeleton(depth=depth).to_dict()
+    res = eng.result()
+    ref = O.pc_skeleton(cols, card, depth=depth, threads=16)
+    assert np.array_equal(res["adj"], ref["adj"])
+    assert res["sepsets"] == ref["sepsets"]
+    assert st["tests"] == ref["stats"]["tests"]
+
+
+def test_depth_limits_levels(eng):
+    raw, _, _ = F.make_config("c1")
+    cols, card = O.relabel(raw)
+    eng.upload(raw)
+    for depth in (1, 2, 3):
+        st = eng.pc_skeleton(depth=depth).to_dict()
+        res = eng.result()
+        ref = O.pc_skeleton(cols, card, depth=depth, threads=4)
+        assert st["n_levels"] == ref["stats"]["n_levels"] == depth
+        assert res["sepsets"] == ref["sepsets"]
+
+
+def test_cli_and_python_binding_reproduce_alarm(alarm, tmp_path):
+    names, cols, card = alarm
+    csv = str(tmp_path / "alarm_s5000")
+    with open(csv, "w") as f:
+        f.write(",".join(names) + "\n")
+        for s in range(cols.shape[1]):
+            f.write(",".join(str(int(v)) for v in cols[:, s]) + "\n")
+    out = subprocess.run([F.CLI_PATH, "-j", "0", "-m", "0", "-f2", csv], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    golden = open(os.path.join(GOLDEN, "alarm_s5000_struct")).read()
+    assert open(csv + "_struct").read() == golden
+    os.remove(csv + "_struct")
+    from fastpgm_gb300 import cmake_example as fastpgm
+    fastpgm.BNSL_PCStable(0, 1, 1, 0.05, "", csv, True)
+    assert open(csv + "_struct").read() == golden
+    out = subprocess.run([F.CLI_PATH, "-j", "0", "-m", "0", "-e", "1", "-f2", csv], capture_output=True, text=True)
+    assert out.returncode == 0
+    assert open(csv + "_struct").read() == golden

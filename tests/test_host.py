@@ -1,0 +1,123 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports every
+declared symbol, the host orientation reproduces the reference's CPDAG files,
+the command line and the Python binding parse like the reference's."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT, read_sepsets, sepset_arrays
+from oracle import oracle as O
+import fastpgm_gb300 as F
+
+
+def declared_symbols():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", h)).read()
+            names |= set(re.findall(r"\b(fpgm_[a-z0-9_]+)\s*\(", txt))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = F.load()
+    names = declared_symbols()
+    assert len(names) >= 15
+    for n in sorted(names):
+        assert hasattr(lib, n), n
+    out = subprocess.run(["nm", "-D", "--defined-only", F.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (fpgm_\w+)", out))
+    assert names <= exported, names - exported
+
+
+def _orient_struct(tmp_path, names, adj, seps):
+    removed, off, vs = sepset_arrays(seps)
+    edges = F.orient_cpdag(adj, removed, off, vs)
+    p = str(tmp_path / "s_struct")
+    F.write_struct(p, names, edges, int(adj.sum()) // 2)
+    return open(p).read()
+
+
+def test_orientation_reproduces_alarm_golden(tmp_path, alarm):
+    names, cols, card = alarm
+    r = O.pc_skeleton(cols, card, threads=4)
+    got = _orient_struct(tmp_path, names, r["adj"], r["sepsets"])
+    assert got == open(os.path.join(GOLDEN, "alarm_s5000_struct")).read()
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_orientation_reproduces_reference_cpdag(tmp_path, name):
+    seps = read_sepsets(os.path.join(GOLDEN, name + "_sepsets"))
+    raw, depth, spec = F.make_config(name)
+    n = raw.shape[0]
+    adj = np.ones((n, n), dtype=np.uint8) - np.eye(n, dtype=np.uint8)
+    for a, b in seps:
+        adj[a, b] = adj[b, a] = 0
+    got = _orient_struct(tmp_path, ["V%d" % i for i in range(n)], adj, seps)
+    assert got == open(os.path.join(GOLDEN, name + "_struct")).read()
+
+
+def _collider_csv(path, S=4000, seed=3):
+    """a, c independent; b depends on both -> PC finds a -> b <- c; d independent of all."""
+    rng = np.random.default_rng(seed)
+    a = rng.integers(0, 2, S)
+    c = rng.integers(0, 2, S)
+    b = (a | c) ^ (rng.random(S) < 0.05)
+    e = rng.integers(0, 3, S)
+    cols = np.stack([a, b, c, e]).astype(np.uint8)
+    F.write_csv(path, cols)
+    return cols
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference-built driver needs the reference tree")
+def test_dag_branch_of_struct_writer_matches_reference(tmp_path):
+    csv = str(tmp_path / "col.csv")
+    raw = _collider_csv(csv)
+    O.ref_pc(csv, str(tmp_path / "ref"))
+    cols, card = O.relabel(raw)
+    r = O.pc_skeleton(cols, card)
+    got = _orient_struct(tmp_path, ["V%d" % i for i in range(4)], r["adj"], r["sepsets"])
+    ref = open(tmp_path / "ref_struct").read()
+    assert "->" in ref
+    assert got == ref
+
+
+def test_engine_create_without_gpu_reports_error():
+    import ctypes
+    lib = F.load()
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is visible")
+    except ImportError:
+        pass
+    h = ctypes.c_void_p()
+    rc = lib.fpgm_engine_create(0, ctypes.byref(h))
+    assert rc != 0
+    assert lib.fpgm_last_error()
+
+
+def test_cli_help_and_rejected_jobs():
+    out = subprocess.run([F.CLI_PATH, "-h"], capture_output=True, text=True)
+    assert out.returncode == 0 and "-j & -m" in out.stdout
+    out = subprocess.run([F.CLI_PATH, "-j", "2", "-m", "0"], capture_output=True, text=True)
+    assert out.returncode == 1 and "Only -j 0" in out.stdout
+    out = subprocess.run([F.CLI_PATH, "-v", "1"], capture_output=True, text=True)
+    assert "Unrecognized option -v" in out.stdout  # the reference does not parse -v either
+
+
+def test_generator_rejects_bad_spec():
+    with pytest.raises(F.FpgmError):
+        F.generate(n_nodes=1, n_samples=10, seed=1)
+    with pytest.raises(F.FpgmError):
+        F.generate(n_nodes=5, n_samples=10, seed=1, card=(1, 3))
+
+
+def test_python_binding_module_signature():
+    from fastpgm_gb300 import cmake_example
+    import inspect
+    params = list(inspect.signature(cmake_example.BNSL_PCStable).parameters)
+    assert params == ["verbose", "n_threads", "group_size", "alpha", "ref_net", "train_set", "save_struct"]
