@@ -37,7 +37,8 @@ class PCStats(ctypes.Structure):
                 ("waves", ctypes.c_int32 * 64), ("ms", ctypes.c_double * 64), ("rechecks", ctypes.c_int64),
                 ("near_ties", ctypes.c_int64), ("large_tests", ctypes.c_int64), ("max_abs_dp", ctypes.c_double),
                 ("count_ms", ctypes.c_double), ("count_bytes", ctypes.c_double),
-                ("count_launches", ctypes.c_int64), ("total_ms", ctypes.c_double)]
+                ("count_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("span_ms", ctypes.c_double),
+                ("total_ms", ctypes.c_double)]
 
     def to_dict(self):
         L = self.n_levels
@@ -48,7 +49,8 @@ class PCStats(ctypes.Structure):
                 "rechecks": int(self.rechecks), "near_ties": int(self.near_ties),
                 "large_tests": int(self.large_tests), "max_abs_dp": float(self.max_abs_dp),
                 "count_ms": float(self.count_ms), "count_bytes": float(self.count_bytes),
-                "count_launches": int(self.count_launches), "total_ms": float(self.total_ms)}
+                "count_launches": int(self.count_launches), "kernel_launches": int(self.kernel_launches),
+                "span_ms": float(self.span_ms), "total_ms": float(self.total_ms)}
 
 
 class GenSpec(ctypes.Structure):

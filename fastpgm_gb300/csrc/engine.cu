@@ -817,9 +817,11 @@ int run_waves_and_count(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_
         CK(cudaEventRecord(e->ev0, e->stream));
         ci_kernel<SRC_WAVE><<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
         CK(cudaGetLastError());
+        st->kernel_launches += 3;  // plan, count, reduce
         if (a.large_ws) {
             ci_large_kernel<SRC_WAVE><<<kLargeSlots, kThreads, 0, e->stream>>>(a);
             CK(cudaGetLastError());
+            st->kernel_launches += 1;
         }
         CK(cudaEventRecord(e->ev1, e->stream));
         CK(cudaMemsetAsync(dstat + ST_UNRESOLVED, 0, 8, e->stream));
@@ -858,6 +860,7 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
     RET(e->bits.ensure((size_t)n * W * 4));
     init_bits_kernel<<<blocks_for((int64_t)n * W, 256), 256, 0, e->stream>>>(e->bits.as<uint32_t>(), n, W);
     CK(cudaGetLastError());
+    st->kernel_launches += 1;
     RET(e->log_pair.ensure((size_t)E * 8 + 16));
     RET(e->log_meta.ensure((size_t)E * 8 + 16));
     RET(e->log_vars.ensure((size_t)1 << 20));
@@ -885,6 +888,7 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
                                                                  stride, e->deg.as<int32_t>(),
                                                                  e->node_cnt.as<int32_t>());
             CK(cudaGetLastError());
+            st->kernel_launches += 1;
             CK(cudaMemsetAsync(e->node_cnt.as<int32_t>() + n, 0, 4, e->stream));
             size_t sb = 0;
             cub::DeviceScan::ExclusiveSum(nullptr, sb, e->node_cnt.as<int32_t>(), e->node_off.as<int32_t>(), n + 1,
@@ -925,6 +929,7 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
                     e->status.as<uint8_t>(), dstat);
             }
             CK(cudaGetLastError());
+            st->kernel_launches += 1;
             CK(cudaMemsetAsync(dstat + ST_DET, 0, 8 * 2, e->stream));
             WaveArgs a;
             wave_args_base(e, a, alpha, d);
@@ -953,9 +958,11 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
                 e->log_pair.as<int32_t>(), e->log_meta.as<int32_t>(), e->log_vars.as<int32_t>(), log_count, var_count,
                 dstat);
             CK(cudaGetLastError());
+            st->kernel_launches += 1;
         }
         degree_kernel<<<blocks_for(n, 128), 128, 0, e->stream>>>(e->bits.as<uint32_t>(), n, W, dstat);
         CK(cudaGetLastError());
+        st->kernel_launches += 1;
         unsigned long long hs[ST_COUNT];
         CK(cudaMemcpyAsync(hs, dstat, sizeof hs, cudaMemcpyDeviceToHost, e->stream));
         CK(cudaStreamSynchronize(e->stream));
@@ -1023,7 +1030,7 @@ int plain_grid(const fpgm_engine *e) {
 }
 
 int plain_test(fpgm_engine *e, int x, int y, const int *z, int d, double alpha, int want_hash,
-               fpgm_ci_result *out) {
+               fpgm_ci_result *out, fpgm_pc_stats *st = nullptr) {
     if (!e->plain_ws.p) {
         RET(e->plain_ws.ensure((size_t)kLargeIntsPerSlot * 4 + 64));
         CK(cudaMemsetAsync(e->plain_ws.p, 0, e->plain_ws.bytes, e->stream));
@@ -1047,6 +1054,7 @@ int plain_test(fpgm_engine *e, int x, int y, const int *z, int d, double alpha, 
     p.stats = e->stats.as<unsigned long long>();
     ci_plain_kernel<<<plain_grid(e), kThreads, kSmemBytes, e->stream>>>(p);
     CK(cudaGetLastError());
+    if (st) st->kernel_launches += 1;
     CK(cudaMemcpyAsync(out, p.out, sizeof(fpgm_ci_result), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     if (out->path == 2)
@@ -1078,7 +1086,7 @@ int run_plain(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
     std::vector<std::pair<int, int>> kill;
     for (int i = 0; i < n; ++i)
         for (int j = i + 1; j < n; ++j) {
-            RET(plain_test(e, i, j, nullptr, 0, alpha, 0, &r));
+            RET(plain_test(e, i, j, nullptr, 0, alpha, 0, &r, st));
             ++tests;
             if (r.independent) {
                 kill.push_back({i, j});
@@ -1115,7 +1123,7 @@ int run_plain(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
                     for (int k = 0; k < d; ++k) c[k] = k;
                     do {
                         for (int k = 0; k < d; ++k) z[k] = cand[c[k]];
-                        RET(plain_test(e, x, y, z.data(), d, alpha, 0, &r));
+                        RET(plain_test(e, x, y, z.data(), d, alpha, 0, &r, st));
                         ++tests;
                         if (r.independent) {
                             found = true;
@@ -1240,9 +1248,23 @@ extern "C" int fpgm_pc_skeleton(fpgm_engine *e, double alpha, int32_t depth, int
     fpgm_pc_stats *st = stats ? stats : &local;
     memset(st, 0, sizeof *st);
     e->has_result = false;
+    cudaEvent_t span0, span1;
+    CK(cudaEventCreate(&span0));
+    CK(cudaEventCreate(&span1));
+    CK(cudaStreamSynchronize(e->stream));
     auto t0 = std::chrono::steady_clock::now();
+    CK(cudaEventRecord(span0, e->stream));
     int rc = mode == FPGM_MODE_BATCHED ? run_batched(e, alpha, depth, st) : run_plain(e, alpha, depth, st);
+    if (rc == FPGM_OK) {
+        CK(cudaEventRecord(span1, e->stream));
+        CK(cudaEventSynchronize(span1));
+        float sp = 0.f;
+        CK(cudaEventElapsedTime(&sp, span0, span1));
+        st->span_ms = sp;
+    }
     st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    cudaEventDestroy(span0);
+    cudaEventDestroy(span1);
     if (rc == FPGM_OK) e->has_result = true;
     return rc;
 }

@@ -82,7 +82,9 @@ typedef struct {
     double count_ms;             /* device time of the counting+scoring kernels (CUDA events) */
     double count_bytes;          /* algorithmic bytes those kernels had to read: sum (2+d) * n_samples */
     int64_t count_launches;      /* launches of the counting+scoring kernels */
-    double total_ms;             /* wall time of the whole skeleton call */
+    int64_t kernel_launches;     /* launches of this library's own kernels (library scans excluded) */
+    double span_ms;              /* CUDA-event span of the whole call on the engine's stream */
+    double total_ms;             /* host wall time of the whole skeleton call */
 } fpgm_pc_stats;
 
 typedef struct {
