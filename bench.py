@@ -268,7 +268,8 @@ def run_ours(a, d):
         "config": {"workload": WORKLOADS[a.config], "alpha": a.alpha, "tests_per_step": tests // a.steps,
                    "levels": last["n_levels"], "tests_per_level": last["tests"],
                    "tests_executed_per_level": last["tests_executed"], "edges_after": last["edges_after"],
-                   "waves": last["waves"], "l2": "flushed before each timed step (512 MB write)",
+                   "waves": last["waves"], "level_ms": [round(x, 3) for x in last["ms"]],
+                   "large_table_ms": last["large_ms"], "l2": "flushed before each timed step (512 MB write)",
                    "parallelism": "replicas" if a.gpus > 1 else "single GPU"},
         "e2e": {"value": e2e, "unit": "CI tests/s", "h2d_bytes_per_step": int(raw.nbytes), "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

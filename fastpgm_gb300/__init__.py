@@ -26,7 +26,8 @@ EXPORTED = ["fpgm_last_error", "fpgm_engine_create", "fpgm_engine_destroy", "fpg
 
 
 class CIResult(ctypes.Structure):
-    _fields_ = [("table_hash", ctypes.c_uint64), ("cells", ctypes.c_int64), ("df", ctypes.c_int32),
+    _fields_ = [("table_hash", ctypes.c_uint64), ("cell_hash", ctypes.c_uint64), ("cells", ctypes.c_int64),
+                ("df", ctypes.c_int32),
                 ("independent", ctypes.c_int32), ("g2", ctypes.c_double), ("p_value", ctypes.c_double),
                 ("rechecked", ctypes.c_int32), ("path", ctypes.c_int32)]
 
@@ -36,7 +37,7 @@ class PCStats(ctypes.Structure):
                 ("tests_executed", ctypes.c_int64 * 64), ("edges_after", ctypes.c_int32 * 64),
                 ("waves", ctypes.c_int32 * 64), ("ms", ctypes.c_double * 64), ("rechecks", ctypes.c_int64),
                 ("near_ties", ctypes.c_int64), ("large_tests", ctypes.c_int64), ("max_abs_dp", ctypes.c_double),
-                ("count_ms", ctypes.c_double), ("count_bytes", ctypes.c_double),
+                ("count_ms", ctypes.c_double), ("count_bytes", ctypes.c_double), ("large_ms", ctypes.c_double),
                 ("count_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("span_ms", ctypes.c_double),
                 ("total_ms", ctypes.c_double)]
 
@@ -49,6 +50,7 @@ class PCStats(ctypes.Structure):
                 "rechecks": int(self.rechecks), "near_ties": int(self.near_ties),
                 "large_tests": int(self.large_tests), "max_abs_dp": float(self.max_abs_dp),
                 "count_ms": float(self.count_ms), "count_bytes": float(self.count_bytes),
+                "large_ms": float(self.large_ms),
                 "count_launches": int(self.count_launches), "kernel_launches": int(self.kernel_launches),
                 "span_ms": float(self.span_ms), "total_ms": float(self.total_ms)}
 

@@ -4,14 +4,17 @@
 // with z the mixed-radix code of (z1..zd), last variable fastest
 // (reference: structure_learning/CellTable.cpp:39-51, :254-291), builds the
 // marginals N_x+z, N_+yz, N_++z (:242-250), the adjusted degrees of freedom
-// and G^2 (IndependenceTest.cpp:94-138), and p = 1 - P(df/2, G^2/2)
-// (:146), independent iff df == 0 or p > alpha (:140-142, :153).
+// and G^2 (IndependenceTest.cpp:94-138), and decides independence as
+// df == 0 or p = 1 - P(df/2, G^2/2) > alpha (:140-153).
 //
-// Precision policy: counts are exact int32; G^2 terms are FP32 with a
-// Neumaier-compensated sum and a running error bound; the p-value is FP64.
-// A test whose p lies within the recheck band of alpha (|p - alpha| < 1e-3,
-// widened by the propagated FP32 error) is recomputed with FP64 terms, so
-// every decision is an FP64 decision wherever FP32 could flip it.
+// Precision policy.  Counts are exact int32.  G^2 terms are FP32 with a
+// Neumaier-compensated sum and a running error bound.  The decision compares
+// G^2 +- bound with two FP64 band-edge tables per df, the G^2 values at which
+// p = alpha + 1e-3 and p = alpha - 1e-3 (computed once per alpha with the
+// FP64 incomplete gamma below).  A test whose G^2 interval reaches into that
+// band -- every test whose p-value may lie within 1e-3 of alpha -- is
+// recomputed with FP64 terms and an FP64 p-value.  Outside the band the
+// decision equals the FP64 one by monotonicity of p in G^2.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -23,9 +26,17 @@ constexpr int kMaxCond = FPGM_MAX_COND;
 constexpr int kMaxCols = kMaxCond + 2;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kBinomN = 4096;   // rows of the binomial table
-constexpr int kBinomK = 32;     // columns (k <= 31)
-constexpr double kBand = 1e-3;  // FP64 recheck band around alpha
+constexpr int kSmemBytes = 96 * 1024;
+constexpr int kCtaInts = kSmemBytes / 4;                 // CTA tier: table + marginals
+constexpr int kWarpInts = kSmemBytes / 4 / kWarps;      // warp tier: per-warp region
+constexpr int kHashCap = 4096;                           // compact tier: shared-memory strata hash
+constexpr int kHashBytes = kHashCap * 12;                // u64 keys + int ids
+constexpr int kCompactSmemInts = (kSmemBytes - kHashBytes) / 4;
+constexpr int kBinomN = 4096;
+constexpr int kBinomK = 32;
+constexpr double kBand = 1e-3;
+constexpr int kBandDfMax = 1 << 16;
+constexpr uint64_t kEmptyKey = ~0ull;
 
 // ---------------------------------------------------------------- p-value (FP64)
 // Regularised incomplete gamma, written from its series (DLMF 8.7.1) and the
@@ -67,170 +78,135 @@ __host__ __device__ inline double chisq_pvalue(double g2, long long df) {
     return 1.0 - igamma_p(0.5 * (double)df, 0.5 * g2);
 }
 
-// chi-square density, used to turn a G^2 error bound into a p error bound.
-__host__ __device__ inline double chisq_pdf(double x, long long df) {
-    if (!(x > 0.0)) return df <= 2 ? 1.0 : 0.0;
-    double k = 0.5 * (double)df;
-    return exp((k - 1.0) * log(x) - 0.5 * x - k * 0.69314718055994530942 - lgamma(k));
+// G^2 at which the p-value of df degrees of freedom equals target (bisection;
+// p is decreasing in G^2).  Returns 0 for target >= 1 and +inf for target <= 0.
+__host__ __device__ inline double chisq_quantile_upper(double target, long long df) {
+    if (target >= 1.0) return 0.0;
+    if (target <= 0.0) return 1e300;
+    double lo = 0.0, hi = (double)df + 10.0 * sqrt(2.0 * (double)df) + 50.0;
+    while (chisq_pvalue(hi, df) > target) hi *= 2.0;
+    for (int it = 0; it < 200 && hi - lo > 1e-10 * hi; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (chisq_pvalue(mid, df) > target) lo = mid; else hi = mid;
+    }
+    return 0.5 * (lo + hi);
 }
 
-// ---------------------------------------------------------------- test descriptor
-struct TestDesc {
-    int32_t x, y, d, ncols;
-    int32_t dx, dy;
-    int32_t R;            // replicas of the shared-memory table
-    int32_t path;         // 0 shared memory, 1 global memory, 2 unsupported
-    int64_t dz, cells;
-    int32_t dims[kMaxCols];             // Z dims, then dx, dy (Horner order)
-    const uint8_t *col[kMaxCols];       // matching column pointers
-    int32_t z[kMaxCond];
+struct BandTables {
+    const double *lo;  // G^2 below lo[df]  =>  p > alpha + band  (independent)
+    const double *hi;  // G^2 above hi[df]  =>  p < alpha - band  (dependent)
+    int dfmax;
 };
 
-// Fills dims/cols/cells from x, y, z and picks the counting path.
-// budget_ints: shared-memory ints available for table + marginals.
-__device__ inline void desc_finish(TestDesc &t, const uint8_t *cols, int64_t S_pad, const uint8_t *card,
-                                   int64_t budget_ints, int64_t large_ints) {
-    t.dx = card[t.x];
-    t.dy = card[t.y];
-    int64_t dz = 1;
-    bool over = false;
-    for (int k = 0; k < t.d; ++k) {
-        int dk = card[t.z[k]];
-        t.dims[k] = dk;
-        t.col[k] = cols + (int64_t)t.z[k] * S_pad;
-        dz *= dk;
-        if (dz > ((int64_t)1 << 40)) over = true;
-    }
-    t.dims[t.d] = t.dx;
-    t.col[t.d] = cols + (int64_t)t.x * S_pad;
-    t.dims[t.d + 1] = t.dy;
-    t.col[t.d + 1] = cols + (int64_t)t.y * S_pad;
-    t.ncols = t.d + 2;
-    t.dz = dz;
-    t.cells = dz * t.dx * t.dy;
-    int64_t marg = dz * (t.dx + t.dy + 1);
-    t.R = 1;
-    if (over) {
-        t.path = 2;
-        return;
-    }
-    if (t.cells + marg <= budget_ints) {
-        t.path = 0;
-        for (int R = 32; R >= 2; R >>= 1)
-            if (t.cells * R + t.cells + marg <= budget_ints) { t.R = R; break; }
-    } else if (t.cells + marg <= large_ints) {
-        t.path = 1;
-    } else {
-        t.path = 2;
+// 1 independent, 0 dependent, -1 undecided (FP64 recheck).
+__device__ inline int band_decide(long long df, double g, double err, const BandTables &bt) {
+    if (df == 0) return 1;
+    if (df > bt.dfmax) return -1;
+    if (g + err < bt.lo[df]) return 1;
+    if (g - err > bt.hi[df]) return 0;
+    return -1;
+}
+
+// ---------------------------------------------------------------- counting helpers
+// 16 samples of one column (one 128-bit load) folded into 8 packed pairs of
+// 16-bit Horner codes: pair q holds samples of its low/high halves.  Valid
+// while every code stays below 65536 (tables of at most 65536 cells).
+__device__ __forceinline__ void horner16(uint32_t (&c2)[8], const uint4 w, const uint32_t dim) {
+    const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        c2[2 * q] = c2[2 * q] * dim + __byte_perm(ww[q], 0, 0x4140);      // samples 4q, 4q+1
+        c2[2 * q + 1] = c2[2 * q + 1] * dim + __byte_perm(ww[q], 0, 0x4342);  // samples 4q+2, 4q+3
     }
 }
 
-// ---------------------------------------------------------------- counting
-// Counts samples of vector range [v0, v1) (16 samples per vector) and, if
-// tail, the S % 16 leftover samples, into tab (R replicas, skewed layout so
-// the lanes of a warp hitting one cell land in different banks).
-template <bool kGlobal>
-__device__ inline void count_range(const TestDesc &t, int64_t v0, int64_t v1, bool tail, int64_t S, int *tab,
-                                   int tid, int nthreads) {
-    const int lane = threadIdx.x & 31;
-    const int R = t.R, Rm = R - 1;
-    const int ncols = t.ncols;
-    for (int64_t v = v0 + tid; v < v1; v += nthreads) {
-        uint32_t code[16];
-#pragma unroll
-        for (int b = 0; b < 16; ++b) code[b] = 0;
-        for (int j = 0; j < ncols; ++j) {
-            const uint4 w = __ldg(reinterpret_cast<const uint4 *>(t.col[j]) + v);
-            const uint32_t dim = (uint32_t)t.dims[j];
-            const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-            for (int b = 0; b < 16; ++b) code[b] = code[b] * dim + ((ww[b >> 2] >> (8 * (b & 3))) & 0xffu);
-        }
-#pragma unroll
-        for (int b = 0; b < 16; ++b) {
-            const uint32_t c = code[b];
-            if (kGlobal)
-                atomicAdd(&tab[c], 1);
-            else
-                atomicAdd(&tab[(int64_t)c * R + ((lane + (int)c) & Rm)], 1);
-        }
-    }
-    if (tail) {
-        for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += nthreads) {
-            uint32_t c = 0;
-            for (int j = 0; j < ncols; ++j) c = c * (uint32_t)t.dims[j] + t.col[j][s];
-            if (kGlobal)
-                atomicAdd(&tab[c], 1);
-            else
-                atomicAdd(&tab[(int64_t)c * R + ((lane + (int)c) & Rm)], 1);
-        }
-    }
+// Order-independent fingerprint of a count table: sum over nonzero cells of a
+// 64-bit mix of (cell index in reference order, count).
+__host__ __device__ inline uint64_t cell_mix(uint64_t key, uint32_t count) {
+    uint64_t z = key * 0x100000001B3ull + (uint64_t)count + 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
 }
 
-// ---------------------------------------------------------------- reductions
+// ---------------------------------------------------------------- thread groups
+struct WarpGroup {
+    int t;
+    __device__ int n() const { return 32; }
+    __device__ void sync() const { __syncwarp(); }
+};
+struct CtaGroup {
+    int t;
+    __device__ int n() const { return (int)blockDim.x; }
+    __device__ void sync() const { __syncthreads(); }
+};
+
 struct Partial {
     long long df;
     double g2, err, abs_g2;
+    unsigned long long hash;
 };
 
-__device__ inline Partial block_reduce(Partial p, Partial *scratch /* kWarps */) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__device__ inline Partial warp_sum(Partial p) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        p.df += __shfl_down_sync(0xffffffffu, p.df, o);
-        p.g2 += __shfl_down_sync(0xffffffffu, p.g2, o);
-        p.err += __shfl_down_sync(0xffffffffu, p.err, o);
-        p.abs_g2 += __shfl_down_sync(0xffffffffu, p.abs_g2, o);
+        p.df += __shfl_xor_sync(0xffffffffu, p.df, o);
+        p.g2 += __shfl_xor_sync(0xffffffffu, p.g2, o);
+        p.err += __shfl_xor_sync(0xffffffffu, p.err, o);
+        p.abs_g2 += __shfl_xor_sync(0xffffffffu, p.abs_g2, o);
+        p.hash += __shfl_xor_sync(0xffffffffu, p.hash, o);
     }
-    if (lane == 0) scratch[warp] = p;
-    __syncthreads();
-    Partial r{0, 0.0, 0.0, 0.0};
-    if (threadIdx.x == 0) {
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-            r.df += scratch[w].df;
-            r.g2 += scratch[w].g2;
-            r.err += scratch[w].err;
-            r.abs_g2 += scratch[w].abs_g2;
-        }
-    }
-    __syncthreads();
-    return r;  // valid in thread 0
+    return p;
 }
 
-struct Verdict {
-    long long df;
-    double g2, p;
-    int indep, rechecked;
-    double dp;  // |p32 - p64| when rechecked
-};
+// Block-wide sum; the result is valid in every thread.  scratch: kWarps entries.
+__device__ inline Partial block_sum(Partial p, Partial *scratch) {
+    p = warp_sum(p);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) scratch[warp] = p;
+    __syncthreads();
+    Partial r{0, 0.0, 0.0, 0.0, 0ull};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        r.df += scratch[w].df;
+        r.g2 += scratch[w].g2;
+        r.err += scratch[w].err;
+        r.abs_g2 += scratch[w].abs_g2;
+        r.hash += scratch[w].hash;
+    }
+    return r;
+}
+
+__device__ inline Partial group_sum(const WarpGroup &, Partial p, Partial *) { return warp_sum(p); }
+__device__ inline Partial group_sum(const CtaGroup &, Partial p, Partial *scratch) { return block_sum(p, scratch); }
 
 // ---------------------------------------------------------------- scoring
-// ct: compact table [dz][dx][dy]; ni/nj/nk scratch of dz*dx, dz*dy, dz ints.
-// Every thread of the block must call this; the verdict is valid in thread 0.
-__device__ inline Verdict score_table(const TestDesc &t, const int *ct, int *ni, int *nj, int *nk, double alpha,
-                                      Partial *scratch, int tid, int nthreads) {
-    const int dx = t.dx, dy = t.dy;
-    const int64_t dz = t.dz, dxy = (int64_t)dx * dy;
-    for (int64_t idx = tid; idx < dz * dx; idx += nthreads) {
+// ct: table [dz][dx][dy]; ni/nj/nk: dz*dx, dz*dy, dz ints of scratch.
+// Marginals, then per-thread partial df (strata) -- every thread of g calls it.
+template <class G>
+__device__ inline long long marginals(const G &g, const int *ct, int *ni, int *nj, int *nk, int dx, int dy,
+                                      int64_t dz) {
+    const int64_t dxy = (int64_t)dx * dy;
+    for (int64_t idx = g.t; idx < dz * dx; idx += g.n()) {
         const int *row = ct + idx * dy;
         int s = 0;
         for (int j = 0; j < dy; ++j) s += row[j];
         ni[idx] = s;
     }
-    for (int64_t idx = tid; idx < dz * dy; idx += nthreads) {
-        int64_t k = idx / dy;
-        int j = (int)(idx - k * dy);
+    for (int64_t idx = g.t; idx < dz * dy; idx += g.n()) {
+        const int64_t k = idx / dy;
+        const int j = (int)(idx - k * dy);
         const int *base = ct + k * dxy + j;
         int s = 0;
         for (int i = 0; i < dx; ++i) s += base[(int64_t)i * dy];
         nj[idx] = s;
     }
-    __syncthreads();
-    Partial p{0, 0.0, 0.0, 0.0};
-    for (int64_t k = tid; k < dz; k += nthreads) {
+    g.sync();
+    long long df = 0;
+    for (int64_t k = g.t; k < dz; k += g.n()) {
         int alx = 0, aly = 0, tot = 0;
         for (int i = 0; i < dx; ++i) {
-            int v = ni[k * dx + i];
+            const int v = ni[k * dx + i];
             alx += v > 0;
             tot += v;
         }
@@ -238,81 +214,101 @@ __device__ inline Verdict score_table(const TestDesc &t, const int *ct, int *ni,
         nk[k] = tot;
         alx = alx >= 1 ? alx : 1;
         aly = aly >= 1 ? aly : 1;
-        p.df += (long long)(alx - 1) * (aly - 1);
+        df += (long long)(alx - 1) * (aly - 1);
     }
-    __syncthreads();
-    // FP32 terms 2 O ln(O N_z / (N_x N_y)) with exact int64 products.
+    g.sync();
+    return df;
+}
+
+// FP32 G^2 terms 2 O ln(O N_z / (N_x N_y)) over this thread's cells, with exact
+// int64 products, Neumaier compensation and a first-order error bound.
+// zkeys (optional): stratum code of each table row, for the cell fingerprint.
+template <class G>
+__device__ inline void g2_fp32(const G &g, const int *ct, const int *ni, const int *nj, const int *nk, int dx, int dy,
+                               int64_t cells, const uint64_t *zkeys, bool want_hash, Partial &p) {
+    const int64_t dxy = (int64_t)dx * dy;
     float s = 0.f, c = 0.f, e = 0.f, a = 0.f;
-    for (int64_t cell = tid; cell < t.cells; cell += nthreads) {
+    unsigned long long h = 0;
+    for (int64_t cell = g.t; cell < cells; cell += g.n()) {
         const int O = ct[cell];
         if (O == 0) continue;
         const int64_t k = cell / dxy;
         const int rem = (int)(cell - k * dxy);
         const int i = rem / dy, j = rem - (rem / dy) * dy;
+        if (want_hash) {
+            const uint64_t key = zkeys ? (zkeys[k] * (uint64_t)dx + i) * (uint64_t)dy + j : (uint64_t)cell;
+            h += cell_mix(key, (uint32_t)O);
+        }
         const long long num = (long long)O * nk[k];
         const long long den = (long long)ni[k * dx + i] * nj[k * dy + j];
         if (num == den) continue;
         const float q = (float)(num - den) / (float)den;
-        float l;
-        if (fabsf(q) < 0.5f)
-            l = log1pf(q);
-        else
-            l = logf((float)num / (float)den);
+        const float l = fabsf(q) < 0.5f ? log1pf(q) : logf((float)num / (float)den);
         const float term = 2.0f * (float)O * l;
-        // Neumaier compensated accumulation
         const float tt = s + term;
-        if (fabsf(s) >= fabsf(term))
-            c += (s - tt) + term;
-        else
-            c += (term - tt) + s;
+        c += fabsf(s) >= fabsf(term) ? (s - tt) + term : (term - tt) + s;
         s = tt;
         e += 2.0f * (float)O * (2.5e-7f * fminf(1.0f, 2.0f * fabsf(q)) + 2.5e-7f * fabsf(l));
         a += fabsf(term);
     }
-    p.g2 = (double)s + (double)c;
-    p.err = (double)e;
-    p.abs_g2 = (double)a;
-    Partial r = block_reduce(p, scratch);
-    __shared__ int s_recheck;
-    __shared__ double s_p32;
-    Verdict v{0, 0.0, 1.0, 1, 0, 0.0};
-    if (tid == 0) {
-        v.df = r.df;
-        v.g2 = r.g2;
-        s_recheck = 0;
-        if (r.df == 0) {
-            v.p = 1.0;
-            v.indep = 1;
-        } else {
-            const double err = 2.0 * r.err + 1e-6 * r.abs_g2 + 1e-12;
-            v.p = chisq_pvalue(r.g2, r.df);
-            const double dpb = chisq_pdf(r.g2 > err ? r.g2 - err : 0.0, r.df) * err * 2.0;
-            v.indep = v.p > alpha;
-            if (fabs(v.p - alpha) < kBand || fabs(v.p - alpha) < dpb) s_recheck = 1;
-            s_p32 = v.p;
-        }
+    p.g2 += (double)s + (double)c;
+    p.err += (double)e;
+    p.abs_g2 += (double)a;
+    p.hash += h;
+}
+
+// FP64 G^2 terms with the reference's formula: E = N_+yz N_x+z / N_++z, 2 O ln(O / E).
+template <class G>
+__device__ inline double g2_fp64(const G &g, const int *ct, const int *ni, const int *nj, const int *nk, int dx,
+                                 int dy, int64_t cells) {
+    const int64_t dxy = (int64_t)dx * dy;
+    double s = 0.0;
+    for (int64_t cell = g.t; cell < cells; cell += g.n()) {
+        const int O = ct[cell];
+        if (O == 0) continue;
+        const int64_t k = cell / dxy;
+        const int rem = (int)(cell - k * dxy);
+        const int i = rem / dy, j = rem - (rem / dy) * dy;
+        const double expected = (double)nj[k * dy + j] * (double)ni[k * dx + i] / (double)nk[k];
+        s += 2.0 * O * log(O / expected);
     }
-    __syncthreads();
-    if (s_recheck) {
-        // FP64 terms, the reference's formula: E = N_+yz * N_x+z / N_++z, 2 O ln(O / E).
-        Partial q{0, 0.0, 0.0, 0.0};
-        for (int64_t cell = tid; cell < t.cells; cell += nthreads) {
-            const int O = ct[cell];
-            if (O == 0) continue;
-            const int64_t k = cell / dxy;
-            const int rem = (int)(cell - k * dxy);
-            const int i = rem / dy, j = rem - (rem / dy) * dy;
-            const double expected = (double)nj[k * dy + j] * (double)ni[k * dx + i] / (double)nk[k];
-            q.g2 += 2.0 * O * log(O / expected);
-        }
-        Partial r2 = block_reduce(q, scratch);
-        if (tid == 0) {
-            v.g2 = r2.g2;
-            v.p = chisq_pvalue(r2.g2, v.df);
-            v.indep = v.p > alpha;
-            v.rechecked = 1;
-            v.dp = fabs(v.p - s_p32);
-        }
+    return s;
+}
+
+struct Verdict {
+    long long df;
+    double g2, p;
+    int indep, rechecked;
+    double dp;  // |p(FP32 G^2) - p(FP64 G^2)| when rechecked
+    unsigned long long hash;
+};
+
+// Full scoring of a dense table held by group g (shared or global memory).
+// Every thread of g calls it; the verdict is valid in every thread.
+template <class G>
+__device__ inline Verdict score_dense(const G &g, const int *ct, int *ni, int *nj, int *nk, int dx, int dy,
+                                      int64_t dz, double alpha, const BandTables &bt, bool want_p, bool want_hash,
+                                      Partial *scratch) {
+    Partial p{0, 0.0, 0.0, 0.0, 0ull};
+    p.df = marginals(g, ct, ni, nj, nk, dx, dy, dz);
+    const int64_t cells = dz * dx * dy;
+    g2_fp32(g, ct, ni, nj, nk, dx, dy, cells, nullptr, want_hash, p);
+    Partial r = group_sum(g, p, scratch);
+    Verdict v{r.df, r.g2, 1.0, 1, 0, 0.0, r.hash};
+    const double err = 2.0 * r.err + 1e-6 * r.abs_g2 + 1e-12;
+    const int dec = band_decide(r.df, r.g2, err, bt);
+    if (dec < 0) {
+        Partial q{0, 0.0, 0.0, 0.0, 0ull};
+        q.g2 = g2_fp64(g, ct, ni, nj, nk, dx, dy, cells);
+        Partial r2 = group_sum(g, q, scratch);
+        v.g2 = r2.g2;
+        v.p = chisq_pvalue(r2.g2, r.df);
+        v.indep = v.p > alpha;
+        v.rechecked = 1;
+        v.dp = fabs(v.p - chisq_pvalue(r.g2, r.df));
+    } else {
+        v.indep = dec;
+        v.p = (want_p && r.df > 0) ? chisq_pvalue(r.g2, r.df) : (r.df == 0 ? 1.0 : (dec ? 1.0 : 0.0));
     }
     return v;
 }

@@ -1,0 +1,623 @@
+// CI-test kernels of the engine.  Every test of a wave (or of an explicit
+// batch) is first classified by the size of its joint table and sent to one
+// of three persistent kernels:
+//
+//   tier 0  ci_warp_kernel     one warp per test, table + marginals in a 12 KB
+//                              per-warp slice of shared memory (<= 3072 ints)
+//   tier 1  ci_cta_kernel      one CTA per test, table in 96 KB of shared memory
+//   tier 2  ci_compact_kernel  one CTA per test; the observed Z strata are first
+//                              hashed to compact ids (shared-memory hash, global
+//                              fallback), then counted stratum-chunk by chunk --
+//                              work O(samples + observed cells), never O(dz)
+//
+// Tiers 0/1 count with 128-bit column loads folded into packed 16-bit Horner
+// codes (two samples per 32-bit multiply-add) and shared-memory atomics into R
+// replicas of the table laid out with an odd stride, so lanes of a warp that
+// hit the same cell land in different banks.
+#pragma once
+#include "ci_device.cuh"
+
+namespace fpgm {
+
+// counters[] slots (int32)
+enum { C_TIER0 = 0, C_TIER1, C_TIER2, C_WORK0, C_WORK1, C_WORK2, C_COUNT };
+// stats[] slots (unsigned long long)
+enum { ST_RECHECK = 0, ST_NEARTIE, ST_LARGE, ST_MAXDP, ST_UNSUPPORTED, ST_DET, ST_EXEC, ST_UNRESOLVED,
+       ST_REMOVED, ST_MAXDEG, ST_TIER0, ST_TIER1, ST_TIER2, ST_COUNT };
+
+enum { SRC_WAVE = 0, SRC_EXPLICIT = 1 };
+
+struct WaveArgs {
+    const uint8_t *cols;
+    int64_t S, S_pad;
+    const uint8_t *card;
+    int d;
+    // wave source
+    const int32_t *adjl;
+    int32_t adj_stride;
+    const int32_t *deg;
+    const int32_t *ex, *ey, *pxy, *pyx;
+    const uint64_t *cntx, *next;
+    const int32_t *off;
+    int32_t n_edges;
+    const uint64_t *btab;
+    // explicit source
+    const int32_t *tests;  // [n][2+d]: x, y, z...
+    int32_t n_tests;
+    // classified items
+    uint16_t *item_vars;   // [T][2+d], Horner order: z1..zd, x, y
+    int32_t *lists;        // 3 lists of list_cap items
+    int64_t list_cap;
+    // outputs
+    uint8_t *flag;         // 1 independent, 0 dependent, 2 unsupported
+    fpgm_ci_result *detail;
+    int32_t want_hash;
+    int32_t *counters;
+    unsigned long long *stats;
+    double alpha;
+    BandTables bt;
+    // compact tier: per-CTA global slots
+    char *slot_mem;
+    int64_t slot_bytes;
+    int32_t hash_cap_global;  // power of two >= 2 * n_samples
+    int64_t slot_tab_ints;
+};
+
+__device__ inline int upper_bound_i32(const int32_t *a, int n, int v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] <= v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// Item -> (x, y, Z) -> tier.  One thread per item, grid-stride.
+template <int kSource>
+__global__ void classify_kernel(WaveArgs a) {
+    const int T = kSource == SRC_EXPLICIT ? a.n_tests : a.off[a.n_edges];
+    const int d = a.d, ncols = d + 2;
+    for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < T; item += gridDim.x * blockDim.x) {
+        int x, y, z[kMaxCond];
+        if (kSource == SRC_EXPLICIT) {
+            const int32_t *tt = a.tests + (int64_t)item * ncols;
+            x = tt[0];
+            y = tt[1];
+            for (int k = 0; k < d; ++k) z[k] = tt[2 + k];
+        } else {
+            const int e = upper_bound_i32(a.off, a.n_edges + 1, item) - 1;
+            uint64_t rank = a.next[e] + (uint64_t)(item - a.off[e]);
+            x = a.ex[e];
+            y = a.ey[e];
+            if (d > 0) {
+                int side_node, skip;
+                if (rank < a.cntx[e]) {
+                    side_node = x;
+                    skip = a.pxy[e];
+                } else {
+                    rank -= a.cntx[e];
+                    side_node = y;
+                    skip = a.pyx[e];
+                }
+                int c[kMaxCond];
+                unrank_lex(a.btab, a.deg[side_node] - 1, d, rank, c);
+                const int32_t *L = a.adjl + (int64_t)side_node * a.adj_stride;
+                for (int k = 0; k < d; ++k) z[k] = L[c[k] < skip ? c[k] : c[k] + 1];
+            }
+        }
+        uint16_t *iv = a.item_vars + (int64_t)item * ncols;
+        double dzf = 1.0;
+        int64_t dz = 1;
+        for (int k = 0; k < d; ++k) {
+            iv[k] = (uint16_t)z[k];
+            const int dk = a.card[z[k]];
+            dzf *= dk;
+            dz *= dk;
+        }
+        iv[d] = (uint16_t)x;
+        iv[d + 1] = (uint16_t)y;
+        const int dx = a.card[x], dy = a.card[y];
+        int tier;
+        if (dzf * dx * dy > 4e18) {
+            tier = 3;  // stratum codes would not fit 64 bits
+        } else {
+            const int64_t need = dz * dx * dy + dz * (dx + dy + 1);
+            tier = need <= kWarpInts - 32 ? 0 : (need <= kCtaInts - 64 ? 1 : 2);
+            if (tier == 2 && a.slot_mem == nullptr) tier = 3;
+        }
+        if (tier == 3) {
+            a.flag[item] = 2;
+            atomicAdd(&a.stats[ST_UNSUPPORTED], 1ull);
+            continue;
+        }
+        const int slot = atomicAdd(&a.counters[C_TIER0 + tier], 1);
+        a.lists[tier * a.list_cap + slot] = item;
+    }
+}
+
+__device__ inline void record(const WaveArgs &a, int item, const Verdict &v, int64_t cells, uint64_t fnv, int path) {
+    a.flag[item] = (uint8_t)v.indep;
+    if (v.rechecked) {
+        atomicAdd(&a.stats[ST_RECHECK], 1ull);
+        if (fabs(v.p - a.alpha) < 1e-12) atomicAdd(&a.stats[ST_NEARTIE], 1ull);
+        atomicMax(&a.stats[ST_MAXDP], (unsigned long long)__double_as_longlong(v.dp));
+    }
+    if (a.detail) {
+        fpgm_ci_result r;
+        r.table_hash = fnv;
+        r.cell_hash = v.hash;
+        r.cells = cells;
+        r.df = (int32_t)v.df;
+        r.independent = v.indep;
+        r.g2 = v.g2;
+        r.p_value = v.p;
+        r.rechecked = v.rechecked;
+        r.path = path;
+        a.detail[item] = r;
+    }
+}
+
+// ---------------------------------------------------------------- tier 0: warp per test
+__global__ void __launch_bounds__(kThreads, 2) ci_warp_kernel(WaveArgs a) {
+    extern __shared__ int smem[];
+    __shared__ const uint8_t *s_col[kWarps][kMaxCols];
+    __shared__ uint32_t s_dim[kWarps][kMaxCols];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int *wreg = smem + warp * kWarpInts;
+    const int n0 = a.counters[C_TIER0];
+    const int d = a.d, ncols = d + 2;
+    const int64_t nvec = a.S >> 4;
+    const WarpGroup g{lane};
+    for (;;) {
+        int idx = 0;
+        if (lane == 0) idx = atomicAdd(&a.counters[C_WORK0], 1);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx >= n0) break;
+        const int item = a.lists[idx];
+        uint32_t dim = 1;
+        if (lane < ncols) {
+            const int var = a.item_vars[(int64_t)item * ncols + lane];
+            dim = a.card[var];
+            s_col[warp][lane] = a.cols + (int64_t)var * a.S_pad;
+            s_dim[warp][lane] = dim;
+        }
+        uint32_t cells = dim;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cells *= __shfl_xor_sync(0xffffffffu, cells, o);
+        const int dx = __shfl_sync(0xffffffffu, (int)dim, d), dy = __shfl_sync(0xffffffffu, (int)dim, d + 1);
+        const int dz = (int)cells / (dx * dy);
+        __syncwarp();
+        const int marg = dz * (dx + dy + 1);
+        const int stride = (int)cells | 1;
+        int R = 1;
+        for (int r = 32; r >= 2; r >>= 1)
+            if (stride * r + marg <= kWarpInts) { R = r; break; }
+        int *tab = wreg;
+        int *ni = wreg + stride * R, *nj = ni + dz * dx, *nk = nj + dz * dy;
+        for (int i = lane; i < stride * R; i += 32) tab[i] = 0;
+        __syncwarp();
+        int *mytab = tab + (lane & (R - 1)) * stride;
+        for (int64_t v = lane; v < nvec; v += 32) {
+            uint32_t c2[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int j = 0; j < ncols; ++j)
+                horner16(c2, __ldg(reinterpret_cast<const uint4 *>(s_col[warp][j]) + v), s_dim[warp][j]);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                atomicAdd(&mytab[c2[q] & 0xffffu], 1);
+                atomicAdd(&mytab[c2[q] >> 16], 1);
+            }
+        }
+        for (int64_t s = (a.S & ~(int64_t)15) + lane; s < a.S; s += 32) {
+            uint32_t c = 0;
+            for (int j = 0; j < ncols; ++j) c = c * s_dim[warp][j] + s_col[warp][j][s];
+            atomicAdd(&mytab[c], 1);
+        }
+        __syncwarp();
+        if (R > 1) {
+            for (int c = lane; c < (int)cells; c += 32) {
+                int s = 0;
+                for (int r = 0; r < R; ++r) s += tab[r * stride + c];
+                tab[c] = s;
+            }
+            __syncwarp();
+        }
+        const Verdict v = score_dense(g, tab, ni, nj, nk, dx, dy, dz, a.alpha, a.bt, a.detail != nullptr,
+                                      a.want_hash != 0, nullptr);
+        if (lane == 0) record(a, item, v, cells, a.want_hash ? table_hash(tab, cells) : 0, 0);
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------- tier 1: CTA per test
+__global__ void __launch_bounds__(kThreads, 2) ci_cta_kernel(WaveArgs a) {
+    extern __shared__ int smem[];
+    __shared__ const uint8_t *s_col[kMaxCols];
+    __shared__ uint32_t s_dim[kMaxCols];
+    __shared__ int s_idx;
+    __shared__ Partial scratch[kWarps];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int n1 = a.counters[C_TIER1];
+    const int d = a.d, ncols = d + 2;
+    const int64_t nvec = a.S >> 4;
+    const CtaGroup g{tid};
+    for (;;) {
+        if (tid == 0) s_idx = atomicAdd(&a.counters[C_WORK1], 1);
+        __syncthreads();
+        const int idx = s_idx;
+        if (idx >= n1) break;
+        const int item = a.lists[a.list_cap + idx];
+        if (tid < ncols) {
+            const int var = a.item_vars[(int64_t)item * ncols + tid];
+            s_dim[tid] = a.card[var];
+            s_col[tid] = a.cols + (int64_t)var * a.S_pad;
+        }
+        __syncthreads();
+        int cells = 1;
+        for (int j = 0; j < ncols; ++j) cells *= (int)s_dim[j];
+        const int dx = s_dim[d], dy = s_dim[d + 1];
+        const int dz = cells / (dx * dy);
+        const int marg = dz * (dx + dy + 1);
+        const int stride = cells | 1;
+        int R = 1;
+        for (int r = 32; r >= 2; r >>= 1)
+            if (stride * r + marg <= kCtaInts) { R = r; break; }
+        int *tab = smem;
+        int *ni = smem + stride * R, *nj = ni + dz * dx, *nk = nj + dz * dy;
+        for (int i = tid; i < stride * R; i += kThreads) tab[i] = 0;
+        __syncthreads();
+        int *mytab = tab + (lane & (R - 1)) * stride;
+        for (int64_t v = tid; v < nvec; v += kThreads) {
+            uint32_t c2[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int j = 0; j < ncols; ++j) horner16(c2, __ldg(reinterpret_cast<const uint4 *>(s_col[j]) + v), s_dim[j]);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                atomicAdd(&mytab[c2[q] & 0xffffu], 1);
+                atomicAdd(&mytab[c2[q] >> 16], 1);
+            }
+        }
+        for (int64_t s = (a.S & ~(int64_t)15) + tid; s < a.S; s += kThreads) {
+            uint32_t c = 0;
+            for (int j = 0; j < ncols; ++j) c = c * s_dim[j] + s_col[j][s];
+            atomicAdd(&mytab[c], 1);
+        }
+        __syncthreads();
+        if (R > 1) {
+            for (int c = tid; c < cells; c += kThreads) {
+                int s = 0;
+                for (int r = 0; r < R; ++r) s += tab[r * stride + c];
+                tab[c] = s;
+            }
+            __syncthreads();
+        }
+        const Verdict v = score_dense(g, tab, ni, nj, nk, dx, dy, dz, a.alpha, a.bt, a.detail != nullptr,
+                                      a.want_hash != 0, scratch);
+        if (tid == 0) record(a, item, v, cells, a.want_hash ? table_hash(tab, cells) : 0, 1);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- tier 2: compact strata
+__device__ __forceinline__ uint32_t zhash(uint64_t z, uint32_t cap) {
+    return (uint32_t)((z * 0x9E3779B97F4A7C15ull) >> 32) & (cap - 1);
+}
+
+// Returns false when the table is full.
+__device__ inline bool zinsert(uint64_t *keys, uint32_t cap, uint64_t z, int *distinct) {
+    uint32_t h = zhash(z, cap);
+    for (uint32_t p = 0; p < cap; ++p) {
+        uint64_t k = keys[h];
+        if (k == z) return true;
+        if (k == kEmptyKey) {
+            unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(&keys[h]),
+                                               (unsigned long long)kEmptyKey, (unsigned long long)z);
+            if (old == kEmptyKey) {
+                atomicAdd(distinct, 1);
+                return true;
+            }
+            if (old == z) return true;
+        }
+        h = (h + 1) & (cap - 1);
+    }
+    return false;
+}
+
+__device__ inline int zlookup(const uint64_t *keys, const int *ids, uint32_t cap, uint64_t z) {
+    uint32_t h = zhash(z, cap);
+    for (uint32_t p = 0; p < cap; ++p) {
+        if (keys[h] == z) return ids[h];
+        h = (h + 1) & (cap - 1);
+    }
+    return -1;
+}
+
+__global__ void __launch_bounds__(kThreads) ci_compact_kernel(WaveArgs a) {
+    extern __shared__ int smem[];
+    uint64_t *hkeys = reinterpret_cast<uint64_t *>(smem);
+    int *hids = reinterpret_cast<int *>(hkeys + kHashCap);
+    int *stab = hids + kHashCap;
+    __shared__ const uint8_t *s_col[kMaxCols];
+    __shared__ uint32_t s_dim[kMaxCols];
+    __shared__ int s_idx, s_over, s_distinct, s_base;
+    __shared__ int s_wsum[kWarps];
+    __shared__ Partial scratch[kWarps];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t gcap = (uint32_t)a.hash_cap_global;
+    char *slot = a.slot_mem + (int64_t)blockIdx.x * a.slot_bytes;
+    uint64_t *gkeys = reinterpret_cast<uint64_t *>(slot);
+    int *gids = reinterpret_cast<int *>(gkeys + gcap);
+    uint64_t *gzk = reinterpret_cast<uint64_t *>(gids + gcap);
+    int *gtab = reinterpret_cast<int *>(gzk + gcap);
+    const int n2 = a.counters[C_TIER2];
+    const int d = a.d, ncols = d + 2;
+    const CtaGroup g{tid};
+    for (;;) {
+        if (tid == 0) s_idx = atomicAdd(&a.counters[C_WORK2], 1);
+        __syncthreads();
+        const int idx = s_idx;
+        if (idx >= n2) break;
+        const int item = a.lists[2 * a.list_cap + idx];
+        if (tid < ncols) {
+            const int var = a.item_vars[(int64_t)item * ncols + tid];
+            s_dim[tid] = a.card[var];
+            s_col[tid] = a.cols + (int64_t)var * a.S_pad;
+        }
+        __syncthreads();
+        const int dx = s_dim[d], dy = s_dim[d + 1];
+        const uint8_t *colx = s_col[d], *coly = s_col[d + 1];
+        // phase 1: observed strata -> hash (shared, then global if it fills up)
+        uint64_t *keys = hkeys;
+        int *ids = hids;
+        uint32_t cap = kHashCap;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            for (uint32_t i = tid; i < cap; i += kThreads) keys[i] = kEmptyKey;
+            if (tid == 0) {
+                s_over = 0;
+                s_distinct = 0;
+            }
+            __syncthreads();
+            for (int64_t s = tid; s < a.S; s += kThreads) {
+                if (*(volatile int *)&s_over) break;
+                uint64_t z = 0;
+                for (int j = 0; j < d; ++j) z = z * s_dim[j] + s_col[j][s];
+                if (!zinsert(keys, cap, z, &s_distinct) || *(volatile int *)&s_distinct > (int)(cap / 2))
+                    s_over = 1;
+            }
+            __syncthreads();
+            if (!s_over || attempt == 1) break;
+            keys = gkeys;
+            ids = gids;
+            cap = gcap;
+            __syncthreads();
+        }
+        if (s_over) {  // cannot happen with cap >= 2 S; flag instead of guessing
+            if (tid == 0) {
+                a.flag[item] = 2;
+                atomicAdd(&a.stats[ST_UNSUPPORTED], 1ull);
+            }
+            __syncthreads();
+            continue;
+        }
+        // compact ids in slot order (block-wide exclusive scan over the slots)
+        const uint32_t per_t = (cap + kThreads - 1) / kThreads;
+        const uint32_t b0 = min(cap, tid * per_t), b1 = min(cap, b0 + per_t);
+        int cnt = 0;
+        for (uint32_t i = b0; i < b1; ++i) cnt += keys[i] != kEmptyKey;
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) s_wsum[warp] = incl;
+        __syncthreads();
+        if (tid == 0) {
+            int acc = 0;
+            for (int w = 0; w < kWarps; ++w) {
+                int t = s_wsum[w];
+                s_wsum[w] = acc;
+                acc += t;
+            }
+            s_base = acc;  // total observed strata
+        }
+        __syncthreads();
+        int id = s_wsum[warp] + incl - cnt;
+        for (uint32_t i = b0; i < b1; ++i)
+            if (keys[i] != kEmptyKey) {
+                ids[i] = id;
+                if (a.want_hash) gzk[id] = keys[i];
+                ++id;
+            }
+        const int n_obs = s_base;
+        __syncthreads();
+        // phase 2: count the observed strata chunk by chunk
+        const int64_t dxy = (int64_t)dx * dy, per = dxy + dx + dy + 1;
+        int *table;
+        int64_t budget;
+        if ((int64_t)n_obs * per <= (int64_t)kCompactSmemInts) {
+            table = stab;
+            budget = kCompactSmemInts;
+        } else {
+            table = gtab;
+            budget = a.slot_tab_ints;
+        }
+        const int64_t chunk = budget / per;
+        Partial acc{0, 0.0, 0.0, 0.0, 0ull};
+        for (int64_t lo = 0; lo < n_obs; lo += chunk) {
+            const int64_t nz = min((int64_t)n_obs - lo, chunk);
+            for (int64_t i = tid; i < nz * per; i += kThreads) table[i] = 0;
+            __syncthreads();
+            for (int64_t s = tid; s < a.S; s += kThreads) {
+                uint64_t z = 0;
+                for (int j = 0; j < d; ++j) z = z * s_dim[j] + s_col[j][s];
+                const int64_t sid = (int64_t)zlookup(keys, ids, cap, z) - lo;
+                if (sid >= 0 && sid < nz) atomicAdd(&table[(sid * dx + colx[s]) * dy + coly[s]], 1);
+            }
+            __syncthreads();
+            int *ni = table + nz * dxy, *nj = ni + nz * dx, *nk = nj + nz * dy;
+            acc.df += marginals(g, table, ni, nj, nk, dx, dy, nz);
+            acc.g2 += g2_fp64(g, table, ni, nj, nk, dx, dy, nz * dxy);
+            if (a.want_hash) {
+                for (int64_t cell = tid; cell < nz * dxy; cell += kThreads) {
+                    const int O = table[cell];
+                    if (!O) continue;
+                    const int64_t k = cell / dxy;
+                    const int rem = (int)(cell - k * dxy);
+                    acc.hash += cell_mix((gzk[lo + k] * (uint64_t)dx + rem / dy) * (uint64_t)dy + rem % dy, (uint32_t)O);
+                }
+            }
+            __syncthreads();
+        }
+        const Partial r = block_sum(acc, scratch);
+        if (tid == 0) {
+            Verdict v{r.df, r.g2, 1.0, 1, 1, 0.0, r.hash};
+            if (r.df > 0) {
+                v.p = chisq_pvalue(r.g2, r.df);
+                v.indep = v.p > a.alpha;
+            }
+            a.flag[item] = (uint8_t)v.indep;
+            atomicAdd(&a.stats[ST_LARGE], 1ull);
+            if (a.detail) {
+                fpgm_ci_result res;
+                res.table_hash = 0;
+                res.cell_hash = r.hash;
+                res.cells = (int64_t)n_obs * dxy;
+                res.df = (int32_t)r.df;
+                res.independent = v.indep;
+                res.g2 = r.g2;
+                res.p_value = v.p;
+                res.rechecked = 1;
+                res.path = 2;
+                a.detail[item] = res;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- band tables
+__global__ void band_table_kernel(double alpha, double *lo, double *hi, int dfmax) {
+    const int df = blockIdx.x * blockDim.x + threadIdx.x;
+    if (df > dfmax) return;
+    if (df == 0) {
+        lo[0] = 0.0;
+        hi[0] = 0.0;
+        return;
+    }
+    lo[df] = chisq_quantile_upper(alpha + kBand, df);
+    hi[df] = chisq_quantile_upper(alpha - kBand, df);
+}
+
+// ---------------------------------------------------------------- plain: one test, whole grid, one launch
+struct PlainArgs {
+    const uint8_t *cols;
+    int64_t S, S_pad;
+    const uint8_t *card;
+    int32_t ncols;
+    int32_t vars[kMaxCols];  // Horner order: z..., x, y
+    double alpha;
+    BandTables bt;
+    int32_t want_hash;
+    int32_t *gtab;  // zeroed table + marginals
+    int32_t *done;  // ticket counter, reset by the last CTA
+    fpgm_ci_result *out;
+    unsigned long long *stats;
+};
+
+__global__ void __launch_bounds__(kThreads) ci_plain_kernel(PlainArgs p) {
+    extern __shared__ int smem[];
+    __shared__ const uint8_t *s_col[kMaxCols];
+    __shared__ uint32_t s_dim[kMaxCols];
+    __shared__ Partial scratch[kWarps];
+    __shared__ int s_last;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int ncols = p.ncols, d = ncols - 2;
+    if (tid < ncols) {
+        s_dim[tid] = p.card[p.vars[tid]];
+        s_col[tid] = p.cols + (int64_t)p.vars[tid] * p.S_pad;
+    }
+    __syncthreads();
+    int64_t cells = 1;
+    for (int j = 0; j < ncols; ++j) cells *= s_dim[j];
+    const int dx = s_dim[d], dy = s_dim[d + 1];
+    const int64_t dz = cells / (dx * dy);
+    const int64_t marg = dz * (dx + dy + 1);
+    const int64_t nvec = p.S >> 4;
+    const int64_t per = (nvec + gridDim.x - 1) / gridDim.x;
+    const int64_t v0 = min(nvec, per * blockIdx.x), v1 = min(nvec, v0 + per);
+    const bool tail = blockIdx.x == 0;
+    if (cells + marg <= kCtaInts && cells < 65536) {
+        const int stride = (int)cells | 1;
+        int R = 1;
+        for (int r = 32; r >= 2; r >>= 1)
+            if (stride * r <= kCtaInts) { R = r; break; }
+        for (int i = tid; i < stride * R; i += kThreads) smem[i] = 0;
+        __syncthreads();
+        int *mytab = smem + (lane & (R - 1)) * stride;
+        for (int64_t v = v0 + tid; v < v1; v += kThreads) {
+            uint32_t c2[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int j = 0; j < ncols; ++j) horner16(c2, __ldg(reinterpret_cast<const uint4 *>(s_col[j]) + v), s_dim[j]);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                atomicAdd(&mytab[c2[q] & 0xffffu], 1);
+                atomicAdd(&mytab[c2[q] >> 16], 1);
+            }
+        }
+        if (tail)
+            for (int64_t s = (p.S & ~(int64_t)15) + tid; s < p.S; s += kThreads) {
+                uint32_t c = 0;
+                for (int j = 0; j < ncols; ++j) c = c * s_dim[j] + s_col[j][s];
+                atomicAdd(&mytab[c], 1);
+            }
+        __syncthreads();
+        for (int c = tid; c < (int)cells; c += kThreads) {
+            int s = 0;
+            for (int r = 0; r < R; ++r) s += smem[r * stride + c];
+            if (s) atomicAdd(&p.gtab[c], s);
+        }
+    } else {
+        for (int64_t v = v0 * 16 + tid; v < v1 * 16; v += kThreads) {
+            uint32_t c = 0;
+            for (int j = 0; j < ncols; ++j) c = c * s_dim[j] + s_col[j][v];
+            atomicAdd(&p.gtab[c], 1);
+        }
+        if (tail)
+            for (int64_t s = (p.S & ~(int64_t)15) + tid; s < p.S; s += kThreads) {
+                uint32_t c = 0;
+                for (int j = 0; j < ncols; ++j) c = c * s_dim[j] + s_col[j][s];
+                atomicAdd(&p.gtab[c], 1);
+            }
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(p.done, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    int *ct = p.gtab;
+    int *ni = ct + cells, *nj = ni + dz * dx, *nk = nj + dz * dy;
+    const CtaGroup g{tid};
+    const Verdict v = score_dense(g, ct, ni, nj, nk, dx, dy, dz, p.alpha, p.bt, true, p.want_hash != 0, scratch);
+    if (tid == 0) {
+        fpgm_ci_result r;
+        r.table_hash = p.want_hash ? table_hash(ct, cells) : 0;
+        r.cell_hash = v.hash;
+        r.cells = cells;
+        r.df = (int32_t)v.df;
+        r.independent = v.indep;
+        r.g2 = v.g2;
+        r.p_value = v.p;
+        r.rechecked = v.rechecked;
+        r.path = 1;
+        *p.out = r;
+        if (v.rechecked) {
+            atomicAdd(&p.stats[ST_RECHECK], 1ull);
+            if (fabs(v.p - p.alpha) < 1e-12) atomicAdd(&p.stats[ST_NEARTIE], 1ull);
+            atomicMax(&p.stats[ST_MAXDP], (unsigned long long)__double_as_longlong(v.dp));
+        }
+    }
+    __syncthreads();
+    for (int64_t i = tid; i < cells + marg; i += kThreads) ct[i] = 0;
+    if (tid == 0) *p.done = 0;
+}
+
+}  // namespace fpgm

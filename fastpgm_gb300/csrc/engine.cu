@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "ci_device.cuh"
+#include "ci_kernels.cuh"
 #include "fastpgm_gb300.h"
 #include "engine_internal.h"
 
@@ -100,14 +101,9 @@ struct DevBuf {
 };
 
 constexpr int kStatusActive = 0, kStatusRemoved = 1, kStatusKept = 2;
-// device statistics slots
-enum { ST_RECHECK = 0, ST_NEARTIE, ST_LARGE, ST_MAXDP, ST_UNSUPPORTED, ST_DET, ST_EXEC, ST_UNRESOLVED,
-       ST_REMOVED, ST_MAXDEG, ST_NACTIVE, ST_COUNT };
-
-constexpr int kSmemBytes = 96 * 1024;
-constexpr int64_t kSmemBudgetInts = (kSmemBytes / 4);
-constexpr int64_t kLargeIntsPerSlot = (int64_t)1 << 25;  // 128 MB per global-memory slot
-constexpr int kLargeSlots = 16;
+constexpr int64_t kPlainInts = (int64_t)1 << 25;       // plain kernel's global table (128 MB)
+constexpr int64_t kSlotTabInts = (int64_t)1 << 21;     // compact tier: global chunk table per slot (8 MB)
+constexpr int64_t kMaxItems = (int64_t)1 << 22;        // tests per wave
 
 }  // namespace
 
@@ -115,7 +111,7 @@ struct fpgm_engine {
     int device = 0;
     cudaStream_t stream = nullptr;
     int num_sms = 0, ci_blocks = 0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     // data
     int n = 0;
     int64_t S = 0, S_pad = 0;
@@ -124,8 +120,10 @@ struct fpgm_engine {
     DevBuf btab;
     // level workspace
     DevBuf bits, deg, adjl, edges_x, edges_y, pxy, pyx, cntx, total, next, status, seprank, g, off, flag,
-        large_list, counters, stats, scan_tmp, log_pair, log_vars, log_meta, node_cnt, node_off;
-    DevBuf large_ws, plain_ws, tests_buf, detail_buf;
+        counters, stats, scan_tmp, log_pair, log_vars, log_meta, node_cnt, node_off;
+    DevBuf slots, plain_ws, tests_buf, detail_buf, item_vars, lists, band;
+    double band_alpha = -1.0;
+    int n_slots = 0, hash_cap_global = 0;
     // result
     bool has_result = false;
     std::vector<uint8_t> res_adj;
@@ -134,280 +132,6 @@ struct fpgm_engine {
 
 // ------------------------------------------------------------------ kernels
 namespace {
-
-struct WaveArgs {
-    const uint8_t *cols;
-    int64_t S, S_pad;
-    const uint8_t *card;
-    int d;
-    // wave source
-    const int32_t *adjl;
-    int32_t adj_stride;
-    const int32_t *deg;
-    const int32_t *ex, *ey, *pxy, *pyx;
-    const uint64_t *cntx, *next;
-    const int32_t *off;
-    int32_t n_edges;
-    const uint64_t *btab;
-    // explicit source
-    const int32_t *tests;
-    int32_t n_tests;
-    // outputs
-    uint8_t *flag;
-    fpgm_ci_result *detail;
-    int32_t want_hash;
-    int32_t *large_list;
-    int32_t *counters;  // [0] work, [1] large count, [2] large work
-    unsigned long long *stats;
-    double alpha;
-    int32_t *large_ws;
-    int64_t large_stride;
-};
-
-enum { SRC_WAVE = 0, SRC_EXPLICIT = 1 };
-
-__device__ inline int upper_bound_i32(const int32_t *a, int n, int v) {
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (a[mid] <= v) lo = mid + 1; else hi = mid;
-    }
-    return lo;
-}
-
-// thread-0 prologue: item -> descriptor
-template <int kSource>
-__device__ inline void build_desc(const WaveArgs &a, int item, TestDesc &t) {
-    if (kSource == SRC_EXPLICIT) {
-        const int32_t *tt = a.tests + (int64_t)item * (2 + a.d);
-        t.x = tt[0];
-        t.y = tt[1];
-        t.d = a.d;
-        for (int k = 0; k < a.d; ++k) t.z[k] = tt[2 + k];
-    } else {
-        const int e = upper_bound_i32(a.off, a.n_edges + 1, item) - 1;
-        uint64_t rank = a.next[e] + (uint64_t)(item - a.off[e]);
-        t.x = a.ex[e];
-        t.y = a.ey[e];
-        t.d = a.d;
-        if (a.d > 0) {
-            int side_node, skip;
-            if (rank < a.cntx[e]) {
-                side_node = t.x;
-                skip = a.pxy[e];
-            } else {
-                rank -= a.cntx[e];
-                side_node = t.y;
-                skip = a.pyx[e];
-            }
-            int c[kMaxCond];
-            unrank_lex(a.btab, a.deg[side_node] - 1, a.d, rank, c);
-            const int32_t *L = a.adjl + (int64_t)side_node * a.adj_stride;
-            for (int k = 0; k < a.d; ++k) t.z[k] = L[c[k] < skip ? c[k] : c[k] + 1];
-        }
-    }
-    desc_finish(t, a.cols, a.S_pad, a.card, kSmemBudgetInts, kLargeIntsPerSlot);
-}
-
-__device__ inline void record_verdict(const WaveArgs &a, int item, const TestDesc &t, const Verdict &v,
-                                      const int *ct, int path) {
-    a.flag[item] = (uint8_t)v.indep;
-    if (v.rechecked) {
-        atomicAdd(&a.stats[ST_RECHECK], 1ull);
-        if (fabs(v.p - a.alpha) < 1e-12) atomicAdd(&a.stats[ST_NEARTIE], 1ull);
-        atomicMax(&a.stats[ST_MAXDP], (unsigned long long)__double_as_longlong(v.dp));
-    }
-    if (a.detail) {
-        fpgm_ci_result r;
-        r.table_hash = a.want_hash ? table_hash(ct, t.cells) : 0;
-        r.cells = t.cells;
-        r.df = (int32_t)v.df;
-        r.independent = v.indep;
-        r.g2 = v.g2;
-        r.p_value = v.p;
-        r.rechecked = v.rechecked;
-        r.path = path;
-        a.detail[item] = r;
-    }
-}
-
-// Persistent count+score kernel: one CTA per test at a time, shared-memory tables.
-template <int kSource>
-__global__ void __launch_bounds__(kThreads, 2) ci_kernel(WaveArgs a) {
-    extern __shared__ int smem[];
-    __shared__ TestDesc td;
-    __shared__ int s_item;
-    __shared__ Partial scratch[kWarps];
-    const int tid = threadIdx.x;
-    const int T = kSource == SRC_EXPLICIT ? a.n_tests : a.off[a.n_edges];
-    const int64_t nvec = a.S >> 4;
-    for (;;) {
-        if (tid == 0) s_item = atomicAdd(&a.counters[0], 1);
-        __syncthreads();
-        const int item = s_item;
-        if (item >= T) break;
-        if (tid == 0) build_desc<kSource>(a, item, td);
-        __syncthreads();
-        if (td.path != 0) {
-            if (tid == 0) {
-                if (td.path == 1 && a.large_ws != nullptr) {
-                    int slot = atomicAdd(&a.counters[1], 1);
-                    a.large_list[slot] = item;
-                    atomicAdd(&a.stats[ST_LARGE], 1ull);
-                } else {
-                    a.flag[item] = 2;
-                    atomicAdd(&a.stats[ST_UNSUPPORTED], 1ull);
-                }
-            }
-            __syncthreads();
-            continue;
-        }
-        const int64_t tabn = td.cells * td.R;
-        int *tab = smem;
-        int *ct = td.R > 1 ? smem + tabn : smem;
-        int *ni = ct + td.cells;
-        int *nj = ni + td.dz * td.dx;
-        int *nk = nj + td.dz * td.dy;
-        for (int64_t i = tid; i < tabn; i += kThreads) tab[i] = 0;
-        __syncthreads();
-        count_range<false>(td, 0, nvec, true, a.S, tab, tid, kThreads);
-        __syncthreads();
-        if (td.R > 1) {
-            const int R = td.R, Rm = R - 1;
-            for (int64_t c = tid; c < td.cells; c += kThreads) {
-                int s = 0;
-                for (int r = 0; r < R; ++r) s += tab[c * R + ((r + (int)c) & Rm)];
-                ct[c] = s;
-            }
-            __syncthreads();
-        }
-        Verdict v = score_table(td, ct, ni, nj, nk, a.alpha, scratch, tid, kThreads);
-        if (tid == 0) record_verdict(a, item, td, v, ct, 0);
-        __syncthreads();
-    }
-}
-
-// Global-memory tables for tests too large for shared memory: one slot per CTA.
-template <int kSource>
-__global__ void __launch_bounds__(kThreads) ci_large_kernel(WaveArgs a) {
-    __shared__ TestDesc td;
-    __shared__ int s_idx;
-    __shared__ Partial scratch[kWarps];
-    const int tid = threadIdx.x;
-    int *ws = a.large_ws + (int64_t)blockIdx.x * a.large_stride;
-    const int64_t nvec = a.S >> 4;
-    for (;;) {
-        if (tid == 0) s_idx = atomicAdd(&a.counters[2], 1);
-        __syncthreads();
-        const int idx = s_idx;
-        if (idx >= a.counters[1]) break;
-        const int item = a.large_list[idx];
-        if (tid == 0) build_desc<kSource>(a, item, td);
-        __syncthreads();
-        int *tab = ws;
-        int *ni = tab + td.cells;
-        int *nj = ni + td.dz * td.dx;
-        int *nk = nj + td.dz * td.dy;
-        const int64_t tot = td.cells + td.dz * (td.dx + td.dy + 1);
-        for (int64_t i = tid; i < tot; i += kThreads) tab[i] = 0;
-        __syncthreads();
-        count_range<true>(td, 0, nvec, true, a.S, tab, tid, kThreads);
-        __threadfence_block();
-        __syncthreads();
-        Verdict v = score_table(td, tab, ni, nj, nk, a.alpha, scratch, tid, kThreads);
-        if (tid == 0) record_verdict(a, item, td, v, tab, 1);
-        __syncthreads();
-    }
-}
-
-// ---- plain: one test, whole grid, one launch
-struct PlainArgs {
-    const uint8_t *cols;
-    int64_t S, S_pad;
-    const uint8_t *card;
-    int32_t x, y, d;
-    int32_t z[kMaxCond];
-    double alpha;
-    int32_t want_hash;
-    int32_t *gtab;         // zeroed table + marginals (large_stride ints)
-    int32_t *done;         // ticket counter, reset by the last CTA
-    fpgm_ci_result *out;
-    unsigned long long *stats;
-};
-
-__global__ void __launch_bounds__(kThreads) ci_plain_kernel(PlainArgs p) {
-    extern __shared__ int smem[];
-    __shared__ TestDesc td;
-    __shared__ Partial scratch[kWarps];
-    __shared__ int s_last;
-    const int tid = threadIdx.x;
-    if (tid == 0) {
-        td.x = p.x;
-        td.y = p.y;
-        td.d = p.d;
-        for (int k = 0; k < p.d; ++k) td.z[k] = p.z[k];
-        desc_finish(td, p.cols, p.S_pad, p.card, kSmemBudgetInts, kLargeIntsPerSlot);
-    }
-    __syncthreads();
-    if (td.path == 2) {
-        if (blockIdx.x == 0 && tid == 0) {
-            p.out->independent = 0;
-            p.out->path = 2;
-            p.out->cells = td.cells;
-        }
-        return;
-    }
-    const int64_t nvec = p.S >> 4;
-    const int64_t per = (nvec + gridDim.x - 1) / gridDim.x;
-    const int64_t v0 = min(nvec, per * blockIdx.x), v1 = min(nvec, v0 + per);
-    if (td.path == 0) {
-        const int64_t tabn = td.cells * td.R;
-        for (int64_t i = tid; i < tabn; i += kThreads) smem[i] = 0;
-        __syncthreads();
-        count_range<false>(td, v0, v1, blockIdx.x == 0, p.S, smem, tid, kThreads);
-        __syncthreads();
-        const int R = td.R, Rm = R - 1;
-        for (int64_t c = tid; c < td.cells; c += kThreads) {
-            int s = 0;
-            for (int r = 0; r < R; ++r) s += smem[c * R + ((r + (int)c) & Rm)];
-            if (s) atomicAdd(&p.gtab[c], s);
-        }
-    } else {
-        count_range<true>(td, v0, v1, blockIdx.x == 0, p.S, p.gtab, tid, kThreads);
-    }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = atomicAdd(p.done, 1) == (int)gridDim.x - 1;
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    int *ct = p.gtab;
-    int *ni = ct + td.cells;
-    int *nj = ni + td.dz * td.dx;
-    int *nk = nj + td.dz * td.dy;
-    Verdict v = score_table(td, ct, ni, nj, nk, p.alpha, scratch, tid, kThreads);
-    if (tid == 0) {
-        fpgm_ci_result r;
-        r.table_hash = p.want_hash ? table_hash(ct, td.cells) : 0;
-        r.cells = td.cells;
-        r.df = (int32_t)v.df;
-        r.independent = v.indep;
-        r.g2 = v.g2;
-        r.p_value = v.p;
-        r.rechecked = v.rechecked;
-        r.path = td.path;
-        *p.out = r;
-        if (v.rechecked) {
-            atomicAdd(&p.stats[ST_RECHECK], 1ull);
-            if (fabs(v.p - p.alpha) < 1e-12) atomicAdd(&p.stats[ST_NEARTIE], 1ull);
-            atomicMax(&p.stats[ST_MAXDP], (unsigned long long)__double_as_longlong(v.dp));
-        }
-    }
-    __syncthreads();
-    const int64_t tot = td.cells + td.dz * (td.dx + td.dy + 1);
-    for (int64_t i = tid; i < tot; i += kThreads) ct[i] = 0;
-    if (tid == 0) *p.done = 0;
-}
 
 // ---- data preparation
 // First-appearance ids per column (Dataset.cpp:459-467) and observed cardinality.
@@ -669,11 +393,13 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&e->ev0));
     CK(cudaEventCreate(&e->ev1));
-    CK(cudaFuncSetAttribute(ci_kernel<SRC_WAVE>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-    CK(cudaFuncSetAttribute(ci_kernel<SRC_EXPLICIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    CK(cudaEventCreate(&e->ev2));
+    CK(cudaFuncSetAttribute(ci_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    CK(cudaFuncSetAttribute(ci_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    CK(cudaFuncSetAttribute(ci_compact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     CK(cudaFuncSetAttribute(ci_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     int occ = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ci_kernel<SRC_WAVE>, kThreads, kSmemBytes));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ci_warp_kernel, kThreads, kSmemBytes));
     e->ci_blocks = e->num_sms * std::max(1, occ);
     // binomial table, saturating
     std::vector<uint64_t> bt((size_t)kBinomN * kBinomK, 0);
@@ -699,12 +425,13 @@ extern "C" int fpgm_engine_destroy(fpgm_engine *e) {
     cudaSetDevice(e->device);
     DevBuf *bufs[] = {&e->cols, &e->card, &e->btab, &e->bits, &e->deg, &e->adjl, &e->edges_x, &e->edges_y,
                       &e->pxy, &e->pyx, &e->cntx, &e->total, &e->next, &e->status, &e->seprank, &e->g,
-                      &e->off, &e->flag, &e->large_list, &e->counters, &e->stats, &e->scan_tmp, &e->log_pair,
-                      &e->log_vars, &e->log_meta, &e->node_cnt, &e->node_off, &e->large_ws, &e->plain_ws,
-                      &e->tests_buf, &e->detail_buf};
+                      &e->off, &e->flag, &e->counters, &e->stats, &e->scan_tmp, &e->log_pair,
+                      &e->log_vars, &e->log_meta, &e->node_cnt, &e->node_off, &e->slots, &e->plain_ws,
+                      &e->tests_buf, &e->detail_buf, &e->item_vars, &e->lists, &e->band};
     for (DevBuf *b : bufs) b->release();
     if (e->ev0) cudaEventDestroy(e->ev0);
     if (e->ev1) cudaEventDestroy(e->ev1);
+    if (e->ev2) cudaEventDestroy(e->ev2);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
     return FPGM_OK;
@@ -751,23 +478,19 @@ extern "C" int fpgm_dataset_download(fpgm_engine *e, uint8_t *columns) {
 // ------------------------------------------------------------------ batched skeleton
 namespace {
 
-int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d) {
-    memset(&a, 0, sizeof a);
-    a.cols = e->cols.as<uint8_t>();
-    a.S = e->S;
-    a.S_pad = e->S_pad;
-    a.card = e->card.as<uint8_t>();
-    a.d = d;
-    a.btab = e->btab.as<uint64_t>();
-    a.counters = e->counters.as<int32_t>();
-    a.stats = e->stats.as<unsigned long long>();
-    a.alpha = alpha;
-    a.large_stride = kLargeIntsPerSlot;
+// Band-edge tables for alpha (cached per alpha).
+int ensure_band(fpgm_engine *e, double alpha) {
+    if (e->band_alpha == alpha && e->band.p) return FPGM_OK;
+    RET(e->band.ensure((size_t)2 * (kBandDfMax + 1) * sizeof(double)));
+    double *lo = e->band.as<double>(), *hi = lo + kBandDfMax + 1;
+    band_table_kernel<<<blocks_for(kBandDfMax + 1, 128), 128, 0, e->stream>>>(alpha, lo, hi, kBandDfMax);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(e->stream));
+    e->band_alpha = alpha;
     return FPGM_OK;
 }
 
-// Largest table + marginals a level-d test can need, from the largest cardinality m:
-// m^(d+2) cells and m^d (2m + 1) marginal counters.
+// Largest table + marginals a level-d test can need, from the largest cardinality m.
 int64_t max_table_ints(const std::vector<uint8_t> &card, int d) {
     int64_t m = 1;
     for (uint8_t c : card) m = std::max<int64_t>(m, c);
@@ -779,29 +502,91 @@ int64_t max_table_ints(const std::vector<uint8_t> &card, int d) {
     return dz * m * m + dz * (2 * m + 1);
 }
 
-int run_waves_and_count(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t n_active, fpgm_pc_stats *st,
-                        int level_idx) {
-    (void)alpha;
-    unsigned long long *dstat = e->stats.as<unsigned long long>();
-    // global-memory slots only when a table of this level can outgrow shared memory
-    if (max_table_ints(e->h_card, d) > kSmemBudgetInts) {
-        RET(e->large_ws.ensure((size_t)kLargeSlots * kLargeIntsPerSlot * 4));
-        a.large_ws = e->large_ws.as<int32_t>();
+// Global slots of the compact tier, allocated the first time a level can need them.
+int ensure_slots(fpgm_engine *e) {
+    if (e->slots.p) return FPGM_OK;
+    uint32_t cap = 4096;
+    while ((int64_t)cap < 2 * e->S) cap <<= 1;
+    e->hash_cap_global = (int)cap;
+    e->n_slots = e->num_sms;
+    const size_t slot = (size_t)cap * (8 + 4 + 8) + (size_t)kSlotTabInts * 4;
+    RET(e->slots.ensure(slot * e->n_slots));
+    return FPGM_OK;
+}
+
+int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t items) {
+    memset(&a, 0, sizeof a);
+    a.cols = e->cols.as<uint8_t>();
+    a.S = e->S;
+    a.S_pad = e->S_pad;
+    a.card = e->card.as<uint8_t>();
+    a.d = d;
+    a.btab = e->btab.as<uint64_t>();
+    a.counters = e->counters.as<int32_t>();
+    a.stats = e->stats.as<unsigned long long>();
+    a.alpha = alpha;
+    RET(ensure_band(e, alpha));
+    a.bt.lo = e->band.as<double>();
+    a.bt.hi = a.bt.lo + kBandDfMax + 1;
+    a.bt.dfmax = kBandDfMax;
+    RET(e->item_vars.ensure((size_t)std::max<int64_t>(items, 1) * (2 + d) * 2 + 16));
+    RET(e->lists.ensure((size_t)3 * std::max<int64_t>(items, 1) * 4 + 16));
+    RET(e->flag.ensure((size_t)std::max<int64_t>(items, 1) + 16));
+    a.item_vars = e->item_vars.as<uint16_t>();
+    a.lists = e->lists.as<int32_t>();
+    a.list_cap = std::max<int64_t>(items, 1);
+    a.flag = e->flag.as<uint8_t>();
+    if (max_table_ints(e->h_card, d) > kCtaInts - 64) {
+        RET(ensure_slots(e));
+        a.slot_mem = e->slots.as<char>();
+        a.slot_bytes = (int64_t)e->hash_cap_global * 20 + kSlotTabInts * 4;
+        a.hash_cap_global = e->hash_cap_global;
+        a.slot_tab_ints = kSlotTabInts;
     }
+    return FPGM_OK;
+}
+
+// Classify + the three tiers on the current stream.  Returns launches issued.
+template <int kSource>
+int launch_tiers(fpgm_engine *e, const WaveArgs &a) {
+    classify_kernel<kSource><<<e->ci_blocks, kThreads, 0, e->stream>>>(a);
+    ci_warp_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+    ci_cta_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+    int n = 3;
+    if (a.slot_mem) {
+        ci_compact_kernel<<<e->n_slots, kThreads, kSmemBytes, e->stream>>>(a);
+        ++n;
+    }
+    return n;
+}
+
+int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, fpgm_pc_stats *st, int level_idx,
+                        const WaveArgs &proto) {
+    unsigned long long *dstat = e->stats.as<unsigned long long>();
     int wave = 0;
     int64_t unresolved = n_active;
     size_t scan_bytes = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, e->g.as<int32_t>(), e->off.as<int32_t>(),
                                   (int)(n_active + 1), e->stream);
     RET(e->scan_tmp.ensure(scan_bytes + 16));
-    const int64_t kMaxItems = (int64_t)1 << 24;
     while (unresolved > 0) {
         int64_t q = (int64_t)1 << std::min(wave, 12);
-        int64_t target = (int64_t)e->ci_blocks * 8;
+        const int64_t target = (int64_t)e->ci_blocks * 64;
         if (q * unresolved < target) q = std::min<int64_t>(4096, (target + unresolved - 1) / unresolved);
         if (d == 0) q = 1;
         q = std::max<int64_t>(1, std::min<int64_t>(q, kMaxItems / std::max<int64_t>(1, n_active)));
-        RET(e->flag.ensure((size_t)std::min<int64_t>(kMaxItems, q * n_active) + 16));
+        const int64_t items = std::max<int64_t>(q * n_active, 1);
+        WaveArgs a = proto;
+        RET(wave_args_base(e, a, alpha, d, items));
+        a.adjl = proto.adjl;
+        a.adj_stride = proto.adj_stride;
+        a.deg = proto.deg;
+        a.ex = proto.ex;
+        a.ey = proto.ey;
+        a.pxy = proto.pxy;
+        a.pyx = proto.pyx;
+        a.cntx = proto.cntx;
+        a.next = proto.next;
         wave_plan_kernel<<<blocks_for(n_active + 1, 256), 256, 0, e->stream>>>(
             (int)n_active, e->status.as<uint8_t>(), e->total.as<uint64_t>(), e->next.as<uint64_t>(), (int)q,
             e->g.as<int32_t>());
@@ -812,18 +597,19 @@ int run_waves_and_count(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_
         CK(cudaMemsetAsync(e->counters.p, 0, 64, e->stream));
         a.off = e->off.as<int32_t>();
         a.n_edges = (int32_t)n_active;
-        a.flag = e->flag.as<uint8_t>();
-        a.large_list = e->large_list.as<int32_t>();
         CK(cudaEventRecord(e->ev0, e->stream));
-        ci_kernel<SRC_WAVE><<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+        classify_kernel<SRC_WAVE><<<e->ci_blocks, kThreads, 0, e->stream>>>(a);
+        ci_warp_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+        ci_cta_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
         CK(cudaGetLastError());
-        st->kernel_launches += 3;  // plan, count, reduce
-        if (a.large_ws) {
-            ci_large_kernel<SRC_WAVE><<<kLargeSlots, kThreads, 0, e->stream>>>(a);
+        CK(cudaEventRecord(e->ev1, e->stream));
+        st->kernel_launches += 5;  // plan, classify, warp tier, CTA tier, reduce
+        if (a.slot_mem) {
+            ci_compact_kernel<<<e->n_slots, kThreads, kSmemBytes, e->stream>>>(a);
             CK(cudaGetLastError());
             st->kernel_launches += 1;
         }
-        CK(cudaEventRecord(e->ev1, e->stream));
+        CK(cudaEventRecord(e->ev2, e->stream));
         CK(cudaMemsetAsync(dstat + ST_UNRESOLVED, 0, 8, e->stream));
         wave_reduce_kernel<<<blocks_for(n_active, 256), 256, 0, e->stream>>>(
             (int)n_active, e->off.as<int32_t>(), e->flag.as<uint8_t>(), e->status.as<uint8_t>(),
@@ -834,16 +620,18 @@ int run_waves_and_count(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_
         CK(cudaMemcpyAsync(hs, dstat, sizeof hs, cudaMemcpyDeviceToHost, e->stream));
         CK(cudaMemcpyAsync(&T, e->off.as<int32_t>() + n_active, 4, cudaMemcpyDeviceToHost, e->stream));
         CK(cudaStreamSynchronize(e->stream));
-        float ms = 0.f;
+        float ms = 0.f, ms2 = 0.f;
         CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+        CK(cudaEventElapsedTime(&ms2, e->ev1, e->ev2));
         st->count_ms += ms;
+        st->large_ms += ms2;
         st->count_bytes += (double)T * (2.0 + d) * (double)e->S;
         st->count_launches += 1;
         if (hs[ST_UNSUPPORTED])
             return set_error(FPGM_ERR_UNSUPPORTED,
-                             "level %d: %llu CI test(s) need a joint table beyond %lld cells or a candidate "
-                             "count beyond 2^64 (node degree >= %d)",
-                             d, hs[ST_UNSUPPORTED], (long long)kLargeIntsPerSlot, kBinomN);
+                             "level %d: %llu CI test(s) are outside the engine's limits (joint table beyond 2^62 "
+                             "cells or a node degree >= %d)",
+                             d, hs[ST_UNSUPPORTED], kBinomN);
         unresolved = (int64_t)hs[ST_UNRESOLVED];
         ++wave;
     }
@@ -914,7 +702,6 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
         RET(e->status.ensure(ne));
         RET(e->g.ensure(ne * 4));
         RET(e->off.ensure(ne * 4));
-        RET(e->large_list.ensure((size_t)1 << 26));
         if (n_active > 0) {
             if (d == 0) {
                 level0_edges_kernel<<<blocks_for(E, 256), 256, 0, e->stream>>>(
@@ -932,7 +719,7 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
             st->kernel_launches += 1;
             CK(cudaMemsetAsync(dstat + ST_DET, 0, 8 * 2, e->stream));
             WaveArgs a;
-            wave_args_base(e, a, alpha, d);
+            memset(&a, 0, sizeof a);
             a.adjl = e->adjl.as<int32_t>();
             a.adj_stride = stride;
             a.deg = e->deg.as<int32_t>();
@@ -942,7 +729,7 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
             a.pyx = e->pyx.as<int32_t>();
             a.cntx = e->cntx.as<uint64_t>();
             a.next = e->next.as<uint64_t>();
-            RET(run_waves_and_count(e, a, alpha, d, n_active, st, st->n_levels));
+            RET(run_waves_and_count(e, alpha, d, n_active, st, st->n_levels, a));
         }
         // finalize: removals into the bitset and the removal log
         RET(e->log_vars.ensure((size_t)(var_count + std::max<int64_t>(n_active, 1) * std::max(d, 1)) * 4 + 16, true,
@@ -1032,34 +819,63 @@ int plain_grid(const fpgm_engine *e) {
 int plain_test(fpgm_engine *e, int x, int y, const int *z, int d, double alpha, int want_hash,
                fpgm_ci_result *out, fpgm_pc_stats *st = nullptr) {
     if (!e->plain_ws.p) {
-        RET(e->plain_ws.ensure((size_t)kLargeIntsPerSlot * 4 + 64));
+        RET(e->plain_ws.ensure((size_t)kPlainInts * 4 + 64));
         CK(cudaMemsetAsync(e->plain_ws.p, 0, e->plain_ws.bytes, e->stream));
-        RET(e->detail_buf.ensure(sizeof(fpgm_ci_result) * 64));
     }
-    PlainArgs p;
-    memset(&p, 0, sizeof p);
-    p.cols = e->cols.as<uint8_t>();
-    p.S = e->S;
-    p.S_pad = e->S_pad;
-    p.card = e->card.as<uint8_t>();
-    p.x = x;
-    p.y = y;
-    p.d = d;
-    for (int k = 0; k < d; ++k) p.z[k] = z[k];
-    p.alpha = alpha;
-    p.want_hash = want_hash;
-    p.gtab = e->plain_ws.as<int32_t>();
-    p.done = reinterpret_cast<int32_t *>(e->plain_ws.as<char>() + (size_t)kLargeIntsPerSlot * 4);
-    p.out = e->detail_buf.as<fpgm_ci_result>();
-    p.stats = e->stats.as<unsigned long long>();
-    ci_plain_kernel<<<plain_grid(e), kThreads, kSmemBytes, e->stream>>>(p);
-    CK(cudaGetLastError());
+    RET(e->detail_buf.ensure(sizeof(fpgm_ci_result) * 64));
+    RET(ensure_band(e, alpha));
+    // table size decides: dense grid-wide kernel, or the compact-strata kernel on one CTA
+    double cells = (double)e->h_card[x] * e->h_card[y], dz = 1.0;
+    for (int k = 0; k < d; ++k) dz *= e->h_card[z[k]];
+    cells *= dz;
+    const double need = cells + dz * (e->h_card[x] + e->h_card[y] + 1);
+    if (need <= (double)kPlainInts) {
+        PlainArgs p;
+        memset(&p, 0, sizeof p);
+        p.cols = e->cols.as<uint8_t>();
+        p.S = e->S;
+        p.S_pad = e->S_pad;
+        p.card = e->card.as<uint8_t>();
+        p.ncols = d + 2;
+        for (int k = 0; k < d; ++k) p.vars[k] = z[k];
+        p.vars[d] = x;
+        p.vars[d + 1] = y;
+        p.alpha = alpha;
+        p.bt.lo = e->band.as<double>();
+        p.bt.hi = p.bt.lo + kBandDfMax + 1;
+        p.bt.dfmax = kBandDfMax;
+        p.want_hash = want_hash;
+        p.gtab = e->plain_ws.as<int32_t>();
+        p.done = reinterpret_cast<int32_t *>(e->plain_ws.as<char>() + (size_t)kPlainInts * 4);
+        p.out = e->detail_buf.as<fpgm_ci_result>();
+        p.stats = e->stats.as<unsigned long long>();
+        ci_plain_kernel<<<plain_grid(e), kThreads, kSmemBytes, e->stream>>>(p);
+        CK(cudaGetLastError());
+    } else {
+        WaveArgs a;
+        RET(wave_args_base(e, a, alpha, d, 1));
+        RET(ensure_slots(e));
+        a.slot_mem = e->slots.as<char>();
+        a.slot_bytes = (int64_t)e->hash_cap_global * 20 + kSlotTabInts * 4;
+        a.hash_cap_global = e->hash_cap_global;
+        a.slot_tab_ints = kSlotTabInts;
+        a.detail = e->detail_buf.as<fpgm_ci_result>();
+        a.want_hash = want_hash;
+        uint16_t iv[kMaxCols];
+        for (int k = 0; k < d; ++k) iv[k] = (uint16_t)z[k];
+        iv[d] = (uint16_t)x;
+        iv[d + 1] = (uint16_t)y;
+        int32_t ctr[C_COUNT] = {0, 0, 1, 0, 0, 0};
+        int32_t zero = 0;
+        CK(cudaMemcpyAsync(a.item_vars, iv, (d + 2) * 2, cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemcpyAsync(a.lists + 2 * a.list_cap, &zero, 4, cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemcpyAsync(a.counters, ctr, sizeof ctr, cudaMemcpyHostToDevice, e->stream));
+        ci_compact_kernel<<<1, kThreads, kSmemBytes, e->stream>>>(a);
+        CK(cudaGetLastError());
+    }
     if (st) st->kernel_launches += 1;
-    CK(cudaMemcpyAsync(out, p.out, sizeof(fpgm_ci_result), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaMemcpyAsync(out, e->detail_buf.p, sizeof(fpgm_ci_result), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
-    if (out->path == 2)
-        return set_error(FPGM_ERR_UNSUPPORTED, "CI test (%d,%d|%d vars) needs a %lld-cell table, beyond %lld", x, y,
-                         d, (long long)out->cells, (long long)kLargeIntsPerSlot);
     return FPGM_OK;
 }
 
@@ -1201,36 +1017,24 @@ extern "C" int fpgm_ci_test_batch(fpgm_engine *e, const int32_t *tests, int32_t 
     CK(cudaSetDevice(e->device));
     RET(e->tests_buf.ensure((size_t)n_tests * (2 + d) * 4));
     RET(e->detail_buf.ensure((size_t)n_tests * sizeof(fpgm_ci_result)));
-    RET(e->flag.ensure((size_t)n_tests + 16));
-    RET(e->large_list.ensure((size_t)n_tests * 4 + 16));
     CK(cudaMemcpyAsync(e->tests_buf.p, tests, (size_t)n_tests * (2 + d) * 4, cudaMemcpyHostToDevice, e->stream));
     CK(cudaMemsetAsync(e->counters.p, 0, 64, e->stream));
     CK(cudaMemsetAsync(e->stats.p, 0, ST_COUNT * 8, e->stream));
     WaveArgs a;
-    wave_args_base(e, a, alpha, d);
+    RET(wave_args_base(e, a, alpha, d, n_tests));
     a.tests = e->tests_buf.as<int32_t>();
     a.n_tests = n_tests;
-    a.flag = e->flag.as<uint8_t>();
     a.detail = e->detail_buf.as<fpgm_ci_result>();
     a.want_hash = want_hash;
-    a.large_list = e->large_list.as<int32_t>();
-    if (max_table_ints(e->h_card, d) > kSmemBudgetInts) {
-        RET(e->large_ws.ensure((size_t)kLargeSlots * kLargeIntsPerSlot * 4));
-        a.large_ws = e->large_ws.as<int32_t>();
-    }
-    ci_kernel<SRC_EXPLICIT><<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+    launch_tiers<SRC_EXPLICIT>(e, a);
     CK(cudaGetLastError());
-    if (a.large_ws) {
-        ci_large_kernel<SRC_EXPLICIT><<<kLargeSlots, kThreads, 0, e->stream>>>(a);
-        CK(cudaGetLastError());
-    }
     unsigned long long hs[ST_COUNT];
     CK(cudaMemcpyAsync(out, a.detail, (size_t)n_tests * sizeof(fpgm_ci_result), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaMemcpyAsync(hs, e->stats.p, sizeof hs, cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     if (hs[ST_UNSUPPORTED])
-        return set_error(FPGM_ERR_UNSUPPORTED, "%llu CI test(s) need a joint table beyond %lld cells",
-                         hs[ST_UNSUPPORTED], (long long)kLargeIntsPerSlot);
+        return set_error(FPGM_ERR_UNSUPPORTED, "%llu CI test(s) need a joint table beyond 2^62 cells",
+                         hs[ST_UNSUPPORTED]);
     return FPGM_OK;
 }
 

@@ -58,14 +58,17 @@ enum { FPGM_MODE_BATCHED = 0, FPGM_MODE_PLAIN = 1 };
 typedef struct fpgm_engine fpgm_engine;
 
 typedef struct {
-    uint64_t table_hash;   /* FNV-1a-64 of the int32 joint table n[z][x][y] in reference cell order (0 if not asked) */
-    int64_t cells;         /* dz * dx * dy */
+    uint64_t table_hash;   /* FNV-1a-64 of the int32 joint table n[z][x][y] in reference cell order
+                              (0 if not asked, and 0 for tests counted by observed strata) */
+    uint64_t cell_hash;    /* order-free fingerprint: sum over nonzero cells of a 64-bit mix of
+                              (cell index in reference order, count) (0 if not asked) */
+    int64_t cells;         /* dz * dx * dy (observed strata * dx * dy on the compact path) */
     int32_t df;            /* adjusted degrees of freedom (IndependenceTest.cpp:96-111) */
     int32_t independent;   /* df == 0 or p > alpha */
     double g2;             /* G^2 the decision used: FP64 when rechecked, else the FP32 compensated sum */
     double p_value;        /* 1 - P(df/2, G^2/2) */
-    int32_t rechecked;     /* 1 when the FP64 recheck band was entered */
-    int32_t path;          /* 0 shared-memory table, 1 global-memory table */
+    int32_t rechecked;     /* 1 when G^2 was computed with FP64 terms (recheck band or compact path) */
+    int32_t path;          /* 0 warp tier, 1 CTA tier or plain kernel, 2 compact strata */
 } fpgm_ci_result;
 
 typedef struct {
@@ -79,8 +82,9 @@ typedef struct {
     int64_t near_ties;           /* FP64 |p - alpha| < 1e-12 (decision could differ from any other FP64 order) */
     int64_t large_tests;         /* tests counted in global memory */
     double max_abs_dp;           /* max |p32 - p64| over rechecked tests */
-    double count_ms;             /* device time of the counting+scoring kernels (CUDA events) */
-    double count_bytes;          /* algorithmic bytes those kernels had to read: sum (2+d) * n_samples */
+    double count_ms;             /* device time of the shared-memory counting+scoring kernel (CUDA events) */
+    double count_bytes;          /* algorithmic bytes its tests read: sum (2+d) * n_samples */
+    double large_ms;             /* device time of the global-memory (large table) kernel */
     int64_t count_launches;      /* launches of the counting+scoring kernels */
     int64_t kernel_launches;     /* launches of this library's own kernels (library scans excluded) */
     double span_ms;              /* CUDA-event span of the whole call on the engine's stream */

@@ -19,7 +19,8 @@ REFERENCE_TREE = "/root/reference"
 
 
 class CIResult(ctypes.Structure):
-    _fields_ = [("table_hash", ctypes.c_uint64), ("cells", ctypes.c_int64), ("df", ctypes.c_int32),
+    _fields_ = [("table_hash", ctypes.c_uint64), ("cell_hash", ctypes.c_uint64), ("cells", ctypes.c_int64),
+                ("df", ctypes.c_int32),
                 ("g2", ctypes.c_double), ("p_value", ctypes.c_double), ("independent", ctypes.c_int32)]
 
 

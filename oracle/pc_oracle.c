@@ -37,7 +37,8 @@
 #include "igamma.h"
 
 typedef struct {
-    uint64_t table_hash; /* FNV-1a-64 over the int32 joint table in reference cell order */
+    uint64_t table_hash; /* FNV-1a-64 over the int32 joint table in reference cell order (0 when sparse) */
+    uint64_t cell_hash;  /* order-free: sum over nonzero cells of mix(cell index, count) */
     int64_t cells;       /* dz * dx * dy */
     int32_t df;
     double g2;
@@ -81,6 +82,98 @@ static uint64_t fnv1a_i32(const int32_t *v, int64_t n) {
     return h;
 }
 
+static uint64_t cell_mix(uint64_t key, uint32_t count) {
+    uint64_t z = key * 0x100000001B3ull + (uint64_t)count + 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+static int cmp_u64(const void *a, const void *b) {
+    uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
+    return x < y ? -1 : x > y;
+}
+
+/* Tables beyond this many cells are counted from sorted cell keys instead of a dense array. */
+#define ORACLE_DENSE_MAX ((int64_t)1 << 24)
+
+static void finish_result(oracle_ci_result *res, double g2, int64_t df, double alpha) {
+    res->df = (int32_t)df;
+    res->g2 = g2;
+    if (df == 0) {
+        res->p_value = 1.0;
+        res->independent = 1;
+    } else {
+        res->p_value = oracle_chisq_pvalue(g2, (int)df);
+        res->independent = res->p_value > alpha;
+    }
+}
+
+/* Same test over the observed cells only: keys (z, x, y) sorted ascending visit the
+ * nonzero cells in the reference's k, i, j loop order, so the FP64 sum is the same. */
+static int ci_test_sparse(int32_t *const *cols, const uint8_t *card, int64_t S, int x, int y, const int *z, int d,
+                          double alpha, oracle_ci_result *res) {
+    const uint64_t dx = card[x], dy = card[y], dxy = dx * dy;
+    uint64_t radix[64], dz = 1;
+    for (int j = d - 1; j >= 0; --j) {
+        radix[j] = dz;
+        dz *= card[z[j]];
+    }
+    uint64_t *keys = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)S);
+    int32_t *ni = (int32_t *)calloc(dx, sizeof(int32_t)), *nj = (int32_t *)calloc(dy, sizeof(int32_t));
+    if (!keys || !ni || !nj) {
+        free(keys); free(ni); free(nj);
+        return -1;
+    }
+    for (int64_t s = 0; s < S; ++s) {
+        uint64_t zc = 0;
+        for (int j = 0; j < d; ++j) zc += (uint64_t)cols[z[j]][s] * radix[j];
+        keys[s] = (zc * dx + (uint64_t)cols[x][s]) * dy + (uint64_t)cols[y][s];
+    }
+    qsort(keys, (size_t)S, sizeof(uint64_t), cmp_u64);
+    double g2 = 0.0;
+    int64_t df = 0;
+    uint64_t h = 0;
+    int64_t a = 0;
+    while (a < S) { /* one stratum: keys with the same key / dxy */
+        const uint64_t zk = keys[a] / dxy;
+        int64_t b = a;
+        while (b < S && keys[b] / dxy == zk) ++b;
+        memset(ni, 0, sizeof(int32_t) * dx);
+        memset(nj, 0, sizeof(int32_t) * dy);
+        for (int64_t t = a; t < b; ++t) {
+            const uint64_t c = keys[t] % dxy;
+            ni[c / dy]++;
+            nj[c % dy]++;
+        }
+        int alx = 0, aly = 0;
+        for (uint64_t i = 0; i < dx; ++i) alx += ni[i] > 0;
+        for (uint64_t j = 0; j < dy; ++j) aly += nj[j] > 0;
+        alx = alx >= 1 ? alx : 1;
+        aly = aly >= 1 ? aly : 1;
+        df += (int64_t)(alx - 1) * (aly - 1);
+        const long total = (long)(b - a);
+        int64_t t = a;
+        while (t < b) {
+            int64_t u = t;
+            while (u < b && keys[u] == keys[t]) ++u;
+            const uint64_t c = keys[t] % dxy;
+            const long obs = (long)(u - t), row = ni[c / dy], col = nj[c % dy];
+            const double expected = (double)col * (double)row / (double)total;
+            g2 += 2.0 * obs * log(obs / expected);
+            h += cell_mix(keys[t], (uint32_t)obs);
+            t = u;
+        }
+        a = b;
+    }
+    res->cells = (int64_t)(dz * dxy);
+    res->table_hash = 0;
+    res->cell_hash = h;
+    finish_result(res, g2, df, alpha);
+    free(keys); free(ni); free(nj);
+    return 0;
+}
+
 /* One CI test on int32 columns.  Returns 0, or -1 if the table cannot be allocated. */
 static int ci_test_cols(int32_t *const *cols, const uint8_t *card, int64_t S, int x, int y,
                         const int *z, int d, double alpha, int want_hash, oracle_ci_result *res) {
@@ -88,10 +181,13 @@ static int ci_test_cols(int32_t *const *cols, const uint8_t *card, int64_t S, in
     /* mixed radix over Z, last variable fastest (CellTable.cpp:39-51) */
     int64_t dz = 1;
     int64_t radix[64];
+    double dzf = 1.0;
     for (int j = d - 1; j >= 0; --j) {
         radix[j] = dz;
         dz *= card[z[j]];
+        dzf *= card[z[j]];
     }
+    if (dzf * dx * dy > (double)ORACLE_DENSE_MAX) return ci_test_sparse(cols, card, S, x, y, z, d, alpha, res);
     const int64_t cells = dz * dx * dy;
     int32_t *n = (int32_t *)calloc((size_t)cells, sizeof(int32_t));
     int32_t *ni = (int32_t *)calloc((size_t)(dz * dx), sizeof(int32_t));
@@ -145,15 +241,12 @@ static int ci_test_cols(int32_t *const *cols, const uint8_t *card, int64_t S, in
     }
     res->cells = cells;
     res->table_hash = want_hash ? fnv1a_i32(n, cells) : 0;
-    res->df = (int32_t)df;
-    res->g2 = g2;
-    if (df == 0) {
-        res->p_value = 1.0;
-        res->independent = 1;
-    } else {
-        res->p_value = oracle_chisq_pvalue(g2, (int)df);
-        res->independent = res->p_value > alpha;
-    }
+    uint64_t h = 0;
+    if (want_hash)
+        for (int64_t c = 0; c < cells; ++c)
+            if (n[c]) h += cell_mix((uint64_t)c, (uint32_t)n[c]);
+    res->cell_hash = h;
+    finish_result(res, g2, df, alpha);
     free(n); free(ni); free(nj); free(nk);
     return 0;
 }

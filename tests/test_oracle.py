@@ -106,3 +106,27 @@ def test_reference_driver_reproduces_shipped_golden(tmp_path):
     O.ref_pc("/root/reference/dataset/alarm/alarm_s5000", str(tmp_path / "a"))
     got = open(tmp_path / "a_struct").read()
     assert got == open(os.path.join(GOLDEN, "alarm_s5000_struct")).read()
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference-built driver needs the reference tree")
+def test_sparse_oracle_path_matches_reference_bit_for_bit(tmp_path):
+    """Tables above 2^24 cells are counted from sorted keys; G^2 must equal the reference's dense loop."""
+    import subprocess
+    import fastpgm_gb300 as F
+    rng = np.random.default_rng(2)
+    S = 20000
+    raw = np.stack([rng.integers(0, 9, S), rng.integers(0, 8, S)] + [rng.integers(0, 64, S) for _ in range(3)])
+    raw[1] = (raw[1] + (raw[0] > 6)) % 8
+    raw = raw.astype(np.uint8)
+    csv = str(tmp_path / "big.csv")
+    F.write_csv(csv, raw)
+    tin, tout = str(tmp_path / "t.txt"), str(tmp_path / "o.txt")
+    with open(tin, "w") as f:
+        f.write("0 1 3 2 3 4\n")
+    subprocess.check_call([O.REF_DRIVER, "tests", csv, "0.05", tin, tout])
+    h, df, g2, p, ind = open(tout).read().split()
+    cols, card = O.relabel(raw)
+    r = O.ci_tests(cols, card, np.array([[0, 1, 2, 3, 4]], dtype=np.int32), 3, threads=1)[0]
+    assert r.cells > (1 << 24) and r.table_hash == 0
+    assert r.df == int(df) and r.independent == int(ind)
+    assert r.g2 == float(g2) and r.p_value == float(p)
