@@ -35,7 +35,7 @@ constexpr int kCompactSmemInts = (kSmemBytes - kHashBytes) / 4;
 constexpr int kBinomN = 4096;
 constexpr int kBinomK = 32;
 constexpr double kBand = 1e-3;
-constexpr int kBandDfMax = 1 << 16;
+constexpr int kBandDfMax = 1 << 15;   // dense tiers have df < cells <= 24,576
 constexpr uint64_t kEmptyKey = ~0ull;
 
 // ---------------------------------------------------------------- p-value (FP64)
