@@ -503,10 +503,13 @@ int64_t max_table_ints(const std::vector<uint8_t> &card, int d) {
 }
 
 // Global slots of the compact tier, allocated the first time a level can need them.
+// The global strata hash must hold every sample's stratum at load <= 1/2, so it is
+// resized whenever a dataset with more samples is uploaded.
 int ensure_slots(fpgm_engine *e) {
-    if (e->slots.p) return FPGM_OK;
     uint32_t cap = 4096;
     while ((int64_t)cap < 2 * e->S) cap <<= 1;
+    if (e->slots.p && (uint32_t)e->hash_cap_global >= cap) return FPGM_OK;
+    e->slots.release();
     e->hash_cap_global = (int)cap;
     e->n_slots = e->num_sms;
     const size_t slot = (size_t)cap * (8 + 4 + 8) + (size_t)kSlotTabInts * 4;
