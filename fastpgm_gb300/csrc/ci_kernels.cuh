@@ -5,10 +5,10 @@
 //   tier 0  ci_warp_kernel     one warp per test, table + marginals in a 12 KB
 //                              per-warp slice of shared memory (<= 3072 ints)
 //   tier 1  ci_cta_kernel      one CTA per test, table in 96 KB of shared memory
-//   tier 2  ci_compact_kernel  one CTA per test; the observed Z strata are first
-//                              hashed to compact ids (shared-memory hash, global
-//                              fallback), then counted stratum-chunk by chunk --
-//                              work O(samples + observed cells), never O(dz)
+//   tier 2  ci_compact_kernel  one CTA per test; the observed Z strata are hashed
+//                              to compact ids, the samples counting-sorted by
+//                              stratum, and one warp per stratum scores it --
+//                              work O(samples), never O(dz) or O(strata * dx * dy)
 //
 // Tiers 0/1 count with 128-bit column loads folded into packed 16-bit Horner
 // codes (two samples per 32-bit multiply-add) and shared-memory atomics into R
@@ -60,7 +60,6 @@ struct WaveArgs {
     char *slot_mem;
     int64_t slot_bytes;
     int32_t hash_cap_global;  // power of two >= 2 * n_samples
-    int64_t slot_tab_ints;
 };
 
 __device__ inline int upper_bound_i32(const int32_t *a, int n, int v) {
@@ -330,26 +329,73 @@ __device__ inline int zlookup(const uint64_t *keys, const int *ids, uint32_t cap
     return -1;
 }
 
+// Block-wide exclusive scan of n ints in place (any n), each thread a contiguous chunk.
+// Returns the total.  s_w: kWarps ints of shared scratch.
+__device__ inline int block_exclusive_scan(int *v, int n, int *s_w) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int per = (n + kThreads - 1) / kThreads;
+    const int b0 = min(n, tid * per), b1 = min(n, b0 + per);
+    int sum = 0;
+    for (int i = b0; i < b1; ++i) sum += v[i];
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    __syncthreads();
+    if (lane == 31) s_w[warp] = incl;
+    __syncthreads();
+    int base = 0, total = 0;
+    for (int w = 0; w < kWarps; ++w) {
+        if (w < warp) base += s_w[w];
+        total += s_w[w];
+    }
+    int run = base + incl - sum;
+    for (int i = b0; i < b1; ++i) {
+        const int t = v[i];
+        v[i] = run;
+        run += t;
+    }
+    __syncthreads();
+    return total;
+}
+
+// Tier 2: joint tables too large for shared memory, counted in O(samples):
+//  1. the observed Z strata are hashed to compact ids (shared-memory hash,
+//     global fallback sized >= 2 n_samples);
+//  2. samples are counting-sorted by stratum (x*dy + y codes);
+//  3. one warp per stratum counts its x,y cells in a small dense table and
+//     reads each touched cell back with atomicExch(.., 0), so every distinct
+//     cell contributes exactly once and the table is left zeroed; the
+//     stratum's df and FP64 G^2 terms (the reference's formula) follow.
 __global__ void __launch_bounds__(kThreads) ci_compact_kernel(WaveArgs a) {
-    extern __shared__ int smem[];
-    uint64_t *hkeys = reinterpret_cast<uint64_t *>(smem);
-    int *hids = reinterpret_cast<int *>(hkeys + kHashCap);
-    int *stab = hids + kHashCap;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint64_t *hkeys = reinterpret_cast<uint64_t *>(smem_raw);
+    int *hids = reinterpret_cast<int *>(smem_raw + kHashCap * 8);
+    int *scnt = reinterpret_cast<int *>(smem_raw + kHashCap * 12);   // kSmemStrata + 1 entries
+    int *scur = scnt + (kSmemStrata + 1);
+    int *swt = reinterpret_cast<int *>(smem_raw + kSparseWarpTabOffset);
     __shared__ const uint8_t *s_col[kMaxCols];
     __shared__ uint32_t s_dim[kMaxCols];
-    __shared__ int s_idx, s_over, s_distinct, s_base;
-    __shared__ int s_wsum[kWarps];
+    __shared__ int s_idx, s_over, s_distinct;
+    __shared__ int s_w[kWarps];
     __shared__ Partial scratch[kWarps];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t S = a.S;
     const uint32_t gcap = (uint32_t)a.hash_cap_global;
     char *slot = a.slot_mem + (int64_t)blockIdx.x * a.slot_bytes;
     uint64_t *gkeys = reinterpret_cast<uint64_t *>(slot);
-    int *gids = reinterpret_cast<int *>(gkeys + gcap);
-    uint64_t *gzk = reinterpret_cast<uint64_t *>(gids + gcap);
-    int *gtab = reinterpret_cast<int *>(gzk + gcap);
+    uint64_t *gzk = gkeys + gcap;
+    int *gids = reinterpret_cast<int *>(gzk + gcap);
+    int *gcnt = gids + gcap;                  // S + 1
+    int *gcur = gcnt + (S + 1);               // S + 1
+    int *gsid = gcur + (S + 1);               // S
+    int *gwt = gsid + S;                      // kWarps * kGlobalWarpTab, kept zeroed
+    uint16_t *gord = reinterpret_cast<uint16_t *>(gwt + (int64_t)kWarps * kGlobalWarpTab);  // S
     const int n2 = a.counters[C_TIER2];
     const int d = a.d, ncols = d + 2;
-    const CtaGroup g{tid};
+    for (int i = tid; i < kWarps * kSparseWarpTab; i += kThreads) swt[i] = 0;
     for (;;) {
         if (tid == 0) s_idx = atomicAdd(&a.counters[C_WORK2], 1);
         __syncthreads();
@@ -364,7 +410,7 @@ __global__ void __launch_bounds__(kThreads) ci_compact_kernel(WaveArgs a) {
         __syncthreads();
         const int dx = s_dim[d], dy = s_dim[d + 1];
         const uint8_t *colx = s_col[d], *coly = s_col[d + 1];
-        // phase 1: observed strata -> hash (shared, then global if it fills up)
+        // 1. strata -> hash (shared, then global if it fills up)
         uint64_t *keys = hkeys;
         int *ids = hids;
         uint32_t cap = kHashCap;
@@ -375,12 +421,12 @@ __global__ void __launch_bounds__(kThreads) ci_compact_kernel(WaveArgs a) {
                 s_distinct = 0;
             }
             __syncthreads();
-            for (int64_t s = tid; s < a.S; s += kThreads) {
+            const int limit = attempt == 0 ? kSmemStrata : (int)(cap / 2);
+            for (int64_t s = tid; s < S; s += kThreads) {
                 if (*(volatile int *)&s_over) break;
                 uint64_t z = 0;
                 for (int j = 0; j < d; ++j) z = z * s_dim[j] + s_col[j][s];
-                if (!zinsert(keys, cap, z, &s_distinct) || *(volatile int *)&s_distinct > (int)(cap / 2))
-                    s_over = 1;
+                if (!zinsert(keys, cap, z, &s_distinct) || *(volatile int *)&s_distinct > limit) s_over = 1;
             }
             __syncthreads();
             if (!s_over || attempt == 1) break;
@@ -397,75 +443,96 @@ __global__ void __launch_bounds__(kThreads) ci_compact_kernel(WaveArgs a) {
             __syncthreads();
             continue;
         }
-        // compact ids in slot order (block-wide exclusive scan over the slots)
-        const uint32_t per_t = (cap + kThreads - 1) / kThreads;
-        const uint32_t b0 = min(cap, tid * per_t), b1 = min(cap, b0 + per_t);
-        int cnt = 0;
-        for (uint32_t i = b0; i < b1; ++i) cnt += keys[i] != kEmptyKey;
-        int incl = cnt;
+        // compact ids in slot order
+        {
+            const uint32_t per_t = (cap + kThreads - 1) / kThreads;
+            const uint32_t b0 = min(cap, tid * per_t), b1 = min(cap, b0 + per_t);
+            int cnt = 0;
+            for (uint32_t i = b0; i < b1; ++i) cnt += keys[i] != kEmptyKey;
+            int incl = cnt;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
-        }
-        if (lane == 31) s_wsum[warp] = incl;
-        __syncthreads();
-        if (tid == 0) {
-            int acc = 0;
-            for (int w = 0; w < kWarps; ++w) {
-                int t = s_wsum[w];
-                s_wsum[w] = acc;
-                acc += t;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
             }
-            s_base = acc;  // total observed strata
+            if (lane == 31) s_w[warp] = incl;
+            __syncthreads();
+            int base = 0;
+            for (int w = 0; w < warp; ++w) base += s_w[w];
+            int id = base + incl - cnt;
+            for (uint32_t i = b0; i < b1; ++i)
+                if (keys[i] != kEmptyKey) {
+                    ids[i] = id;
+                    if (a.want_hash) gzk[id] = keys[i];
+                    ++id;
+                }
+            __syncthreads();
+        }
+        const int n_obs = s_distinct;
+        const bool small = n_obs <= kSmemStrata;
+        int *cnt = small ? scnt : gcnt;
+        int *cur = small ? scur : gcur;
+        // 2. counting sort of the samples by stratum
+        for (int i = tid; i <= n_obs; i += kThreads) cnt[i] = 0;
+        __syncthreads();
+        for (int64_t s = tid; s < S; s += kThreads) {
+            uint64_t z = 0;
+            for (int j = 0; j < d; ++j) z = z * s_dim[j] + s_col[j][s];
+            const int sid = zlookup(keys, ids, cap, z);
+            gsid[s] = sid;
+            atomicAdd(&cnt[sid], 1);
         }
         __syncthreads();
-        int id = s_wsum[warp] + incl - cnt;
-        for (uint32_t i = b0; i < b1; ++i)
-            if (keys[i] != kEmptyKey) {
-                ids[i] = id;
-                if (a.want_hash) gzk[id] = keys[i];
-                ++id;
-            }
-        const int n_obs = s_base;
+        block_exclusive_scan(cnt, n_obs + 1, s_w);  // cnt -> stratum offsets, cnt[n_obs] = S
+        for (int i = tid; i <= n_obs; i += kThreads) cur[i] = cnt[i];
         __syncthreads();
-        // phase 2: count the observed strata chunk by chunk
-        const int64_t dxy = (int64_t)dx * dy, per = dxy + dx + dy + 1;
-        int *table;
-        int64_t budget;
-        if ((int64_t)n_obs * per <= (int64_t)kCompactSmemInts) {
-            table = stab;
-            budget = kCompactSmemInts;
-        } else {
-            table = gtab;
-            budget = a.slot_tab_ints;
+        for (int64_t s = tid; s < S; s += kThreads) {
+            const int pos = atomicAdd(&cur[gsid[s]], 1);
+            gord[pos] = (uint16_t)(colx[s] * dy + coly[s]);
         }
-        const int64_t chunk = budget / per;
+        __syncthreads();
+        // 3. one warp per stratum
+        const int dxy = dx * dy;
+        const bool wsmem = dxy + dx + dy <= kSparseWarpTab;
+        int *wt = wsmem ? swt + warp * kSparseWarpTab : gwt + (int64_t)warp * kGlobalWarpTab;
+        int *wni = wt + dxy, *wnj = wni + dx;
         Partial acc{0, 0.0, 0.0, 0.0, 0ull};
-        for (int64_t lo = 0; lo < n_obs; lo += chunk) {
-            const int64_t nz = min((int64_t)n_obs - lo, chunk);
-            for (int64_t i = tid; i < nz * per; i += kThreads) table[i] = 0;
-            __syncthreads();
-            for (int64_t s = tid; s < a.S; s += kThreads) {
-                uint64_t z = 0;
-                for (int j = 0; j < d; ++j) z = z * s_dim[j] + s_col[j][s];
-                const int64_t sid = (int64_t)zlookup(keys, ids, cap, z) - lo;
-                if (sid >= 0 && sid < nz) atomicAdd(&table[(sid * dx + colx[s]) * dy + coly[s]], 1);
+        for (int k = warp; k < n_obs; k += kWarps) {
+            const int o0 = cnt[k], o1 = cnt[k + 1];
+            const int m = o1 - o0;
+            int ax = 0, ay = 0;
+            for (int i = o0 + lane; i < o1; i += 32) {
+                const int c = gord[i];
+                const int x = c / dy, y = c - x * dy;
+                atomicAdd(&wt[c], 1);
+                ax += atomicAdd(&wni[x], 1) == 0;
+                ay += atomicAdd(&wnj[y], 1) == 0;
             }
-            __syncthreads();
-            int *ni = table + nz * dxy, *nj = ni + nz * dx, *nk = nj + nz * dy;
-            acc.df += marginals(g, table, ni, nj, nk, dx, dy, nz);
-            acc.g2 += g2_fp64(g, table, ni, nj, nk, dx, dy, nz * dxy);
-            if (a.want_hash) {
-                for (int64_t cell = tid; cell < nz * dxy; cell += kThreads) {
-                    const int O = table[cell];
-                    if (!O) continue;
-                    const int64_t k = cell / dxy;
-                    const int rem = (int)(cell - k * dxy);
-                    acc.hash += cell_mix((gzk[lo + k] * (uint64_t)dx + rem / dy) * (uint64_t)dy + rem % dy, (uint32_t)O);
+            __syncwarp();
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                ax += __shfl_xor_sync(0xffffffffu, ax, o);
+                ay += __shfl_xor_sync(0xffffffffu, ay, o);
+            }
+            if (lane == 0) acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
+            for (int i = o0 + lane; i < o1; i += 32) {
+                const int c = gord[i];
+                const int O = atomicExch(&wt[c], 0);
+                if (O > 0) {
+                    const int x = c / dy, y = c - x * dy;
+                    const double expected = (double)wnj[y] * (double)wni[x] / (double)m;
+                    acc.g2 += 2.0 * O * log(O / expected);
+                    if (a.want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x) * (uint64_t)dy + y, (uint32_t)O);
                 }
             }
-            __syncthreads();
+            __syncwarp();
+            for (int i = o0 + lane; i < o1; i += 32) {
+                const int c = gord[i];
+                const int x = c / dy;
+                wni[x] = 0;
+                wnj[c - x * dy] = 0;
+            }
+            __syncwarp();
         }
         const Partial r = block_sum(acc, scratch);
         if (tid == 0) {
@@ -492,6 +559,11 @@ __global__ void __launch_bounds__(kThreads) ci_compact_kernel(WaveArgs a) {
         }
         __syncthreads();
     }
+}
+
+// Bytes of one compact-tier global slot for n_samples samples and a strata hash of cap slots.
+__host__ __device__ inline int64_t compact_slot_bytes(int64_t S, int64_t cap) {
+    return cap * 8 * 2 + cap * 4 + (S + 1) * 4 * 2 + S * 4 + (int64_t)kWarps * kGlobalWarpTab * 4 + S * 2 + 256;
 }
 
 // ---------------------------------------------------------------- band tables

@@ -102,7 +102,6 @@ struct DevBuf {
 
 constexpr int kStatusActive = 0, kStatusRemoved = 1, kStatusKept = 2;
 constexpr int64_t kPlainInts = (int64_t)1 << 25;       // plain kernel's global table (128 MB)
-constexpr int64_t kSlotTabInts = (int64_t)1 << 21;     // compact tier: global chunk table per slot (8 MB)
 constexpr int64_t kMaxItems = (int64_t)1 << 22;        // tests per wave
 
 }  // namespace
@@ -124,6 +123,7 @@ struct fpgm_engine {
     DevBuf slots, plain_ws, tests_buf, detail_buf, item_vars, lists, band;
     double band_alpha = -1.0;
     int n_slots = 0, hash_cap_global = 0;
+    int64_t slot_bytes = 0;
     // result
     bool has_result = false;
     std::vector<uint8_t> res_adj;
@@ -512,8 +512,9 @@ int ensure_slots(fpgm_engine *e) {
     e->slots.release();
     e->hash_cap_global = (int)cap;
     e->n_slots = e->num_sms;
-    const size_t slot = (size_t)cap * (8 + 4 + 8) + (size_t)kSlotTabInts * 4;
-    RET(e->slots.ensure(slot * e->n_slots));
+    e->slot_bytes = (compact_slot_bytes(e->S, cap) + 255) & ~(int64_t)255;
+    RET(e->slots.ensure((size_t)e->slot_bytes * e->n_slots));
+    CK(cudaMemsetAsync(e->slots.p, 0, (size_t)e->slot_bytes * e->n_slots, e->stream));  // warp tables start zeroed
     return FPGM_OK;
 }
 
@@ -542,9 +543,8 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t ite
     if (max_table_ints(e->h_card, d) > kCtaInts - 64) {
         RET(ensure_slots(e));
         a.slot_mem = e->slots.as<char>();
-        a.slot_bytes = (int64_t)e->hash_cap_global * 20 + kSlotTabInts * 4;
+        a.slot_bytes = e->slot_bytes;
         a.hash_cap_global = e->hash_cap_global;
-        a.slot_tab_ints = kSlotTabInts;
     }
     return FPGM_OK;
 }
@@ -859,9 +859,8 @@ int plain_test(fpgm_engine *e, int x, int y, const int *z, int d, double alpha, 
         RET(wave_args_base(e, a, alpha, d, 1));
         RET(ensure_slots(e));
         a.slot_mem = e->slots.as<char>();
-        a.slot_bytes = (int64_t)e->hash_cap_global * 20 + kSlotTabInts * 4;
+        a.slot_bytes = e->slot_bytes;
         a.hash_cap_global = e->hash_cap_global;
-        a.slot_tab_ints = kSlotTabInts;
         a.detail = e->detail_buf.as<fpgm_ci_result>();
         a.want_hash = want_hash;
         uint16_t iv[kMaxCols];
