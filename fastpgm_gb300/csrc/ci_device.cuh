@@ -34,6 +34,7 @@ constexpr int kSmemStrata = kHashCap / 2;                // strata counted in sh
 constexpr int kSparseWarpTabOffset = kHashCap * 12 + 2 * (kSmemStrata + 1) * 4 + 8;  // 16-aligned
 constexpr int kSparseWarpTab = (kSmemBytes - kSparseWarpTabOffset) / 4 / kWarps;    // ints per warp
 constexpr int kGlobalWarpTab = 255 * 255 + 2 * 255 + 1;  // largest dx*dy + dx + dy
+constexpr int kLaneStratum = 16;                         // strata up to this many samples: one lane each
 constexpr int kBinomN = 4096;
 constexpr int kBinomK = 32;
 constexpr double kBand = 1e-3;

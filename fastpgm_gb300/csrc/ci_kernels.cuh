@@ -365,11 +365,13 @@ __device__ inline int block_exclusive_scan(int *v, int n, int *s_w) {
 //  1. the observed Z strata are hashed to compact ids (shared-memory hash,
 //     global fallback sized >= 2 n_samples);
 //  2. samples are counting-sorted by stratum (x*dy + y codes);
-//  3. one warp per stratum counts its x,y cells in a small dense table and
-//     reads each touched cell back with atomicExch(.., 0), so every distinct
-//     cell contributes exactly once and the table is left zeroed; the
-//     stratum's df and FP64 G^2 terms (the reference's formula) follow.
-__global__ void __launch_bounds__(kThreads) ci_compact_kernel(WaveArgs a) {
+//  3. a stratum of at most kLaneStratum samples is scored by one lane with
+//     pairwise comparisons in registers; a larger one by one warp that counts
+//     its x,y cells in a small dense table and reads each touched cell back
+//     with atomicExch(.., 0), so every distinct cell contributes exactly once
+//     and the table is left zeroed.  Either way the stratum's df and FP64 G^2
+//     terms follow the reference's formula.
+__global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t *hkeys = reinterpret_cast<uint64_t *>(smem_raw);
     int *hids = reinterpret_cast<int *>(smem_raw + kHashCap * 8);
@@ -491,13 +493,51 @@ __global__ void __launch_bounds__(kThreads) ci_compact_kernel(WaveArgs a) {
             gord[pos] = (uint16_t)(colx[s] * dy + coly[s]);
         }
         __syncthreads();
-        // 3. one warp per stratum
+        // 3a. strata of at most kLaneStratum samples: one lane each, pairwise in registers
         const int dxy = dx * dy;
+        Partial acc{0, 0.0, 0.0, 0.0, 0ull};
+        int *big = gsid;  // stratum ids of larger strata (gsid is free after the scatter)
+        if (tid == 0) s_over = 0;
+        __syncthreads();
+        for (int k = tid; k < n_obs; k += kThreads) {
+            const int o0 = cnt[k], m = cnt[k + 1] - o0;
+            if (m > kLaneStratum) {
+                big[atomicAdd(&s_over, 1)] = k;
+                continue;
+            }
+            uint16_t c[kLaneStratum];
+#pragma unroll
+            for (int i = 0; i < kLaneStratum; ++i)
+                if (i < m) c[i] = gord[o0 + i];
+            int ax = 0, ay = 0;
+            for (int i = 0; i < m; ++i) {
+                const int xi = c[i] / dy, yi = c[i] - xi * dy;
+                int O = 0, Nx = 0, Ny = 0;
+                bool fc = true, fx = true, fy = true;
+                for (int j = 0; j < m; ++j) {
+                    const int xj = c[j] / dy, yj = c[j] - xj * dy;
+                    if (c[j] == c[i]) { ++O; fc &= j >= i; }
+                    if (xj == xi) { ++Nx; fx &= j >= i; }
+                    if (yj == yi) { ++Ny; fy &= j >= i; }
+                }
+                ax += fx;
+                ay += fy;
+                if (fc) {
+                    const double expected = (double)Ny * (double)Nx / (double)m;
+                    acc.g2 += 2.0 * O * log(O / expected);
+                    if (a.want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + xi) * (uint64_t)dy + yi, (uint32_t)O);
+                }
+            }
+            acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
+        }
+        __syncthreads();
+        const int n_big = s_over;
+        // 3b. larger strata: one warp each, dense x,y table read back with atomicExch
         const bool wsmem = dxy + dx + dy <= kSparseWarpTab;
         int *wt = wsmem ? swt + warp * kSparseWarpTab : gwt + (int64_t)warp * kGlobalWarpTab;
         int *wni = wt + dxy, *wnj = wni + dx;
-        Partial acc{0, 0.0, 0.0, 0.0, 0ull};
-        for (int k = warp; k < n_obs; k += kWarps) {
+        for (int b = warp; b < n_big; b += kWarps) {
+            const int k = big[b];
             const int o0 = cnt[k], o1 = cnt[k + 1];
             const int m = o1 - o0;
             int ax = 0, ay = 0;

@@ -511,7 +511,7 @@ int ensure_slots(fpgm_engine *e) {
     if (e->slots.p && (uint32_t)e->hash_cap_global >= cap) return FPGM_OK;
     e->slots.release();
     e->hash_cap_global = (int)cap;
-    e->n_slots = e->num_sms;
+    e->n_slots = 2 * e->num_sms;
     e->slot_bytes = (compact_slot_bytes(e->S, cap) + 255) & ~(int64_t)255;
     RET(e->slots.ensure((size_t)e->slot_bytes * e->n_slots));
     CK(cudaMemsetAsync(e->slots.p, 0, (size_t)e->slot_bytes * e->n_slots, e->stream));  // warp tables start zeroed
