@@ -300,33 +300,58 @@ __device__ __forceinline__ uint32_t zhash(uint64_t z, uint32_t cap) {
     return (uint32_t)((z * 0x9E3779B97F4A7C15ull) >> 32) & (cap - 1);
 }
 
-// Returns false when the table is full.
-__device__ inline bool zinsert(uint64_t *keys, uint32_t cap, uint64_t z, int *distinct) {
+// Returns the slot holding z, or -1 when the table is full.
+__device__ inline int zinsert(uint64_t *keys, uint32_t cap, uint64_t z, int *distinct) {
     uint32_t h = zhash(z, cap);
     for (uint32_t p = 0; p < cap; ++p) {
         uint64_t k = keys[h];
-        if (k == z) return true;
+        if (k == z) return (int)h;
         if (k == kEmptyKey) {
             unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(&keys[h]),
                                                (unsigned long long)kEmptyKey, (unsigned long long)z);
             if (old == kEmptyKey) {
                 atomicAdd(distinct, 1);
-                return true;
+                return (int)h;
             }
-            if (old == z) return true;
+            if (old == z) return (int)h;
         }
         h = (h + 1) & (cap - 1);
     }
-    return false;
+    return -1;
 }
 
-__device__ inline int zlookup(const uint64_t *keys, const int *ids, uint32_t cap, uint64_t z) {
-    uint32_t h = zhash(z, cap);
-    for (uint32_t p = 0; p < cap; ++p) {
-        if (keys[h] == z) return ids[h];
-        h = (h + 1) & (cap - 1);
+// Stratum codes of 16 consecutive samples (vector v) from the d Z columns.
+__device__ __forceinline__ void zcodes16(uint64_t (&z)[16], const uint8_t *const *col, const uint32_t *dim, int d,
+                                         int64_t v) {
+#pragma unroll
+    for (int b = 0; b < 16; ++b) z[b] = 0;
+    for (int j = 0; j < d; ++j) {
+        const uint4 w = __ldg(reinterpret_cast<const uint4 *>(col[j]) + v);
+        const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+        const uint64_t dm = dim[j];
+#pragma unroll
+        for (int b = 0; b < 16; ++b) z[b] = z[b] * dm + ((ww[b >> 2] >> (8 * (b & 3))) & 0xffu);
     }
-    return -1;
+}
+
+// Byte offsets of one compact-tier global slot, every region 256-byte aligned.
+struct SlotLayout {
+    int64_t keys, zk, ids, cnt, cur, sid, wt, ord, total;
+};
+__host__ __device__ inline int64_t align256(int64_t x) { return (x + 255) & ~(int64_t)255; }
+__host__ __device__ inline SlotLayout slot_layout(int64_t S, int64_t cap) {
+    SlotLayout L;
+    int64_t o = 0;
+    L.keys = o; o = align256(o + cap * 8);        // strata hash keys
+    L.zk = o;   o = align256(o + cap * 8);        // stratum code per compact id
+    L.ids = o;  o = align256(o + cap * 4);        // compact id per hash slot
+    L.cnt = o;  o = align256(o + (S + 1) * 4);    // samples per stratum -> offsets
+    L.cur = o;  o = align256(o + (S + 1) * 4);    // scatter cursors
+    L.sid = o;  o = align256(o + (S + 16) * 4);   // slot, then stratum id, per sample
+    L.wt = o;   o = align256(o + (int64_t)kWarps * kGlobalWarpTab * 4);  // warp tables, kept zeroed
+    L.ord = o;  o = align256(o + S * 2);          // x*dy + y codes sorted by stratum
+    L.total = o;
+    return L;
 }
 
 // Block-wide exclusive scan of n ints in place (any n), each thread a contiguous chunk.
@@ -387,16 +412,18 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     const int64_t S = a.S;
     const uint32_t gcap = (uint32_t)a.hash_cap_global;
     char *slot = a.slot_mem + (int64_t)blockIdx.x * a.slot_bytes;
-    uint64_t *gkeys = reinterpret_cast<uint64_t *>(slot);
-    uint64_t *gzk = gkeys + gcap;
-    int *gids = reinterpret_cast<int *>(gzk + gcap);
-    int *gcnt = gids + gcap;                  // S + 1
-    int *gcur = gcnt + (S + 1);               // S + 1
-    int *gsid = gcur + (S + 1);               // S
-    int *gwt = gsid + S;                      // kWarps * kGlobalWarpTab, kept zeroed
-    uint16_t *gord = reinterpret_cast<uint16_t *>(gwt + (int64_t)kWarps * kGlobalWarpTab);  // S
+    const SlotLayout L = slot_layout(S, gcap);
+    uint64_t *gkeys = reinterpret_cast<uint64_t *>(slot + L.keys);
+    uint64_t *gzk = reinterpret_cast<uint64_t *>(slot + L.zk);
+    int *gids = reinterpret_cast<int *>(slot + L.ids);
+    int *gcnt = reinterpret_cast<int *>(slot + L.cnt);
+    int *gcur = reinterpret_cast<int *>(slot + L.cur);
+    int *gsid = reinterpret_cast<int *>(slot + L.sid);
+    int *gwt = reinterpret_cast<int *>(slot + L.wt);
+    uint16_t *gord = reinterpret_cast<uint16_t *>(slot + L.ord);
     const int n2 = a.counters[C_TIER2];
     const int d = a.d, ncols = d + 2;
+    const int64_t nvec = S >> 4;
     for (int i = tid; i < kWarps * kSparseWarpTab; i += kThreads) swt[i] = 0;
     for (;;) {
         if (tid == 0) s_idx = atomicAdd(&a.counters[C_WORK2], 1);
@@ -424,11 +451,24 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             }
             __syncthreads();
             const int limit = attempt == 0 ? kSmemStrata : (int)(cap / 2);
-            for (int64_t s = tid; s < S; s += kThreads) {
+            for (int64_t v = tid; v < nvec; v += kThreads) {
+                if (*(volatile int *)&s_over) break;
+                uint64_t z[16];
+                zcodes16(z, s_col, s_dim, d, v);
+#pragma unroll
+                for (int b = 0; b < 16; ++b) {
+                    const int h = zinsert(keys, cap, z[b], &s_distinct);
+                    if (h < 0 || *(volatile int *)&s_distinct > limit) s_over = 1;
+                    gsid[v * 16 + b] = h;
+                }
+            }
+            for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
                 if (*(volatile int *)&s_over) break;
                 uint64_t z = 0;
                 for (int j = 0; j < d; ++j) z = z * s_dim[j] + s_col[j][s];
-                if (!zinsert(keys, cap, z, &s_distinct) || *(volatile int *)&s_distinct > limit) s_over = 1;
+                const int h = zinsert(keys, cap, z, &s_distinct);
+                if (h < 0 || *(volatile int *)&s_distinct > limit) s_over = 1;
+                gsid[s] = h;
             }
             __syncthreads();
             if (!s_over || attempt == 1) break;
@@ -477,10 +517,20 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         // 2. counting sort of the samples by stratum
         for (int i = tid; i <= n_obs; i += kThreads) cnt[i] = 0;
         __syncthreads();
-        for (int64_t s = tid; s < S; s += kThreads) {
-            uint64_t z = 0;
-            for (int j = 0; j < d; ++j) z = z * s_dim[j] + s_col[j][s];
-            const int sid = zlookup(keys, ids, cap, z);
+        for (int64_t s4 = tid; s4 < (S >> 2); s4 += kThreads) {
+            int4 h = reinterpret_cast<int4 *>(gsid)[s4];
+            h.x = ids[h.x];
+            h.y = ids[h.y];
+            h.z = ids[h.z];
+            h.w = ids[h.w];
+            reinterpret_cast<int4 *>(gsid)[s4] = h;
+            atomicAdd(&cnt[h.x], 1);
+            atomicAdd(&cnt[h.y], 1);
+            atomicAdd(&cnt[h.z], 1);
+            atomicAdd(&cnt[h.w], 1);
+        }
+        for (int64_t s = (S & ~(int64_t)3) + tid; s < S; s += kThreads) {
+            const int sid = ids[gsid[s]];
             gsid[s] = sid;
             atomicAdd(&cnt[sid], 1);
         }
@@ -488,7 +538,22 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         block_exclusive_scan(cnt, n_obs + 1, s_w);  // cnt -> stratum offsets, cnt[n_obs] = S
         for (int i = tid; i <= n_obs; i += kThreads) cur[i] = cnt[i];
         __syncthreads();
-        for (int64_t s = tid; s < S; s += kThreads) {
+        for (int64_t v = tid; v < nvec; v += kThreads) {
+            const uint4 wx = __ldg(reinterpret_cast<const uint4 *>(colx) + v);
+            const uint4 wy = __ldg(reinterpret_cast<const uint4 *>(coly) + v);
+            const uint32_t xx[4] = {wx.x, wx.y, wx.z, wx.w}, yy[4] = {wy.x, wy.y, wy.z, wy.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int4 sid = reinterpret_cast<const int4 *>(gsid)[v * 4 + q];
+                const int sv[4] = {sid.x, sid.y, sid.z, sid.w};
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const int pos = atomicAdd(&cur[sv[b]], 1);
+                    gord[pos] = (uint16_t)(((xx[q] >> (8 * b)) & 0xffu) * dy + ((yy[q] >> (8 * b)) & 0xffu));
+                }
+            }
+        }
+        for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
             const int pos = atomicAdd(&cur[gsid[s]], 1);
             gord[pos] = (uint16_t)(colx[s] * dy + coly[s]);
         }
@@ -601,10 +666,6 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     }
 }
 
-// Bytes of one compact-tier global slot for n_samples samples and a strata hash of cap slots.
-__host__ __device__ inline int64_t compact_slot_bytes(int64_t S, int64_t cap) {
-    return cap * 8 * 2 + cap * 4 + (S + 1) * 4 * 2 + S * 4 + (int64_t)kWarps * kGlobalWarpTab * 4 + S * 2 + 256;
-}
 
 // ---------------------------------------------------------------- band tables
 __global__ void band_table_kernel(double alpha, double *lo, double *hi, int dfmax) {

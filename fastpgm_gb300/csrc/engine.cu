@@ -512,7 +512,7 @@ int ensure_slots(fpgm_engine *e) {
     e->slots.release();
     e->hash_cap_global = (int)cap;
     e->n_slots = 2 * e->num_sms;
-    e->slot_bytes = (compact_slot_bytes(e->S, cap) + 255) & ~(int64_t)255;
+    e->slot_bytes = slot_layout(e->S, cap).total;
     RET(e->slots.ensure((size_t)e->slot_bytes * e->n_slots));
     CK(cudaMemsetAsync(e->slots.p, 0, (size_t)e->slot_bytes * e->n_slots, e->stream));  // warp tables start zeroed
     return FPGM_OK;
