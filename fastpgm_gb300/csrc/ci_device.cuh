@@ -81,6 +81,13 @@ __host__ __device__ inline double chisq_pvalue(double g2, long long df) {
     return 1.0 - igamma_p(0.5 * (double)df, 0.5 * g2);
 }
 
+// chi-square density, to turn a G^2 error bound into a p-value error bound.
+__host__ __device__ inline double chisq_pdf(double x, long long df) {
+    if (!(x > 0.0)) return df <= 2 ? 1.0 : 0.0;
+    const double k = 0.5 * (double)df;
+    return exp((k - 1.0) * log(x) - 0.5 * x - k * 0.69314718055994530942 - lgamma(k));
+}
+
 // G^2 at which the p-value of df degrees of freedom equals target (bisection;
 // p is decreasing in G^2).  Returns 0 for target >= 1 and +inf for target <= 0.
 __host__ __device__ inline double chisq_quantile_upper(double target, long long df) {

@@ -386,6 +386,115 @@ __device__ inline int block_exclusive_scan(int *v, int n, int *s_w) {
     return total;
 }
 
+
+// One FP32 (Neumaier, with error bound) or FP64 G^2 term for a cell of count O in a
+// stratum of m samples with margins Nx, Ny.
+template <bool kFp64>
+__device__ __forceinline__ void strata_term(Partial &p, int O, int Nx, int Ny, int m) {
+    if (kFp64) {
+        const double expected = (double)Ny * (double)Nx / (double)m;
+        p.g2 += 2.0 * O * log(O / expected);
+    } else {
+        const long long num = (long long)O * m, den = (long long)Nx * Ny;
+        if (num == den) return;
+        const float q = (float)(num - den) / (float)den;
+        const float l = fabsf(q) < 0.5f ? log1pf(q) : logf((float)num / (float)den);
+        const float term = 2.0f * (float)O * l;
+        // a per-thread running sum in double keeps the compensation exact enough here
+        p.g2 += (double)term;
+        p.err += 2.0 * O * (2.5e-7 * fmin(1.0, 2.0 * fabs((double)q)) + 2.5e-7 * fabs((double)l));
+        p.abs_g2 += fabs((double)term);
+    }
+}
+
+// Strata of at most kLaneStratum samples, one lane each, pairwise in registers.
+// Larger strata are appended to big[] (when n_big != nullptr) for score_big_strata.
+template <bool kFp64>
+__device__ inline Partial score_strata(const int *cnt, const uint16_t *gord, int n_obs, int dx, int dy, int *wt,
+                                       int *big, int *n_big, const uint64_t *gzk, bool want_hash, bool collect) {
+    (void)wt;
+    (void)dx;
+    Partial acc{0, 0.0, 0.0, 0.0, 0ull};
+    for (int k = threadIdx.x; k < n_obs; k += kThreads) {
+        const int o0 = cnt[k], m = cnt[k + 1] - o0;
+        if (m > kLaneStratum) {
+            if (collect) big[atomicAdd(n_big, 1)] = k;
+            continue;
+        }
+        uint16_t c[kLaneStratum];
+#pragma unroll
+        for (int i = 0; i < kLaneStratum; ++i)
+            if (i < m) c[i] = gord[o0 + i];
+        int ax = 0, ay = 0;
+        for (int i = 0; i < m; ++i) {
+            const int xi = c[i] / dy, yi = c[i] - xi * dy;
+            int O = 0, Nx = 0, Ny = 0;
+            bool fc = true, fx = true, fy = true;
+            for (int j = 0; j < m; ++j) {
+                const int xj = c[j] / dy, yj = c[j] - xj * dy;
+                if (c[j] == c[i]) { ++O; fc &= j >= i; }
+                if (xj == xi) { ++Nx; fx &= j >= i; }
+                if (yj == yi) { ++Ny; fy &= j >= i; }
+            }
+            ax += fx;
+            ay += fy;
+            if (fc) {
+                strata_term<kFp64>(acc, O, Nx, Ny, m);
+                if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + xi) * (uint64_t)dy + yi, (uint32_t)O);
+            }
+        }
+        acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
+    }
+    return acc;
+}
+
+// Strata listed in big[]: one warp each, dense x,y table read back with atomicExch.
+template <bool kFp64>
+__device__ inline Partial score_big_strata(Partial acc, const int *cnt, const uint16_t *gord, const int *big, int n_big,
+                                           int dx, int dy, int *wt, const uint64_t *gzk, bool want_hash) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int dxy = dx * dy;
+    int *wni = wt + dxy, *wnj = wni + dx;
+    for (int b = warp; b < n_big; b += kWarps) {
+        const int k = big[b];
+        const int o0 = cnt[k], o1 = cnt[k + 1];
+        const int m = o1 - o0;
+        int ax = 0, ay = 0;
+        for (int i = o0 + lane; i < o1; i += 32) {
+            const int c = gord[i];
+            const int x = c / dy, y = c - x * dy;
+            atomicAdd(&wt[c], 1);
+            ax += atomicAdd(&wni[x], 1) == 0;
+            ay += atomicAdd(&wnj[y], 1) == 0;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            ax += __shfl_xor_sync(0xffffffffu, ax, o);
+            ay += __shfl_xor_sync(0xffffffffu, ay, o);
+        }
+        if (lane == 0) acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
+        for (int i = o0 + lane; i < o1; i += 32) {
+            const int c = gord[i];
+            const int O = atomicExch(&wt[c], 0);
+            if (O > 0) {
+                const int x = c / dy, y = c - x * dy;
+                strata_term<kFp64>(acc, O, wni[x], wnj[y], m);
+                if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x) * (uint64_t)dy + y, (uint32_t)O);
+            }
+        }
+        __syncwarp();
+        for (int i = o0 + lane; i < o1; i += 32) {
+            const int c = gord[i];
+            const int x = c / dy;
+            wni[x] = 0;
+            wnj[c - x * dy] = 0;
+        }
+        __syncwarp();
+    }
+    return acc;
+}
+
 // Tier 2: joint tables too large for shared memory, counted in O(samples):
 //  1. the observed Z strata are hashed to compact ids (shared-memory hash,
 //     global fallback sized >= 2 n_samples);
@@ -558,109 +667,44 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             gord[pos] = (uint16_t)(colx[s] * dy + coly[s]);
         }
         __syncthreads();
-        // 3a. strata of at most kLaneStratum samples: one lane each, pairwise in registers
+        // 3. score the strata: FP32 terms first, FP64 only inside the recheck band
         const int dxy = dx * dy;
-        Partial acc{0, 0.0, 0.0, 0.0, 0ull};
-        int *big = gsid;  // stratum ids of larger strata (gsid is free after the scatter)
-        if (tid == 0) s_over = 0;
-        __syncthreads();
-        for (int k = tid; k < n_obs; k += kThreads) {
-            const int o0 = cnt[k], m = cnt[k + 1] - o0;
-            if (m > kLaneStratum) {
-                big[atomicAdd(&s_over, 1)] = k;
-                continue;
-            }
-            uint16_t c[kLaneStratum];
-#pragma unroll
-            for (int i = 0; i < kLaneStratum; ++i)
-                if (i < m) c[i] = gord[o0 + i];
-            int ax = 0, ay = 0;
-            for (int i = 0; i < m; ++i) {
-                const int xi = c[i] / dy, yi = c[i] - xi * dy;
-                int O = 0, Nx = 0, Ny = 0;
-                bool fc = true, fx = true, fy = true;
-                for (int j = 0; j < m; ++j) {
-                    const int xj = c[j] / dy, yj = c[j] - xj * dy;
-                    if (c[j] == c[i]) { ++O; fc &= j >= i; }
-                    if (xj == xi) { ++Nx; fx &= j >= i; }
-                    if (yj == yi) { ++Ny; fy &= j >= i; }
-                }
-                ax += fx;
-                ay += fy;
-                if (fc) {
-                    const double expected = (double)Ny * (double)Nx / (double)m;
-                    acc.g2 += 2.0 * O * log(O / expected);
-                    if (a.want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + xi) * (uint64_t)dy + yi, (uint32_t)O);
-                }
-            }
-            acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
-        }
-        __syncthreads();
-        const int n_big = s_over;
-        // 3b. larger strata: one warp each, dense x,y table read back with atomicExch
         const bool wsmem = dxy + dx + dy <= kSparseWarpTab;
         int *wt = wsmem ? swt + warp * kSparseWarpTab : gwt + (int64_t)warp * kGlobalWarpTab;
-        int *wni = wt + dxy, *wnj = wni + dx;
-        for (int b = warp; b < n_big; b += kWarps) {
-            const int k = big[b];
-            const int o0 = cnt[k], o1 = cnt[k + 1];
-            const int m = o1 - o0;
-            int ax = 0, ay = 0;
-            for (int i = o0 + lane; i < o1; i += 32) {
-                const int c = gord[i];
-                const int x = c / dy, y = c - x * dy;
-                atomicAdd(&wt[c], 1);
-                ax += atomicAdd(&wni[x], 1) == 0;
-                ay += atomicAdd(&wnj[y], 1) == 0;
-            }
-            __syncwarp();
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                ax += __shfl_xor_sync(0xffffffffu, ax, o);
-                ay += __shfl_xor_sync(0xffffffffu, ay, o);
-            }
-            if (lane == 0) acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
-            for (int i = o0 + lane; i < o1; i += 32) {
-                const int c = gord[i];
-                const int O = atomicExch(&wt[c], 0);
-                if (O > 0) {
-                    const int x = c / dy, y = c - x * dy;
-                    const double expected = (double)wnj[y] * (double)wni[x] / (double)m;
-                    acc.g2 += 2.0 * O * log(O / expected);
-                    if (a.want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x) * (uint64_t)dy + y, (uint32_t)O);
-                }
-            }
-            __syncwarp();
-            for (int i = o0 + lane; i < o1; i += 32) {
-                const int c = gord[i];
-                const int x = c / dy;
-                wni[x] = 0;
-                wnj[c - x * dy] = 0;
-            }
-            __syncwarp();
+        if (tid == 0) s_over = 0;
+        __syncthreads();
+        int *big = gsid;  // stratum ids of larger strata (gsid is free after the scatter)
+        Partial acc = score_strata<false>(cnt, gord, n_obs, dx, dy, wt, big, &s_over, gzk, a.want_hash != 0, true);
+        __syncthreads();
+        const int n_big = s_over;
+        acc = score_big_strata<false>(acc, cnt, gord, big, n_big, dx, dy, wt, gzk, a.want_hash != 0);
+        Partial r = block_sum(acc, scratch);
+        const double err = 2.0 * r.err + 1e-6 * r.abs_g2 + 1e-12;
+        int dec = band_decide(r.df, r.g2, err, a.bt);
+        double p32 = 1.0;
+        if (dec < 0 && r.df > a.bt.dfmax) {
+            // beyond the tables: FP64 p of the FP32 statistic, with the same band rule
+            p32 = chisq_pvalue(r.g2, r.df);
+            const double dpb = 2.0 * err * chisq_pdf(r.g2 > err ? r.g2 - err : 0.0, r.df);
+            if (fabs(p32 - a.alpha) >= kBand && fabs(p32 - a.alpha) > dpb) dec = p32 > a.alpha;
         }
-        const Partial r = block_sum(acc, scratch);
+        Verdict v{r.df, r.g2, 1.0, 1, 0, 0.0, r.hash};
+        if (dec < 0) {
+            Partial q = score_strata<true>(cnt, gord, n_obs, dx, dy, wt, big, nullptr, gzk, false, false);
+            q = score_big_strata<true>(q, cnt, gord, big, n_big, dx, dy, wt, gzk, false);
+            const Partial r2 = block_sum(q, scratch);
+            v.g2 = r2.g2;
+            v.p = chisq_pvalue(r2.g2, r.df);
+            v.indep = v.p > a.alpha;
+            v.rechecked = 1;
+            v.dp = fabs(v.p - chisq_pvalue(r.g2, r.df));
+        } else {
+            v.indep = dec;
+            v.p = (a.detail != nullptr && r.df > 0) ? chisq_pvalue(r.g2, r.df) : (dec ? 1.0 : 0.0);
+        }
         if (tid == 0) {
-            Verdict v{r.df, r.g2, 1.0, 1, 1, 0.0, r.hash};
-            if (r.df > 0) {
-                v.p = chisq_pvalue(r.g2, r.df);
-                v.indep = v.p > a.alpha;
-            }
-            a.flag[item] = (uint8_t)v.indep;
             atomicAdd(&a.stats[ST_LARGE], 1ull);
-            if (a.detail) {
-                fpgm_ci_result res;
-                res.table_hash = 0;
-                res.cell_hash = r.hash;
-                res.cells = (int64_t)n_obs * dxy;
-                res.df = (int32_t)r.df;
-                res.independent = v.indep;
-                res.g2 = r.g2;
-                res.p_value = v.p;
-                res.rechecked = 1;
-                res.path = 2;
-                a.detail[item] = res;
-            }
+            record(a, item, v, (int64_t)n_obs * dxy, 0, 2);
         }
         __syncthreads();
     }
