@@ -300,10 +300,10 @@ __device__ __forceinline__ uint32_t zhash(uint64_t z, uint32_t cap) {
     return (uint32_t)((z * 0x9E3779B97F4A7C15ull) >> 32) & (cap - 1);
 }
 
-// Returns the slot holding z, or -1 when the table is full.
-__device__ inline int zinsert(uint64_t *keys, uint32_t cap, uint64_t z, int *distinct) {
+// Returns the slot holding z, or -1 after max_probe probes (the table is too full).
+__device__ inline int zinsert(uint64_t *keys, uint32_t cap, uint64_t z, int *distinct, uint32_t max_probe) {
     uint32_t h = zhash(z, cap);
-    for (uint32_t p = 0; p < cap; ++p) {
+    for (uint32_t p = 0; p < max_probe; ++p) {
         uint64_t k = keys[h];
         if (k == z) return (int)h;
         if (k == kEmptyKey) {
@@ -560,13 +560,15 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             }
             __syncthreads();
             const int limit = attempt == 0 ? kSmemStrata : (int)(cap / 2);
+            // the shared table gives up early (short probes); the global one never fills past 1/2
+            const uint32_t max_probe = attempt == 0 ? 64u : cap;
             for (int64_t v = tid; v < nvec; v += kThreads) {
                 if (*(volatile int *)&s_over) break;
                 uint64_t z[16];
                 zcodes16(z, s_col, s_dim, d, v);
-#pragma unroll
                 for (int b = 0; b < 16; ++b) {
-                    const int h = zinsert(keys, cap, z[b], &s_distinct);
+                    if (*(volatile int *)&s_over) break;
+                    const int h = zinsert(keys, cap, z[b], &s_distinct, max_probe);
                     if (h < 0 || *(volatile int *)&s_distinct > limit) s_over = 1;
                     gsid[v * 16 + b] = h;
                 }
@@ -575,7 +577,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
                 if (*(volatile int *)&s_over) break;
                 uint64_t z = 0;
                 for (int j = 0; j < d; ++j) z = z * s_dim[j] + s_col[j][s];
-                const int h = zinsert(keys, cap, z, &s_distinct);
+                const int h = zinsert(keys, cap, z, &s_distinct, max_probe);
                 if (h < 0 || *(volatile int *)&s_distinct > limit) s_over = 1;
                 gsid[s] = h;
             }
