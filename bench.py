@@ -49,7 +49,19 @@ def parse():
     ap.add_argument("--alpha", type=float, default=0.05)
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-kernel comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline run")
+    ap.add_argument("--profile-one", action="store_true",
+                    help="run exactly one skeleton (no warm-up, flush, e2e or baselines) for profilers; "
+                         "prints its statistics, not a benchmark line")
     return ap.parse_args()
+
+
+def run_profile_one(a):
+    import fastpgm_gb300 as F
+    raw, depth, _ = F.make_config(a.config)
+    with F.Engine(0) as eng:
+        eng.upload(raw)
+        st = eng.pc_skeleton(alpha=a.alpha, depth=depth).to_dict()
+    print(json.dumps({"profile_one": a.config, "stats": st}))
 
 
 class Dist:
@@ -290,6 +302,9 @@ def run_ours(a, d):
 
 def main():
     a = parse()
+    if a.profile_one:
+        run_profile_one(a)
+        return
     d = Dist()
     try:
         if a.impl == "reference":
