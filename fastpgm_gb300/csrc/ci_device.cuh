@@ -294,7 +294,7 @@ struct Verdict {
 };
 
 // Full scoring of a dense table held by group g (shared or global memory).
-// Every thread of g calls it; the verdict is valid in every thread.
+// Every thread of g calls it; the verdict is valid in the group's thread 0.
 template <class G>
 __device__ inline Verdict score_dense(const G &g, const int *ct, int *ni, int *nj, int *nk, int dx, int dy,
                                       int64_t dz, double alpha, const BandTables &bt, bool want_p, bool want_hash,
@@ -306,21 +306,25 @@ __device__ inline Verdict score_dense(const G &g, const int *ct, int *ni, int *n
     Partial r = group_sum(g, p, scratch);
     Verdict v{r.df, r.g2, 1.0, 1, 0, 0.0, r.hash};
     const double err = 2.0 * r.err + 1e-6 * r.abs_g2 + 1e-12;
-    const int dec = band_decide(r.df, r.g2, err, bt);
+    const int dec = band_decide(r.df, r.g2, err, bt);  // uniform across the group
+    // p-values are evaluated by the group leader only (FP64 incomplete gamma)
+    const bool leader = g.t == 0;
     if (dec < 0) {
         Partial q{0, 0.0, 0.0, 0.0, 0ull};
         q.g2 = g2_fp64(g, ct, ni, nj, nk, dx, dy, cells);
         Partial r2 = group_sum(g, q, scratch);
         v.g2 = r2.g2;
-        v.p = chisq_pvalue(r2.g2, r.df);
-        v.indep = v.p > alpha;
         v.rechecked = 1;
-        v.dp = fabs(v.p - chisq_pvalue(r.g2, r.df));
+        if (leader) {
+            v.p = chisq_pvalue(r2.g2, r.df);
+            v.indep = v.p > alpha;
+            v.dp = fabs(v.p - chisq_pvalue(r.g2, r.df));
+        }
     } else {
         v.indep = dec;
-        v.p = (want_p && r.df > 0) ? chisq_pvalue(r.g2, r.df) : (r.df == 0 ? 1.0 : (dec ? 1.0 : 0.0));
+        if (leader) v.p = (want_p && r.df > 0) ? chisq_pvalue(r.g2, r.df) : (r.df == 0 ? 1.0 : (dec ? 1.0 : 0.0));
     }
-    return v;
+    return v;  // indep and p are valid in the leader
 }
 
 // FNV-1a-64 of the int32 table in cell order (test hook only; one thread).

@@ -683,12 +683,16 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         Partial r = block_sum(acc, scratch);
         const double err = 2.0 * r.err + 1e-6 * r.abs_g2 + 1e-12;
         int dec = band_decide(r.df, r.g2, err, a.bt);
-        double p32 = 1.0;
         if (dec < 0 && r.df > a.bt.dfmax) {
-            // beyond the tables: FP64 p of the FP32 statistic, with the same band rule
-            p32 = chisq_pvalue(r.g2, r.df);
-            const double dpb = 2.0 * err * chisq_pdf(r.g2 > err ? r.g2 - err : 0.0, r.df);
-            if (fabs(p32 - a.alpha) >= kBand && fabs(p32 - a.alpha) > dpb) dec = p32 > a.alpha;
+            // beyond the tables: thread 0 takes the FP64 p of the FP32 statistic, same band rule
+            if (tid == 0) {
+                const double p32 = chisq_pvalue(r.g2, r.df);
+                const double dpb = 2.0 * err * chisq_pdf(r.g2 > err ? r.g2 - err : 0.0, r.df);
+                s_over = (fabs(p32 - a.alpha) >= kBand && fabs(p32 - a.alpha) > dpb) ? (p32 > a.alpha) : -1;
+            }
+            __syncthreads();
+            dec = s_over;
+            __syncthreads();
         }
         Verdict v{r.df, r.g2, 1.0, 1, 0, 0.0, r.hash};
         if (dec < 0) {
@@ -696,13 +700,15 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             q = score_big_strata<true>(q, cnt, gord, big, n_big, dx, dy, wt, gzk, false);
             const Partial r2 = block_sum(q, scratch);
             v.g2 = r2.g2;
-            v.p = chisq_pvalue(r2.g2, r.df);
-            v.indep = v.p > a.alpha;
             v.rechecked = 1;
-            v.dp = fabs(v.p - chisq_pvalue(r.g2, r.df));
+            if (tid == 0) {
+                v.p = chisq_pvalue(r2.g2, r.df);
+                v.indep = v.p > a.alpha;
+                v.dp = fabs(v.p - chisq_pvalue(r.g2, r.df));
+            }
         } else {
             v.indep = dec;
-            v.p = (a.detail != nullptr && r.df > 0) ? chisq_pvalue(r.g2, r.df) : (dec ? 1.0 : 0.0);
+            if (tid == 0) v.p = (a.detail != nullptr && r.df > 0) ? chisq_pvalue(r.g2, r.df) : (dec ? 1.0 : 0.0);
         }
         if (tid == 0) {
             atomicAdd(&a.stats[ST_LARGE], 1ull);
