@@ -684,11 +684,13 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         const double err = 2.0 * r.err + 1e-6 * r.abs_g2 + 1e-12;
         int dec = band_decide(r.df, r.g2, err, a.bt);
         if (dec < 0 && r.df > a.bt.dfmax) {
-            // beyond the tables: thread 0 takes the FP64 p of the FP32 statistic, same band rule
+            // beyond the tables: Wilson-Hilferty p of the FP32 statistic, widened by its own
+            // error and by the propagated G^2 error (chi-square density <= 0.3/sqrt(df) here)
             if (tid == 0) {
-                const double p32 = chisq_pvalue(r.g2, r.df);
-                const double dpb = 2.0 * err * chisq_pdf(r.g2 > err ? r.g2 - err : 0.0, r.df);
-                s_over = (fabs(p32 - a.alpha) >= kBand && fabs(p32 - a.alpha) > dpb) ? (p32 > a.alpha) : -1;
+                const double pw = chisq_pvalue_wh(r.g2, (double)r.df);
+                const double dist = fabs(pw - a.alpha);
+                const double dpb = 2.0 * err * 0.3 / sqrt((double)r.df);
+                s_over = (dist > kBand + kWhMargin && dist > dpb + kWhMargin) ? (pw > a.alpha) : -1;
             }
             __syncthreads();
             dec = s_over;

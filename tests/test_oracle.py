@@ -130,3 +130,17 @@ def test_sparse_oracle_path_matches_reference_bit_for_bit(tmp_path):
     assert r.cells > (1 << 24) and r.table_hash == 0
     assert r.df == int(df) and r.independent == int(ind)
     assert r.g2 == float(g2) and r.p_value == float(p)
+
+
+def test_wilson_hilferty_router_bound():
+    """The engine routes tests with df > 32768 by the Wilson-Hilferty tail with a 1e-5 margin;
+    its error against the exact incomplete gamma must stay far below that margin."""
+    sp = pytest.importorskip("scipy.special")
+    st = pytest.importorskip("scipy.stats")
+    for k in (32769, 50000, 1e5, 1e6):
+        xs = st.chi2.ppf(np.linspace(1e-6, 1 - 1e-6, 4001), k)
+        exact = sp.gammaincc(k / 2, xs / 2)
+        v = 2 / (9 * k)
+        wh = 0.5 * sp.erfc((np.cbrt(xs / k) - (1 - v)) / np.sqrt(v) / np.sqrt(2))
+        assert np.abs(wh - exact).max() < 1e-6
+        assert st.chi2.pdf(xs, k).max() < 0.3 / np.sqrt(k)
