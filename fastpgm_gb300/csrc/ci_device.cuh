@@ -29,12 +29,7 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kSmemBytes = 96 * 1024;
 constexpr int kCtaInts = kSmemBytes / 4;                 // CTA tier: table + marginals
 constexpr int kWarpInts = kSmemBytes / 4 / kWarps;      // warp tier: per-warp region
-constexpr int kHashCap = 4096;                           // compact tier: shared-memory strata hash
-constexpr int kSmemStrata = kHashCap / 2;                // strata counted in shared memory
-constexpr int kSparseWarpTabOffset = kHashCap * 12 + 2 * (kSmemStrata + 1) * 4 + 8;  // 16-aligned
-constexpr int kSparseWarpTab = (kSmemBytes - kSparseWarpTabOffset) / 4 / kWarps;    // ints per warp
 constexpr int kGlobalWarpTab = 255 * 255 + 2 * 255 + 1;  // largest dx*dy + dx + dy
-constexpr int kLaneStratum = 16;                         // strata up to this many samples: one lane each
 constexpr int kBinomN = 4096;
 constexpr int kBinomK = 32;
 constexpr double kBand = 1e-3;

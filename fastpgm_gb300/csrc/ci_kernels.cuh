@@ -60,6 +60,7 @@ struct WaveArgs {
     char *slot_mem;
     int64_t slot_bytes;
     int32_t hash_cap_global;  // power of two >= 2 * n_samples
+    unsigned long long *dbg;  // compact-tier phase timers (FPGM_PHASE_TIMERS), else null
 };
 
 __device__ inline int upper_bound_i32(const int32_t *a, int n, int v) {
@@ -296,21 +297,43 @@ __global__ void __launch_bounds__(kThreads, 2) ci_cta_kernel(WaveArgs a) {
 }
 
 // ---------------------------------------------------------------- tier 2: compact strata
+// Shared-memory plan of the compact kernel (kSmemBytes), phase by phase:
+//   phase 1  strata hash: keys u64[kZCap] at 0, 16-bit ids u16[kZCap] at kZIdsOff
+//   phase 2  per-stratum counts cnt[] at 0 and cursors cur[] at kZCurOff (over the dead keys)
+//   phase 3  per-warp x,y tables from kZTabOff (over the dead ids)
+// Up to kZStrata strata stay in shared memory; beyond that the same arrays live in the
+// CTA's global slot (hash sized >= 2 n_samples).
+constexpr int kZCap = 8192;
+constexpr int kZStrata = kZCap / 2;
+constexpr int kZIdsOff = kZCap * 8;
+constexpr int kZCurOff = ((kZStrata + 1) * 4 + 15) / 16 * 16;
+constexpr int kZTabOff = (kZCurOff + (kZStrata + 1) * 4 + 15) / 16 * 16;
+constexpr int kSparseWarpTab = (kSmemBytes - kZTabOff) / 4 / kWarps;  // ints per warp
+constexpr int kLaneStratum = 8;   // strata of up to this many samples: one lane each
+constexpr int kRegStratum = 64;   // larger strata up to this size keep their codes in registers
+
 __device__ __forceinline__ uint32_t zhash(uint64_t z, uint32_t cap) {
     return (uint32_t)((z * 0x9E3779B97F4A7C15ull) >> 32) & (cap - 1);
 }
 
-// Returns the slot holding z, or -1 after max_probe probes (the table is too full).
-__device__ inline int zinsert(uint64_t *keys, uint32_t cap, uint64_t z, int *distinct, uint32_t max_probe) {
+// Inserts stratum code z; a new code takes the next id from *counter, written to ids[slot]
+// (16- or 32-bit ids) and, when gzk is given, its code to gzk[id].  Returns the slot, or -1
+// after max_probe probes or once more than id_limit strata exist.
+template <class Id>
+__device__ inline int zinsert(uint64_t *keys, Id *ids, uint32_t cap, uint64_t z, int *counter, int id_limit,
+                              uint32_t max_probe, uint64_t *gzk) {
     uint32_t h = zhash(z, cap);
     for (uint32_t p = 0; p < max_probe; ++p) {
-        uint64_t k = keys[h];
+        const uint64_t k = keys[h];
         if (k == z) return (int)h;
         if (k == kEmptyKey) {
-            unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(&keys[h]),
-                                               (unsigned long long)kEmptyKey, (unsigned long long)z);
+            const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(&keys[h]),
+                                                     (unsigned long long)kEmptyKey, (unsigned long long)z);
             if (old == kEmptyKey) {
-                atomicAdd(distinct, 1);
+                const int id = atomicAdd(counter, 1);
+                if (id >= id_limit) return -1;
+                ids[h] = (Id)id;
+                if (gzk) gzk[id] = z;
                 return (int)h;
             }
             if (old == z) return (int)h;
@@ -320,17 +343,25 @@ __device__ inline int zinsert(uint64_t *keys, uint32_t cap, uint64_t z, int *dis
     return -1;
 }
 
-// Stratum codes of 16 consecutive samples (vector v) from the d Z columns.
+// Stratum codes of 16 consecutive samples (vector v) from the d Z columns, four column
+// loads in flight at a time.
 __device__ __forceinline__ void zcodes16(uint64_t (&z)[16], const uint8_t *const *col, const uint32_t *dim, int d,
                                          int64_t v) {
 #pragma unroll
     for (int b = 0; b < 16; ++b) z[b] = 0;
-    for (int j = 0; j < d; ++j) {
-        const uint4 w = __ldg(reinterpret_cast<const uint4 *>(col[j]) + v);
-        const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
-        const uint64_t dm = dim[j];
+    for (int j0 = 0; j0 < d; j0 += 4) {
+        uint4 w[4];
 #pragma unroll
-        for (int b = 0; b < 16; ++b) z[b] = z[b] * dm + ((ww[b >> 2] >> (8 * (b & 3))) & 0xffu);
+        for (int t = 0; t < 4; ++t)
+            if (j0 + t < d) w[t] = __ldg(reinterpret_cast<const uint4 *>(col[j0 + t]) + v);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            if (j0 + t >= d) break;
+            const uint32_t ww[4] = {w[t].x, w[t].y, w[t].z, w[t].w};
+            const uint64_t dm = dim[j0 + t];
+#pragma unroll
+            for (int b = 0; b < 16; ++b) z[b] = z[b] * dm + ((ww[b >> 2] >> (8 * (b & 3))) & 0xffu);
+        }
     }
 }
 
@@ -342,21 +373,21 @@ __host__ __device__ inline int64_t align256(int64_t x) { return (x + 255) & ~(in
 __host__ __device__ inline SlotLayout slot_layout(int64_t S, int64_t cap) {
     SlotLayout L;
     int64_t o = 0;
-    L.keys = o; o = align256(o + cap * 8);        // strata hash keys
-    L.zk = o;   o = align256(o + cap * 8);        // stratum code per compact id
-    L.ids = o;  o = align256(o + cap * 4);        // compact id per hash slot
-    L.cnt = o;  o = align256(o + (S + 1) * 4);    // samples per stratum -> offsets
-    L.cur = o;  o = align256(o + (S + 1) * 4);    // scatter cursors
+    L.keys = o; o = align256(o + cap * 8);        // strata hash keys (overflow path)
+    L.zk = o;   o = align256(o + (S + 1) * 8);    // stratum code per id (fingerprint only)
+    L.ids = o;  o = align256(o + cap * 4);        // id per hash slot (overflow path)
+    L.cnt = o;  o = align256(o + (S + 1) * 4);    // samples per stratum -> offsets (overflow path)
+    L.cur = o;  o = align256(o + (S + 1) * 4);    // scatter cursors (overflow path)
     L.sid = o;  o = align256(o + (S + 16) * 4);   // slot, then stratum id, per sample
-    L.wt = o;   o = align256(o + (int64_t)kWarps * kGlobalWarpTab * 4);  // warp tables, kept zeroed
+    L.wt = o;   o = align256(o + (int64_t)kWarps * kGlobalWarpTab * 4);  // wide x,y tables, kept zeroed
     L.ord = o;  o = align256(o + S * 2);          // x*dy + y codes sorted by stratum
     L.total = o;
     return L;
 }
 
 // Block-wide exclusive scan of n ints in place (any n), each thread a contiguous chunk.
-// Returns the total.  s_w: kWarps ints of shared scratch.
-__device__ inline int block_exclusive_scan(int *v, int n, int *s_w) {
+// s_w: kWarps ints of shared scratch.
+__device__ inline void block_exclusive_scan(int *v, int n, int *s_w) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int per = (n + kThreads - 1) / kThreads;
     const int b0 = min(n, tid * per), b1 = min(n, b0 + per);
@@ -371,11 +402,8 @@ __device__ inline int block_exclusive_scan(int *v, int n, int *s_w) {
     __syncthreads();
     if (lane == 31) s_w[warp] = incl;
     __syncthreads();
-    int base = 0, total = 0;
-    for (int w = 0; w < kWarps; ++w) {
-        if (w < warp) base += s_w[w];
-        total += s_w[w];
-    }
+    int base = 0;
+    for (int w = 0; w < warp; ++w) base += s_w[w];
     int run = base + incl - sum;
     for (int i = b0; i < b1; ++i) {
         const int t = v[i];
@@ -383,12 +411,10 @@ __device__ inline int block_exclusive_scan(int *v, int n, int *s_w) {
         run += t;
     }
     __syncthreads();
-    return total;
 }
 
-
-// One FP32 (Neumaier, with error bound) or FP64 G^2 term for a cell of count O in a
-// stratum of m samples with margins Nx, Ny.
+// One G^2 term for a cell of count O in a stratum of m samples with margins Nx, Ny:
+// FP64 with the reference's formula, or FP32 from exact int64 products with an error bound.
 template <bool kFp64>
 __device__ __forceinline__ void strata_term(Partial &p, int O, int Nx, int Ny, int m) {
     if (kFp64) {
@@ -400,20 +426,17 @@ __device__ __forceinline__ void strata_term(Partial &p, int O, int Nx, int Ny, i
         const float q = (float)(num - den) / (float)den;
         const float l = fabsf(q) < 0.5f ? log1pf(q) : logf((float)num / (float)den);
         const float term = 2.0f * (float)O * l;
-        // a per-thread running sum in double keeps the compensation exact enough here
-        p.g2 += (double)term;
+        p.g2 += (double)term;  // double running sum per thread
         p.err += 2.0 * O * (2.5e-7 * fmin(1.0, 2.0 * fabs((double)q)) + 2.5e-7 * fabs((double)l));
         p.abs_g2 += fabs((double)term);
     }
 }
 
-// Strata of at most kLaneStratum samples, one lane each, pairwise in registers.
-// Larger strata are appended to big[] (when n_big != nullptr) for score_big_strata.
+// Strata of at most kLaneStratum samples, one thread each, pairwise in registers.
+// Larger strata are appended to big[] when collect.
 template <bool kFp64>
-__device__ inline Partial score_strata(const int *cnt, const uint16_t *gord, int n_obs, int dx, int dy, int *wt,
-                                       int *big, int *n_big, const uint64_t *gzk, bool want_hash, bool collect) {
-    (void)wt;
-    (void)dx;
+__device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gord, int n_obs, int dx, int dy, int *big,
+                                             int *n_big, const uint64_t *gzk, bool want_hash, bool collect) {
     Partial acc{0, 0.0, 0.0, 0.0, 0ull};
     for (int k = threadIdx.x; k < n_obs; k += kThreads) {
         const int o0 = cnt[k], m = cnt[k + 1] - o0;
@@ -421,26 +444,38 @@ __device__ inline Partial score_strata(const int *cnt, const uint16_t *gord, int
             if (collect) big[atomicAdd(n_big, 1)] = k;
             continue;
         }
-        uint16_t c[kLaneStratum];
+        int xs[kLaneStratum], ys[kLaneStratum], cs[kLaneStratum];
 #pragma unroll
-        for (int i = 0; i < kLaneStratum; ++i)
-            if (i < m) c[i] = gord[o0 + i];
+        for (int i = 0; i < kLaneStratum; ++i) {
+            const int c = i < m ? (int)gord[o0 + i] : -1;
+            cs[i] = c;
+            xs[i] = c >= 0 ? c / dy : -1;
+            ys[i] = c >= 0 ? c - xs[i] * dy : -1;
+        }
         int ax = 0, ay = 0;
-        for (int i = 0; i < m; ++i) {
-            const int xi = c[i] / dy, yi = c[i] - xi * dy;
+#pragma unroll
+        for (int i = 0; i < kLaneStratum; ++i) {
+            if (i >= m) break;
             int O = 0, Nx = 0, Ny = 0;
             bool fc = true, fx = true, fy = true;
-            for (int j = 0; j < m; ++j) {
-                const int xj = c[j] / dy, yj = c[j] - xj * dy;
-                if (c[j] == c[i]) { ++O; fc &= j >= i; }
-                if (xj == xi) { ++Nx; fx &= j >= i; }
-                if (yj == yi) { ++Ny; fy &= j >= i; }
+#pragma unroll
+            for (int j = 0; j < kLaneStratum; ++j) {
+                if (j >= m) break;
+                const bool sc = cs[j] == cs[i], sx = xs[j] == xs[i], sy = ys[j] == ys[i];
+                O += sc;
+                Nx += sx;
+                Ny += sy;
+                if (j < i) {
+                    fc &= !sc;
+                    fx &= !sx;
+                    fy &= !sy;
+                }
             }
             ax += fx;
             ay += fy;
             if (fc) {
                 strata_term<kFp64>(acc, O, Nx, Ny, m);
-                if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + xi) * (uint64_t)dy + yi, (uint32_t)O);
+                if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + xs[i]) * (uint64_t)dy + ys[i], (uint32_t)O);
             }
         }
         acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
@@ -449,6 +484,7 @@ __device__ inline Partial score_strata(const int *cnt, const uint16_t *gord, int
 }
 
 // Strata listed in big[]: one warp each, dense x,y table read back with atomicExch.
+// Strata of up to kRegStratum samples keep their codes in registers across the passes.
 template <bool kFp64>
 __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const uint16_t *gord, const int *big, int n_big,
                                            int dx, int dy, int *wt, const uint64_t *gzk, bool want_hash) {
@@ -460,12 +496,69 @@ __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const ui
         const int o0 = cnt[k], o1 = cnt[k + 1];
         const int m = o1 - o0;
         int ax = 0, ay = 0;
-        for (int i = o0 + lane; i < o1; i += 32) {
-            const int c = gord[i];
-            const int x = c / dy, y = c - x * dy;
-            atomicAdd(&wt[c], 1);
-            ax += atomicAdd(&wni[x], 1) == 0;
-            ay += atomicAdd(&wnj[y], 1) == 0;
+        if (m <= kRegStratum) {
+            const int c0 = lane < m ? (int)gord[o0 + lane] : -1;
+            const int c1 = lane + 32 < m ? (int)gord[o0 + 32 + lane] : -1;
+            const int x0 = c0 >= 0 ? c0 / dy : 0, x1 = c1 >= 0 ? c1 / dy : 0;
+            if (c0 >= 0) {
+                atomicAdd(&wt[c0], 1);
+                ax += atomicAdd(&wni[x0], 1) == 0;
+                ay += atomicAdd(&wnj[c0 - x0 * dy], 1) == 0;
+            }
+            if (c1 >= 0) {
+                atomicAdd(&wt[c1], 1);
+                ax += atomicAdd(&wni[x1], 1) == 0;
+                ay += atomicAdd(&wnj[c1 - x1 * dy], 1) == 0;
+            }
+            __syncwarp();
+            if (c0 >= 0) {
+                const int O = atomicExch(&wt[c0], 0);
+                if (O > 0) {
+                    strata_term<kFp64>(acc, O, wni[x0], wnj[c0 - x0 * dy], m);
+                    if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x0) * (uint64_t)dy + (c0 - x0 * dy), (uint32_t)O);
+                }
+            }
+            if (c1 >= 0) {
+                const int O = atomicExch(&wt[c1], 0);
+                if (O > 0) {
+                    strata_term<kFp64>(acc, O, wni[x1], wnj[c1 - x1 * dy], m);
+                    if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x1) * (uint64_t)dy + (c1 - x1 * dy), (uint32_t)O);
+                }
+            }
+            __syncwarp();
+            if (c0 >= 0) {
+                wni[x0] = 0;
+                wnj[c0 - x0 * dy] = 0;
+            }
+            if (c1 >= 0) {
+                wni[x1] = 0;
+                wnj[c1 - x1 * dy] = 0;
+            }
+        } else {
+            for (int i = o0 + lane; i < o1; i += 32) {
+                const int c = gord[i];
+                const int x = c / dy;
+                atomicAdd(&wt[c], 1);
+                ax += atomicAdd(&wni[x], 1) == 0;
+                ay += atomicAdd(&wnj[c - x * dy], 1) == 0;
+            }
+            __syncwarp();
+            for (int i = o0 + lane; i < o1; i += 32) {
+                const int c = gord[i];
+                const int O = atomicExch(&wt[c], 0);
+                if (O > 0) {
+                    const int x = c / dy, y = c - x * dy;
+                    strata_term<kFp64>(acc, O, wni[x], wnj[y], m);
+                    if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x) * (uint64_t)dy + y, (uint32_t)O);
+                }
+            }
+            __syncwarp();
+            for (int i = o0 + lane; i < o1; i += 32) {
+                const int c = gord[i];
+                const int x = c / dy;
+                wni[x] = 0;
+                wnj[c - x * dy] = 0;
+            }
         }
         __syncwarp();
 #pragma unroll
@@ -474,50 +567,39 @@ __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const ui
             ay += __shfl_xor_sync(0xffffffffu, ay, o);
         }
         if (lane == 0) acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
-        for (int i = o0 + lane; i < o1; i += 32) {
-            const int c = gord[i];
-            const int O = atomicExch(&wt[c], 0);
-            if (O > 0) {
-                const int x = c / dy, y = c - x * dy;
-                strata_term<kFp64>(acc, O, wni[x], wnj[y], m);
-                if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x) * (uint64_t)dy + y, (uint32_t)O);
-            }
-        }
-        __syncwarp();
-        for (int i = o0 + lane; i < o1; i += 32) {
-            const int c = gord[i];
-            const int x = c / dy;
-            wni[x] = 0;
-            wnj[c - x * dy] = 0;
-        }
-        __syncwarp();
     }
     return acc;
 }
 
+// Phase timers (ns per phase, summed over tests) when a.dbg is set; off in normal runs.
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Tier 2: joint tables too large for shared memory, counted in O(samples):
-//  1. the observed Z strata are hashed to compact ids (shared-memory hash,
-//     global fallback sized >= 2 n_samples);
+//  1. the observed Z strata are hashed, each new one taking the next id (shared-memory
+//     hash of kZCap slots; a global one sized >= 2 n_samples when more than kZStrata);
 //  2. samples are counting-sorted by stratum (x*dy + y codes);
-//  3. a stratum of at most kLaneStratum samples is scored by one lane with
-//     pairwise comparisons in registers; a larger one by one warp that counts
-//     its x,y cells in a small dense table and reads each touched cell back
-//     with atomicExch(.., 0), so every distinct cell contributes exactly once
-//     and the table is left zeroed.  Either way the stratum's df and FP64 G^2
-//     terms follow the reference's formula.
+//  3. a stratum of at most kLaneStratum samples is scored by one thread with pairwise
+//     comparisons; a larger one by one warp that counts its x,y cells in a small dense
+//     table and reads each touched cell back with atomicExch(.., 0), so every distinct
+//     cell contributes once and the table is left zeroed.  FP32 terms first; the FP64
+//     pass runs only when the decision falls inside the recheck band.
 __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t *hkeys = reinterpret_cast<uint64_t *>(smem_raw);
-    int *hids = reinterpret_cast<int *>(smem_raw + kHashCap * 8);
-    int *scnt = reinterpret_cast<int *>(smem_raw + kHashCap * 12);   // kSmemStrata + 1 entries
-    int *scur = scnt + (kSmemStrata + 1);
-    int *swt = reinterpret_cast<int *>(smem_raw + kSparseWarpTabOffset);
+    uint16_t *hids = reinterpret_cast<uint16_t *>(smem_raw + kZIdsOff);
+    int *scnt = reinterpret_cast<int *>(smem_raw);
+    int *scur = reinterpret_cast<int *>(smem_raw + kZCurOff);
+    int *swt = reinterpret_cast<int *>(smem_raw + kZTabOff);
     __shared__ const uint8_t *s_col[kMaxCols];
     __shared__ uint32_t s_dim[kMaxCols];
-    __shared__ int s_idx, s_over, s_distinct;
+    __shared__ int s_idx, s_over, s_distinct, s_flag;
     __shared__ int s_w[kWarps];
     __shared__ Partial scratch[kWarps];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x;
     const int64_t S = a.S;
     const uint32_t gcap = (uint32_t)a.hash_cap_global;
     char *slot = a.slot_mem + (int64_t)blockIdx.x * a.slot_bytes;
@@ -533,43 +615,53 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     const int n2 = a.counters[C_TIER2];
     const int d = a.d, ncols = d + 2;
     const int64_t nvec = S >> 4;
-    for (int i = tid; i < kWarps * kSparseWarpTab; i += kThreads) swt[i] = 0;
+    uint64_t *zk = a.want_hash ? gzk : nullptr;
+    unsigned long long t_prev = 0;
+#define FPGM_PHASE(i)                                                   \
+    do {                                                                \
+        if (a.dbg && tid == 0) {                                        \
+            const unsigned long long t_ = gtimer();                     \
+            if (i >= 0) atomicAdd(&a.dbg[i], t_ - t_prev);              \
+            t_prev = t_;                                                \
+        }                                                               \
+    } while (0)
     for (;;) {
         if (tid == 0) s_idx = atomicAdd(&a.counters[C_WORK2], 1);
         __syncthreads();
         const int idx = s_idx;
         if (idx >= n2) break;
+        FPGM_PHASE(-1);
         const int item = a.lists[2 * a.list_cap + idx];
         if (tid < ncols) {
             const int var = a.item_vars[(int64_t)item * ncols + tid];
             s_dim[tid] = a.card[var];
             s_col[tid] = a.cols + (int64_t)var * a.S_pad;
         }
-        __syncthreads();
-        const int dx = s_dim[d], dy = s_dim[d + 1];
-        const uint8_t *colx = s_col[d], *coly = s_col[d + 1];
-        // 1. strata -> hash (shared, then global if it fills up)
-        uint64_t *keys = hkeys;
-        int *ids = hids;
-        uint32_t cap = kHashCap;
+        // 1. strata -> ids (shared hash, global if more than kZStrata strata)
+        bool global = false;
         for (int attempt = 0; attempt < 2; ++attempt) {
+            global = attempt == 1;
+            const uint32_t cap = global ? gcap : (uint32_t)kZCap;
+            uint64_t *keys = global ? gkeys : hkeys;
             for (uint32_t i = tid; i < cap; i += kThreads) keys[i] = kEmptyKey;
             if (tid == 0) {
                 s_over = 0;
                 s_distinct = 0;
             }
             __syncthreads();
-            const int limit = attempt == 0 ? kSmemStrata : (int)(cap / 2);
-            // the shared table gives up early (short probes); the global one never fills past 1/2
-            const uint32_t max_probe = attempt == 0 ? 64u : cap;
+            const int limit = global ? (int)(cap / 2) : kZStrata;
+            const uint32_t max_probe = global ? cap : 64u;
             for (int64_t v = tid; v < nvec; v += kThreads) {
                 if (*(volatile int *)&s_over) break;
                 uint64_t z[16];
                 zcodes16(z, s_col, s_dim, d, v);
                 for (int b = 0; b < 16; ++b) {
-                    if (*(volatile int *)&s_over) break;
-                    const int h = zinsert(keys, cap, z[b], &s_distinct, max_probe);
-                    if (h < 0 || *(volatile int *)&s_distinct > limit) s_over = 1;
+                    const int h = global ? zinsert(keys, gids, cap, z[b], &s_distinct, limit, max_probe, zk)
+                                         : zinsert(keys, hids, cap, z[b], &s_distinct, limit, max_probe, zk);
+                    if (h < 0) {
+                        s_over = 1;
+                        break;
+                    }
                     gsid[v * 16 + b] = h;
                 }
             }
@@ -577,15 +669,17 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
                 if (*(volatile int *)&s_over) break;
                 uint64_t z = 0;
                 for (int j = 0; j < d; ++j) z = z * s_dim[j] + s_col[j][s];
-                const int h = zinsert(keys, cap, z, &s_distinct, max_probe);
-                if (h < 0 || *(volatile int *)&s_distinct > limit) s_over = 1;
+                const int h = global ? zinsert(keys, gids, cap, z, &s_distinct, limit, max_probe, zk)
+                                     : zinsert(keys, hids, cap, z, &s_distinct, limit, max_probe, zk);
+                if (h < 0) {
+                    s_over = 1;
+                    break;
+                }
                 gsid[s] = h;
             }
             __syncthreads();
-            if (!s_over || attempt == 1) break;
-            keys = gkeys;
-            ids = gids;
-            cap = gcap;
+            FPGM_PHASE(attempt);
+            if (!s_over) break;
             __syncthreads();
         }
         if (s_over) {  // cannot happen with cap >= 2 S; flag instead of guessing
@@ -596,44 +690,29 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             __syncthreads();
             continue;
         }
-        // compact ids in slot order
-        {
-            const uint32_t per_t = (cap + kThreads - 1) / kThreads;
-            const uint32_t b0 = min(cap, tid * per_t), b1 = min(cap, b0 + per_t);
-            int cnt = 0;
-            for (uint32_t i = b0; i < b1; ++i) cnt += keys[i] != kEmptyKey;
-            int incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += t;
-            }
-            if (lane == 31) s_w[warp] = incl;
-            __syncthreads();
-            int base = 0;
-            for (int w = 0; w < warp; ++w) base += s_w[w];
-            int id = base + incl - cnt;
-            for (uint32_t i = b0; i < b1; ++i)
-                if (keys[i] != kEmptyKey) {
-                    ids[i] = id;
-                    if (a.want_hash) gzk[id] = keys[i];
-                    ++id;
-                }
-            __syncthreads();
-        }
         const int n_obs = s_distinct;
-        const bool small = n_obs <= kSmemStrata;
-        int *cnt = small ? scnt : gcnt;
-        int *cur = small ? scur : gcur;
+        if (a.dbg && tid == 0) {
+            atomicAdd(&a.dbg[10], (unsigned long long)n_obs);
+            atomicAdd(&a.dbg[11], 1ull);
+        }
+        int *cnt = global ? gcnt : scnt;
+        int *cur = global ? gcur : scur;
         // 2. counting sort of the samples by stratum
         for (int i = tid; i <= n_obs; i += kThreads) cnt[i] = 0;
         __syncthreads();
         for (int64_t s4 = tid; s4 < (S >> 2); s4 += kThreads) {
             int4 h = reinterpret_cast<int4 *>(gsid)[s4];
-            h.x = ids[h.x];
-            h.y = ids[h.y];
-            h.z = ids[h.z];
-            h.w = ids[h.w];
+            if (global) {
+                h.x = gids[h.x];
+                h.y = gids[h.y];
+                h.z = gids[h.z];
+                h.w = gids[h.w];
+            } else {
+                h.x = hids[h.x];
+                h.y = hids[h.y];
+                h.z = hids[h.z];
+                h.w = hids[h.w];
+            }
             reinterpret_cast<int4 *>(gsid)[s4] = h;
             atomicAdd(&cnt[h.x], 1);
             atomicAdd(&cnt[h.y], 1);
@@ -641,14 +720,17 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             atomicAdd(&cnt[h.w], 1);
         }
         for (int64_t s = (S & ~(int64_t)3) + tid; s < S; s += kThreads) {
-            const int sid = ids[gsid[s]];
+            const int sid = global ? gids[gsid[s]] : (int)hids[gsid[s]];
             gsid[s] = sid;
             atomicAdd(&cnt[sid], 1);
         }
         __syncthreads();
+        FPGM_PHASE(2);
         block_exclusive_scan(cnt, n_obs + 1, s_w);  // cnt -> stratum offsets, cnt[n_obs] = S
         for (int i = tid; i <= n_obs; i += kThreads) cur[i] = cnt[i];
         __syncthreads();
+        const int dy = s_dim[d + 1], dx = s_dim[d];
+        const uint8_t *colx = s_col[d], *coly = s_col[d + 1];
         for (int64_t v = tid; v < nvec; v += kThreads) {
             const uint4 wx = __ldg(reinterpret_cast<const uint4 *>(colx) + v);
             const uint4 wy = __ldg(reinterpret_cast<const uint4 *>(coly) + v);
@@ -669,18 +751,23 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             gord[pos] = (uint16_t)(colx[s] * dy + coly[s]);
         }
         __syncthreads();
+        FPGM_PHASE(3);
         // 3. score the strata: FP32 terms first, FP64 only inside the recheck band
         const int dxy = dx * dy;
         const bool wsmem = dxy + dx + dy <= kSparseWarpTab;
-        int *wt = wsmem ? swt + warp * kSparseWarpTab : gwt + (int64_t)warp * kGlobalWarpTab;
+        int *wt = wsmem ? swt + (threadIdx.x >> 5) * kSparseWarpTab : gwt + (int64_t)(threadIdx.x >> 5) * kGlobalWarpTab;
+        if (wsmem)  // the table region held ids or cursors until now
+            for (int i = tid; i < kWarps * kSparseWarpTab; i += kThreads) swt[i] = 0;
         if (tid == 0) s_over = 0;
         __syncthreads();
         int *big = gsid;  // stratum ids of larger strata (gsid is free after the scatter)
-        Partial acc = score_strata<false>(cnt, gord, n_obs, dx, dy, wt, big, &s_over, gzk, a.want_hash != 0, true);
+        Partial acc = score_small_strata<false>(cnt, gord, n_obs, dx, dy, big, &s_over, zk, a.want_hash != 0, true);
         __syncthreads();
         const int n_big = s_over;
-        acc = score_big_strata<false>(acc, cnt, gord, big, n_big, dx, dy, wt, gzk, a.want_hash != 0);
+        FPGM_PHASE(4);
+        acc = score_big_strata<false>(acc, cnt, gord, big, n_big, dx, dy, wt, zk, a.want_hash != 0);
         Partial r = block_sum(acc, scratch);
+        FPGM_PHASE(5);
         const double err = 2.0 * r.err + 1e-6 * r.abs_g2 + 1e-12;
         int dec = band_decide(r.df, r.g2, err, a.bt);
         if (dec < 0 && r.df > a.bt.dfmax) {
@@ -690,16 +777,15 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
                 const double pw = chisq_pvalue_wh(r.g2, (double)r.df);
                 const double dist = fabs(pw - a.alpha);
                 const double dpb = 2.0 * err * 0.3 / sqrt((double)r.df);
-                s_over = (dist > kBand + kWhMargin && dist > dpb + kWhMargin) ? (pw > a.alpha) : -1;
+                s_flag = (dist > kBand + kWhMargin && dist > dpb + kWhMargin) ? (pw > a.alpha) : -1;
             }
             __syncthreads();
-            dec = s_over;
-            __syncthreads();
+            dec = s_flag;
         }
         Verdict v{r.df, r.g2, 1.0, 1, 0, 0.0, r.hash};
         if (dec < 0) {
-            Partial q = score_strata<true>(cnt, gord, n_obs, dx, dy, wt, big, nullptr, gzk, false, false);
-            q = score_big_strata<true>(q, cnt, gord, big, n_big, dx, dy, wt, gzk, false);
+            Partial q = score_small_strata<true>(cnt, gord, n_obs, dx, dy, big, nullptr, nullptr, false, false);
+            q = score_big_strata<true>(q, cnt, gord, big, n_big, dx, dy, wt, nullptr, false);
             const Partial r2 = block_sum(q, scratch);
             v.g2 = r2.g2;
             v.rechecked = 1;
@@ -716,10 +802,11 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             atomicAdd(&a.stats[ST_LARGE], 1ull);
             record(a, item, v, (int64_t)n_obs * dxy, 0, 2);
         }
+        FPGM_PHASE(6);
         __syncthreads();
     }
+#undef FPGM_PHASE
 }
-
 
 // ---------------------------------------------------------------- band tables
 __global__ void band_table_kernel(double alpha, double *lo, double *hi, int dfmax) {

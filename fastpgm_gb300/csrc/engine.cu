@@ -22,6 +22,7 @@
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -120,7 +121,7 @@ struct fpgm_engine {
     // level workspace
     DevBuf bits, deg, adjl, edges_x, edges_y, pxy, pyx, cntx, total, next, status, seprank, g, off, flag,
         counters, stats, scan_tmp, log_pair, log_vars, log_meta, node_cnt, node_off;
-    DevBuf slots, plain_ws, tests_buf, detail_buf, item_vars, lists, band;
+    DevBuf slots, plain_ws, tests_buf, detail_buf, item_vars, lists, band, phase_timers;
     double band_alpha = -1.0;
     int n_slots = 0, hash_cap_global = 0;
     int64_t slot_bytes = 0;
@@ -416,6 +417,10 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     CK(cudaMemcpy(e->btab.p, bt.data(), bt.size() * 8, cudaMemcpyHostToDevice));
     RET(e->counters.ensure(64));
     RET(e->stats.ensure(ST_COUNT * 8));
+    if (getenv("FPGM_PHASE_TIMERS")) {
+        RET(e->phase_timers.ensure(16 * 8));
+        CK(cudaMemset(e->phase_timers.p, 0, 16 * 8));
+    }
     *out = e;
     return FPGM_OK;
 }
@@ -427,7 +432,8 @@ extern "C" int fpgm_engine_destroy(fpgm_engine *e) {
                       &e->pxy, &e->pyx, &e->cntx, &e->total, &e->next, &e->status, &e->seprank, &e->g,
                       &e->off, &e->flag, &e->counters, &e->stats, &e->scan_tmp, &e->log_pair,
                       &e->log_vars, &e->log_meta, &e->node_cnt, &e->node_off, &e->slots, &e->plain_ws,
-                      &e->tests_buf, &e->detail_buf, &e->item_vars, &e->lists, &e->band};
+                      &e->tests_buf, &e->detail_buf, &e->item_vars, &e->lists, &e->band,
+                      &e->phase_timers};
     for (DevBuf *b : bufs) b->release();
     if (e->ev0) cudaEventDestroy(e->ev0);
     if (e->ev1) cudaEventDestroy(e->ev1);
@@ -607,10 +613,23 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
         CK(cudaGetLastError());
         CK(cudaEventRecord(e->ev1, e->stream));
         st->kernel_launches += 5;  // plan, classify, warp tier, CTA tier, reduce
+        a.dbg = e->phase_timers.as<unsigned long long>();
         if (a.slot_mem) {
             ci_compact_kernel<<<e->n_slots, kThreads, kSmemBytes, e->stream>>>(a);
             CK(cudaGetLastError());
             st->kernel_launches += 1;
+        }
+        if (a.dbg) {  // FPGM_PHASE_TIMERS: per-wave breakdown of the compact tier on stderr
+            unsigned long long h[16];
+            CK(cudaMemcpyAsync(h, a.dbg, sizeof h, cudaMemcpyDeviceToHost, e->stream));
+            CK(cudaMemsetAsync(a.dbg, 0, sizeof h, e->stream));
+            CK(cudaStreamSynchronize(e->stream));
+            if (h[11])
+                fprintf(stderr,
+                        "compact d=%d tests=%llu strata/test=%.0f us/test: shared-hash=%.1f global-hash=%.1f "
+                        "count=%.1f sort=%.1f small=%.1f big=%.1f decide=%.1f\n",
+                        d, h[11], (double)h[10] / h[11], h[0] / 1e3 / h[11], h[1] / 1e3 / h[11], h[2] / 1e3 / h[11],
+                        h[3] / 1e3 / h[11], h[4] / 1e3 / h[11], h[5] / 1e3 / h[11], h[6] / 1e3 / h[11]);
         }
         CK(cudaEventRecord(e->ev2, e->stream));
         CK(cudaMemsetAsync(dstat + ST_UNRESOLVED, 0, 8, e->stream));
