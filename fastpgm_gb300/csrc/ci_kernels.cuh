@@ -655,15 +655,23 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
                 if (*(volatile int *)&s_over) break;
                 uint64_t z[16];
                 zcodes16(z, s_col, s_dim, d, v);
-                for (int b = 0; b < 16; ++b) {
-                    const int h = global ? zinsert(keys, gids, cap, z[b], &s_distinct, limit, max_probe, zk)
-                                         : zinsert(keys, hids, cap, z[b], &s_distinct, limit, max_probe, zk);
-                    if (h < 0) {
-                        s_over = 1;
-                        break;
-                    }
-                    gsid[v * 16 + b] = h;
+                int hs[16];
+                bool ok = true;
+                for (int b = 0; b < 16 && ok; ++b) {
+                    hs[b] = global ? zinsert(keys, gids, cap, z[b], &s_distinct, limit, max_probe, zk)
+                                   : zinsert(keys, hids, cap, z[b], &s_distinct, limit, max_probe, zk);
+                    ok = hs[b] >= 0;
                 }
+                if (!ok) {
+                    s_over = 1;
+                    break;
+                }
+                // one 64-byte run per thread, written after the inserts
+                int4 *dst = reinterpret_cast<int4 *>(gsid + v * 16);
+                dst[0] = make_int4(hs[0], hs[1], hs[2], hs[3]);
+                dst[1] = make_int4(hs[4], hs[5], hs[6], hs[7]);
+                dst[2] = make_int4(hs[8], hs[9], hs[10], hs[11]);
+                dst[3] = make_int4(hs[12], hs[13], hs[14], hs[15]);
             }
             for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
                 if (*(volatile int *)&s_over) break;

@@ -622,6 +622,7 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
         if (a.dbg) {  // FPGM_PHASE_TIMERS: per-wave breakdown of the compact tier on stderr
             unsigned long long h[16];
             CK(cudaMemcpyAsync(h, a.dbg, sizeof h, cudaMemcpyDeviceToHost, e->stream));
+
             CK(cudaMemsetAsync(a.dbg, 0, sizeof h, e->stream));
             CK(cudaStreamSynchronize(e->stream));
             if (h[11])
