@@ -22,7 +22,7 @@ MAX_COND = 30
 EXPORTED = ["fpgm_last_error", "fpgm_engine_create", "fpgm_engine_destroy", "fpgm_dataset_upload",
             "fpgm_dataset_download", "fpgm_ci_test", "fpgm_ci_test_batch", "fpgm_pc_skeleton",
             "fpgm_pc_result_sizes", "fpgm_pc_result_fetch", "fpgm_orient_cpdag", "fpgm_write_struct",
-            "fpgm_bnsl_pcstable", "fpgm_generate_network", "fpgm_write_csv"]
+            "fpgm_bnsl_pcstable", "fpgm_generate_network", "fpgm_write_csv", "fpgm_ci_test_noalloc"]
 
 
 class CIResult(ctypes.Structure):
@@ -100,6 +100,8 @@ def load():
                                      ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32]
     L.fpgm_generate_network.argtypes = [ctypes.POINTER(GenSpec), u8p, u8p, i32p]
     L.fpgm_write_csv.argtypes = [ctypes.c_char_p, u8p, ctypes.c_int32, ctypes.c_int64, ctypes.c_char_p]
+    L.fpgm_ci_test_noalloc.argtypes = [vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
+                                       ctypes.c_int32, i32p, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, vp, vp]
     for name in EXPORTED:
         if name != "fpgm_last_error":
             getattr(L, name).restype = ctypes.c_int

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <mutex>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -1112,5 +1113,141 @@ extern "C" int fpgm_pc_result_fetch(fpgm_engine *e, uint8_t *adj, int32_t *remov
     if (removed && !e->res_removed.empty()) memcpy(removed, e->res_removed.data(), e->res_removed.size() * 4);
     if (sep_offsets) memcpy(sep_offsets, e->res_off.data(), e->res_off.size() * 4);
     if (sep_vars && !e->res_vars.empty()) memcpy(sep_vars, e->res_vars.data(), e->res_vars.size() * 4);
+    return FPGM_OK;
+}
+
+// ------------------------------------------------------------------ CI test without allocation
+// For callers that cannot allocate device memory: a process whose device memory
+// is owned by another allocator (a host framework's caching pool or a fixed
+// arena), or code running where a cudaMalloc would synchronise the device or is
+// not allowed.  Such a caller already holds its samples on the device and wants
+// one G^2 test on them.  This entry point uses only the fixed scratch array
+// below, which every GPU that loads the library holds until the process exits,
+// and calls no cudaMalloc, cudaFree or allocating library routine.
+namespace {
+
+constexpr int64_t kNoAllocTableInts = (int64_t)1 << 20;  // table + marginals: 4 MB
+constexpr int kNoAllocMaxVars = 65536;
+// [table + marginals | done counter + pad | cardinality per variable | stats]
+constexpr int64_t kNoAllocDoneOff = kNoAllocTableInts;                    // ints
+constexpr int64_t kNoAllocCardOff = kNoAllocTableInts + 64;               // ints
+constexpr int64_t kNoAllocStatsOff = kNoAllocCardOff + kNoAllocMaxVars / 4;  // ints (8-byte aligned)
+constexpr int64_t kNoAllocInts = kNoAllocStatsOff + 2 * ST_COUNT + 64;
+
+static __device__ __align__(256) int32_t g_noalloc_scratch[kNoAllocInts];
+
+struct NoAllocDevice {
+    bool ready = false;
+    int32_t *scratch = nullptr;  // device address of g_noalloc_scratch on this device
+    int num_sms = 0;
+};
+std::mutex g_noalloc_mu;
+NoAllocDevice g_noalloc_dev[64];
+
+// Largest id + 1 of each listed column (the cardinality of dense ids).
+__global__ void noalloc_card_kernel(const uint8_t *columns, int64_t pitch, int64_t S, PlainArgs p, uint8_t *card) {
+    __shared__ unsigned s_max;
+    const int var = p.vars[blockIdx.x];
+    if (threadIdx.x == 0) s_max = 0;
+    __syncthreads();
+    const uint8_t *c = columns + (int64_t)var * pitch;
+    unsigned m = 0;
+    for (int64_t s = threadIdx.x; s < S; s += blockDim.x) m = max(m, (unsigned)c[s]);
+    atomicMax(&s_max, m);
+    __syncthreads();
+    if (threadIdx.x == 0) card[var] = (uint8_t)(s_max + 1);
+}
+
+// Per device, with that device current: resolve the scratch array's device
+// address (the host-side symbol is only a stand-in) and prepare the kernel.
+int noalloc_setup(int dev, NoAllocDevice **out) {
+    if (dev < 0 || dev >= 64) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_noalloc: device %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    NoAllocDevice &d = g_noalloc_dev[dev];
+    if (!d.ready) {
+        void *p = nullptr;
+        CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        CK(cudaFuncSetAttribute(ci_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+        CK(cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev));
+        d.scratch = static_cast<int32_t *>(p);
+        d.ready = true;
+    }
+    *out = &d;
+    return FPGM_OK;
+}
+
+}  // namespace
+
+extern "C" int fpgm_ci_test_noalloc(const uint8_t *columns, int64_t pitch, int32_t n_vars, int64_t n_samples,
+                                    int32_t x, int32_t y, const int32_t *z, int32_t nz, double alpha,
+                                    int32_t want_hash, fpgm_ci_result *result, void *stream) {
+    if (!columns || !result || (nz > 0 && !z)) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_noalloc: NULL argument");
+    if (!(alpha >= 0.0 && alpha <= 1.0))
+        return set_error(FPGM_ERR_INVALID, "Error with incorrect significance level alpha!");
+    if (n_vars < 2 || n_vars > kNoAllocMaxVars || n_samples < 1 || n_samples > ((int64_t)1 << 31) - 16)
+        return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_noalloc: n_vars %d / n_samples %lld out of range", n_vars,
+                         (long long)n_samples);
+    if (pitch < n_samples || pitch % 16 != 0 || reinterpret_cast<uintptr_t>(columns) % 16 != 0)
+        return set_error(FPGM_ERR_INVALID,
+                         "fpgm_ci_test_noalloc: columns must be 16-byte aligned with a pitch that is a multiple of 16 "
+                         "and >= n_samples");
+    if (nz < 0 || nz > kMaxCond) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_noalloc: |Z| = %d outside [0, %d]", nz, kMaxCond);
+    if (x < 0 || x >= n_vars || y < 0 || y >= n_vars)
+        return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_noalloc: variable out of range");
+    for (int k = 0; k < nz; ++k)
+        if (z[k] < 0 || z[k] >= n_vars) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_noalloc: variable out of range");
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    NoAllocDevice *nd = nullptr;
+    RET(noalloc_setup(dev, &nd));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int32_t *scratch = nd->scratch;
+    uint8_t *card = reinterpret_cast<uint8_t *>(scratch + kNoAllocCardOff);
+    PlainArgs p;
+    memset(&p, 0, sizeof p);
+    p.ncols = nz + 2;
+    for (int k = 0; k < nz; ++k) p.vars[k] = z[k];
+    p.vars[nz] = x;
+    p.vars[nz + 1] = y;
+    // cardinalities of the involved columns, then the size check on the host
+    noalloc_card_kernel<<<p.ncols, 256, 0, st>>>(columns, pitch, n_samples, p, card);
+    CK(cudaGetLastError());
+    uint8_t hc[kMaxCols];
+    for (int k = 0; k < p.ncols; ++k)
+        CK(cudaMemcpyAsync(&hc[k], card + p.vars[k], 1, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int k = 0; k < p.ncols; ++k)
+        if (hc[k] == 0)
+            return set_error(FPGM_ERR_UNSUPPORTED, "fpgm_ci_test_noalloc: variable %d has 256 states (at most 255)",
+                             p.vars[k]);
+    double dz = 1.0;
+    for (int k = 0; k < nz; ++k) dz *= hc[k];
+    const double need = dz * hc[nz] * hc[nz + 1] + dz * (hc[nz] + hc[nz + 1] + 1);
+    if (need > (double)kNoAllocTableInts)
+        return set_error(FPGM_ERR_UNSUPPORTED,
+                         "fpgm_ci_test_noalloc: the test needs %.0f table ints, beyond the fixed scratch of %lld; use "
+                         "fpgm_ci_test, which allocates",
+                         need, (long long)kNoAllocTableInts);
+    // the scratch keeps the previous call's contents: clear what must start at zero
+    CK(cudaMemsetAsync(scratch, 0, (size_t)need * 4, st));
+    CK(cudaMemsetAsync(scratch + kNoAllocDoneOff, 0, 4, st));
+    CK(cudaMemsetAsync(scratch + kNoAllocStatsOff, 0, (size_t)ST_COUNT * 8, st));
+    p.cols = columns;
+    p.S = n_samples;
+    p.S_pad = pitch;
+    p.card = card;
+    p.alpha = alpha;
+    p.bt.lo = nullptr;  // no band tables: every df > 0 is decided by the FP64 recheck path
+    p.bt.hi = nullptr;
+    p.bt.dfmax = 0;
+    p.want_hash = want_hash;
+    p.gtab = scratch;
+    p.done = scratch + kNoAllocDoneOff;
+    p.out = result;
+    p.stats = reinterpret_cast<unsigned long long *>(scratch + kNoAllocStatsOff);
+    const int64_t nvec = n_samples >> 4;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(nvec / kThreads, 2 * nd->num_sms));
+    ci_plain_kernel<<<grid, kThreads, kSmemBytes, st>>>(p);
+    CK(cudaGetLastError());
     return FPGM_OK;
 }

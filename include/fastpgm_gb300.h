@@ -131,6 +131,32 @@ int fpgm_ci_test(fpgm_engine *eng, int32_t x, int32_t y, const int32_t *z, int32
 int fpgm_ci_test_batch(fpgm_engine *eng, const int32_t *tests, int32_t n_tests, int32_t d, double alpha,
                        int32_t want_hash, fpgm_ci_result *out);
 
+/* ---- CI test without allocation ----
+ * No counterpart in the reference.  For callers that cannot allocate device memory:
+ * their device memory belongs to another allocator (a host framework's caching pool or
+ * a fixed arena), or a cudaMalloc is not allowed or would stall the device where they
+ * run.  Such a caller already holds its samples on the device; this runs the plain
+ * single-test kernel on them and writes one fpgm_ci_result to caller-owned device
+ * memory, using only a fixed scratch array of 2^20 + 16,500 ints (about 4.3 MB) inside
+ * the library, held by every GPU that loads the library until the process exits.  It
+ * calls no cudaMalloc, cudaFree or allocating library routine.
+ *   columns  device pointer; variable v at columns + v*pitch, ids already dense
+ *            (0 .. states-1, e.g. first-appearance relabelled as fpgm_dataset_upload does);
+ *            16-byte aligned, pitch a multiple of 16 and >= n_samples
+ *   result   device pointer to one fpgm_ci_result (written when the stream reaches it)
+ *   stream   cudaStream_t to run on (NULL: the legacy default stream); the call waits on
+ *            it once, to read the tested columns' state counts for the size check
+ * Limits: joint table plus marginals of at most 2^20 ints (else FPGM_ERR_UNSUPPORTED),
+ * at most 65,536 variables and 255 states per variable.
+ * The first call on a device resolves the scratch array's device address
+ * (cudaGetSymbolAddress) with that device current: make that first call before any
+ * stream capture.  All calls share the one scratch array, which keeps the previous
+ * call's contents (each call clears what it uses): calls that overlap on the GPU, from
+ * other streams or threads, race and must be serialised by the caller. */
+int fpgm_ci_test_noalloc(const uint8_t *columns, int64_t pitch, int32_t n_vars, int64_t n_samples, int32_t x,
+                         int32_t y, const int32_t *z, int32_t nz, double alpha, int32_t want_hash,
+                         fpgm_ci_result *result, void *stream);
+
 /* ---- PC-stable skeleton ----
  * depth follows PCStable(Network*, alpha, depth=1000): levels d = 0 .. depth-1.
  * mode: FPGM_MODE_BATCHED (device-resident level engine) or FPGM_MODE_PLAIN

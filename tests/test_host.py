@@ -18,7 +18,8 @@ def declared_symbols():
     for h in os.listdir(os.path.join(ROOT, "include")):
         if h.endswith(".h"):
             txt = open(os.path.join(ROOT, "include", h)).read()
-            names |= set(re.findall(r"\b(fpgm_[a-z0-9_]+)\s*\(", txt))
+            # declarations only: a return type at the start of the line, then the name
+            names |= set(re.findall(r"^(?:int|const char \*)\s*(fpgm_[a-z0-9_]+)\s*\(", txt, re.M))
     return names
 
 
