@@ -135,6 +135,31 @@ __global__ void classify_kernel(WaveArgs a) {
     }
 }
 
+// Packed Horner codes of two 16-sample vectors (va, and vb when two) over ncols
+// columns, with up to eight 128-bit column loads in flight before they are folded.
+__device__ __forceinline__ void horner_pair(uint32_t (&ca)[8], uint32_t (&cb)[8], const uint8_t *const *col,
+                                            const uint32_t *dim, int ncols, int64_t va, int64_t vb, bool two) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) ca[q] = cb[q] = 0;
+    for (int j0 = 0; j0 < ncols; j0 += 4) {
+        uint4 wa[4], wb[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            wa[t] = wb[t] = make_uint4(0, 0, 0, 0);
+            if (j0 + t < ncols) {
+                wa[t] = __ldg(reinterpret_cast<const uint4 *>(col[j0 + t]) + va);
+                if (two) wb[t] = __ldg(reinterpret_cast<const uint4 *>(col[j0 + t]) + vb);
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            if (j0 + t >= ncols) break;
+            horner16(ca, wa[t], dim[j0 + t]);
+            horner16(cb, wb[t], dim[j0 + t]);
+        }
+    }
+}
+
 __device__ inline void record(const WaveArgs &a, int item, const Verdict &v, int64_t cells, uint64_t fnv, int path) {
     a.flag[item] = (uint8_t)v.indep;
     if (v.rechecked) {
@@ -197,14 +222,21 @@ __global__ void __launch_bounds__(kThreads, 2) ci_warp_kernel(WaveArgs a) {
         for (int i = lane; i < stride * R; i += 32) tab[i] = 0;
         __syncwarp();
         int *mytab = tab + (lane & (R - 1)) * stride;
-        for (int64_t v = lane; v < nvec; v += 32) {
-            uint32_t c2[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            for (int j = 0; j < ncols; ++j)
-                horner16(c2, __ldg(reinterpret_cast<const uint4 *>(s_col[warp][j]) + v), s_dim[warp][j]);
+        for (int64_t v = lane; v < nvec; v += 64) {
+            const bool two = v + 32 < nvec;
+            uint32_t ca[8], cb[8];
+            horner_pair(ca, cb, s_col[warp], s_dim[warp], ncols, v, v + 32, two);
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                atomicAdd(&mytab[c2[q] & 0xffffu], 1);
-                atomicAdd(&mytab[c2[q] >> 16], 1);
+                atomicAdd(&mytab[ca[q] & 0xffffu], 1);
+                atomicAdd(&mytab[ca[q] >> 16], 1);
+            }
+            if (two) {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    atomicAdd(&mytab[cb[q] & 0xffffu], 1);
+                    atomicAdd(&mytab[cb[q] >> 16], 1);
+                }
             }
         }
         for (int64_t s = (a.S & ~(int64_t)15) + lane; s < a.S; s += 32) {
@@ -266,13 +298,21 @@ __global__ void __launch_bounds__(kThreads, 2) ci_cta_kernel(WaveArgs a) {
         for (int i = tid; i < stride * R; i += kThreads) tab[i] = 0;
         __syncthreads();
         int *mytab = tab + (lane & (R - 1)) * stride;
-        for (int64_t v = tid; v < nvec; v += kThreads) {
-            uint32_t c2[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            for (int j = 0; j < ncols; ++j) horner16(c2, __ldg(reinterpret_cast<const uint4 *>(s_col[j]) + v), s_dim[j]);
+        for (int64_t v = tid; v < nvec; v += 2 * kThreads) {
+            const bool two = v + kThreads < nvec;
+            uint32_t ca[8], cb[8];
+            horner_pair(ca, cb, s_col, s_dim, ncols, v, v + kThreads, two);
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                atomicAdd(&mytab[c2[q] & 0xffffu], 1);
-                atomicAdd(&mytab[c2[q] >> 16], 1);
+                atomicAdd(&mytab[ca[q] & 0xffffu], 1);
+                atomicAdd(&mytab[ca[q] >> 16], 1);
+            }
+            if (two) {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    atomicAdd(&mytab[cb[q] & 0xffffu], 1);
+                    atomicAdd(&mytab[cb[q] >> 16], 1);
+                }
             }
         }
         for (int64_t s = (a.S & ~(int64_t)15) + tid; s < a.S; s += kThreads) {
@@ -413,24 +453,40 @@ __device__ inline void block_exclusive_scan(int *v, int n, int *s_w) {
     __syncthreads();
 }
 
-// One G^2 term for a cell of count O in a stratum of m samples with margins Nx, Ny:
-// FP64 with the reference's formula, or FP32 from exact int64 products with an error bound.
+// Per-thread accumulator of strata terms: FP64 sum for the recheck pass, or FP32
+// Neumaier-compensated sum with a running error bound (no FP64 in the common path).
 template <bool kFp64>
-__device__ __forceinline__ void strata_term(Partial &p, int O, int Nx, int Ny, int m) {
-    if (kFp64) {
-        const double expected = (double)Ny * (double)Nx / (double)m;
-        p.g2 += 2.0 * O * log(O / expected);
-    } else {
-        const long long num = (long long)O * m, den = (long long)Nx * Ny;
-        if (num == den) return;
-        const float q = (float)(num - den) / (float)den;
-        const float l = fabsf(q) < 0.5f ? log1pf(q) : logf((float)num / (float)den);
-        const float term = 2.0f * (float)O * l;
-        p.g2 += (double)term;  // double running sum per thread
-        p.err += 2.0 * O * (2.5e-7 * fmin(1.0, 2.0 * fabs((double)q)) + 2.5e-7 * fabs((double)l));
-        p.abs_g2 += fabs((double)term);
+struct TermAcc {
+    double g = 0.0;                          // FP64 pass
+    float s = 0.f, c = 0.f, e = 0.f, a = 0.f;  // FP32 pass
+    // cell of count O in a stratum of m samples with margins Nx, Ny
+    __device__ __forceinline__ void add(int O, int Nx, int Ny, int m) {
+        if (kFp64) {
+            const double expected = (double)Ny * (double)Nx / (double)m;
+            g += 2.0 * O * log(O / expected);
+        } else {
+            const long long num = (long long)O * m, den = (long long)Nx * Ny;
+            if (num == den) return;
+            const float q = (float)(num - den) / (float)den;
+            const float l = fabsf(q) < 0.5f ? log1pf(q) : logf((float)num / (float)den);
+            const float term = 2.0f * (float)O * l;
+            const float tt = s + term;
+            c += fabsf(s) >= fabsf(term) ? (s - tt) + term : (term - tt) + s;
+            s = tt;
+            e += 2.0f * (float)O * (2.5e-7f * fminf(1.0f, 2.0f * fabsf(q)) + 2.5e-7f * fabsf(l));
+            a += fabsf(term);
+        }
     }
-}
+    __device__ __forceinline__ void into(Partial &p) const {
+        if (kFp64) {
+            p.g2 += g;
+        } else {
+            p.g2 += (double)s + (double)c;
+            p.err += (double)e;
+            p.abs_g2 += (double)a;
+        }
+    }
+};
 
 // Strata of at most kLaneStratum samples, one thread each, pairwise in registers.
 // Larger strata are appended to big[] when collect.
@@ -438,6 +494,7 @@ template <bool kFp64>
 __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gord, int n_obs, int dx, int dy, int *big,
                                              int *n_big, const uint64_t *gzk, bool want_hash, bool collect) {
     Partial acc{0, 0.0, 0.0, 0.0, 0ull};
+    TermAcc<kFp64> ta;
     for (int k = threadIdx.x; k < n_obs; k += kThreads) {
         const int o0 = cnt[k], m = cnt[k + 1] - o0;
         if (m > kLaneStratum) {
@@ -474,12 +531,13 @@ __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gor
             ax += fx;
             ay += fy;
             if (fc) {
-                strata_term<kFp64>(acc, O, Nx, Ny, m);
+                ta.add(O, Nx, Ny, m);
                 if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + xs[i]) * (uint64_t)dy + ys[i], (uint32_t)O);
             }
         }
         acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
     }
+    ta.into(acc);
     return acc;
 }
 
@@ -491,6 +549,7 @@ __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const ui
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int dxy = dx * dy;
     int *wni = wt + dxy, *wnj = wni + dx;
+    TermAcc<kFp64> ta;
     for (int b = warp; b < n_big; b += kWarps) {
         const int k = big[b];
         const int o0 = cnt[k], o1 = cnt[k + 1];
@@ -514,14 +573,14 @@ __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const ui
             if (c0 >= 0) {
                 const int O = atomicExch(&wt[c0], 0);
                 if (O > 0) {
-                    strata_term<kFp64>(acc, O, wni[x0], wnj[c0 - x0 * dy], m);
+                    ta.add(O, wni[x0], wnj[c0 - x0 * dy], m);
                     if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x0) * (uint64_t)dy + (c0 - x0 * dy), (uint32_t)O);
                 }
             }
             if (c1 >= 0) {
                 const int O = atomicExch(&wt[c1], 0);
                 if (O > 0) {
-                    strata_term<kFp64>(acc, O, wni[x1], wnj[c1 - x1 * dy], m);
+                    ta.add(O, wni[x1], wnj[c1 - x1 * dy], m);
                     if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x1) * (uint64_t)dy + (c1 - x1 * dy), (uint32_t)O);
                 }
             }
@@ -548,7 +607,7 @@ __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const ui
                 const int O = atomicExch(&wt[c], 0);
                 if (O > 0) {
                     const int x = c / dy, y = c - x * dy;
-                    strata_term<kFp64>(acc, O, wni[x], wnj[y], m);
+                    ta.add(O, wni[x], wnj[y], m);
                     if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x) * (uint64_t)dy + y, (uint32_t)O);
                 }
             }
@@ -568,6 +627,7 @@ __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const ui
         }
         if (lane == 0) acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
     }
+    ta.into(acc);
     return acc;
 }
 
