@@ -349,7 +349,7 @@ constexpr int kZIdsOff = kZCap * 8;
 constexpr int kZCurOff = ((kZStrata + 1) * 4 + 15) / 16 * 16;
 constexpr int kZTabOff = (kZCurOff + (kZStrata + 1) * 4 + 15) / 16 * 16;
 constexpr int kSparseWarpTab = (kSmemBytes - kZTabOff) / 4 / kWarps;  // ints per warp
-constexpr int kLaneStratum = 8;   // strata of up to this many samples: one lane each
+constexpr int kLaneStratum = 16;  // strata of up to this many samples: one lane each
 constexpr int kRegStratum = 64;   // larger strata up to this size keep their codes in registers
 
 __device__ __forceinline__ uint32_t zhash(uint64_t z, uint32_t cap) {
@@ -501,13 +501,13 @@ __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gor
             if (collect) big[atomicAdd(n_big, 1)] = k;
             continue;
         }
-        int xs[kLaneStratum], ys[kLaneStratum], cs[kLaneStratum];
+        // one register per sample: (x << 8) | y; equal cells <=> equal words
+        uint32_t pk[kLaneStratum];
 #pragma unroll
         for (int i = 0; i < kLaneStratum; ++i) {
-            const int c = i < m ? (int)gord[o0 + i] : -1;
-            cs[i] = c;
-            xs[i] = c >= 0 ? c / dy : -1;
-            ys[i] = c >= 0 ? c - xs[i] * dy : -1;
+            const int c = i < m ? (int)gord[o0 + i] : 0;
+            const int x = c / dy;
+            pk[i] = ((uint32_t)x << 8) | (uint32_t)(c - x * dy);
         }
         int ax = 0, ay = 0;
 #pragma unroll
@@ -518,7 +518,8 @@ __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gor
 #pragma unroll
             for (int j = 0; j < kLaneStratum; ++j) {
                 if (j >= m) break;
-                const bool sc = cs[j] == cs[i], sx = xs[j] == xs[i], sy = ys[j] == ys[i];
+                const uint32_t dif = pk[j] ^ pk[i];
+                const bool sc = dif == 0, sx = (dif >> 8) == 0, sy = (dif & 0xffu) == 0;
                 O += sc;
                 Nx += sx;
                 Ny += sy;
@@ -532,7 +533,9 @@ __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gor
             ay += fy;
             if (fc) {
                 ta.add(O, Nx, Ny, m);
-                if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + xs[i]) * (uint64_t)dy + ys[i], (uint32_t)O);
+                if (want_hash)
+                    acc.hash += cell_mix((gzk[k] * (uint64_t)dx + (pk[i] >> 8)) * (uint64_t)dy + (pk[i] & 0xffu),
+                                         (uint32_t)O);
             }
         }
         acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
@@ -828,7 +831,8 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             for (int i = tid; i < kWarps * kSparseWarpTab; i += kThreads) swt[i] = 0;
         if (tid == 0) s_over = 0;
         __syncthreads();
-        int *big = gsid;  // stratum ids of larger strata (gsid is free after the scatter)
+        // stratum ids of larger strata: the dead cursors in shared memory, else the free gsid
+        int *big = global ? gsid : scur;
         Partial acc = score_small_strata<false>(cnt, gord, n_obs, dx, dy, big, &s_over, zk, a.want_hash != 0, true);
         __syncthreads();
         const int n_big = s_over;
