@@ -349,7 +349,7 @@ constexpr int kZIdsOff = kZCap * 8;
 constexpr int kZCurOff = ((kZStrata + 1) * 4 + 15) / 16 * 16;
 constexpr int kZTabOff = (kZCurOff + (kZStrata + 1) * 4 + 15) / 16 * 16;
 constexpr int kSparseWarpTab = (kSmemBytes - kZTabOff) / 4 / kWarps;  // ints per warp
-constexpr int kLaneStratum = 16;  // strata of up to this many samples: one lane each
+constexpr int kLaneStratum = 8;   // strata of up to this many samples: one lane each
 constexpr int kRegStratum = 64;   // larger strata up to this size keep their codes in registers
 
 __device__ __forceinline__ uint32_t zhash(uint64_t z, uint32_t cap) {
