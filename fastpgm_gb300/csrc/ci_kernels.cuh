@@ -420,7 +420,7 @@ __host__ __device__ inline SlotLayout slot_layout(int64_t S, int64_t cap) {
     L.cur = o;  o = align256(o + (S + 1) * 4);    // scatter cursors (overflow path)
     L.sid = o;  o = align256(o + (S + 16) * 4);   // slot, then stratum id, per sample
     L.wt = o;   o = align256(o + (int64_t)kWarps * kGlobalWarpTab * 4);  // wide x,y tables, kept zeroed
-    L.ord = o;  o = align256(o + S * 2);          // x*dy + y codes sorted by stratum
+    L.ord = o;  o = align256(o + S * 2);          // (x << 8) | y codes sorted by stratum
     L.total = o;
     return L;
 }
@@ -504,11 +504,7 @@ __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gor
         // one register per sample: (x << 8) | y; equal cells <=> equal words
         uint32_t pk[kLaneStratum];
 #pragma unroll
-        for (int i = 0; i < kLaneStratum; ++i) {
-            const int c = i < m ? (int)gord[o0 + i] : 0;
-            const int x = c / dy;
-            pk[i] = ((uint32_t)x << 8) | (uint32_t)(c - x * dy);
-        }
+        for (int i = 0; i < kLaneStratum; ++i) pk[i] = i < m ? (uint32_t)gord[o0 + i] : 0u;
         int ax = 0, ay = 0;
 #pragma unroll
         for (int i = 0; i < kLaneStratum; ++i) {
@@ -545,90 +541,111 @@ __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gor
 }
 
 // Strata listed in big[]: one warp each, dense x,y table read back with atomicExch.
-// Strata of up to kRegStratum samples keep their codes in registers across the passes.
+// Strata of up to kRegStratum samples keep their packed (x << 8) | y codes in registers,
+// and the next stratum's codes are loaded while the current one is scored.
 template <bool kFp64>
 __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const uint16_t *gord, const int *big, int n_big,
                                            int dx, int dy, int *wt, const uint64_t *gzk, bool want_hash) {
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int dxy = dx * dy;
     int *wni = wt + dxy, *wnj = wni + dx;
     TermAcc<kFp64> ta;
-    for (int b = warp; b < n_big; b += kWarps) {
-        const int k = big[b];
-        const int o0 = cnt[k], o1 = cnt[k + 1];
-        const int m = o1 - o0;
+    int b = warp, k = 0, m = 0, o0 = 0, p0 = -1, p1 = -1;
+    auto fetch = [&](int bb, int &kk, int &mm, int &oo, int &q0, int &q1) {
+        q0 = q1 = -1;
+        if (bb >= n_big) return;
+        kk = big[bb];
+        oo = cnt[kk];
+        mm = cnt[kk + 1] - oo;
+        if (mm <= kRegStratum) {
+            if (lane < mm) q0 = gord[oo + lane];
+            if (lane + 32 < mm) q1 = gord[oo + 32 + lane];
+        }
+    };
+    fetch(b, k, m, o0, p0, p1);
+    for (; b < n_big; b += kWarps) {
+        int kn = 0, mn = 0, on = 0, n0 = -1, n1 = -1;
+        fetch(b + kWarps, kn, mn, on, n0, n1);
         int ax = 0, ay = 0;
         if (m <= kRegStratum) {
-            const int c0 = lane < m ? (int)gord[o0 + lane] : -1;
-            const int c1 = lane + 32 < m ? (int)gord[o0 + 32 + lane] : -1;
-            const int x0 = c0 >= 0 ? c0 / dy : 0, x1 = c1 >= 0 ? c1 / dy : 0;
-            if (c0 >= 0) {
+            const int x0 = p0 >> 8, y0 = p0 & 0xff, x1 = p1 >> 8, y1 = p1 & 0xff;
+            const int c0 = x0 * dy + y0, c1 = x1 * dy + y1;
+            bool nx0 = false, ny0 = false, nx1 = false, ny1 = false;
+            if (p0 >= 0) {
                 atomicAdd(&wt[c0], 1);
-                ax += atomicAdd(&wni[x0], 1) == 0;
-                ay += atomicAdd(&wnj[c0 - x0 * dy], 1) == 0;
+                nx0 = atomicAdd(&wni[x0], 1) == 0;
+                ny0 = atomicAdd(&wnj[y0], 1) == 0;
             }
-            if (c1 >= 0) {
+            if (p1 >= 0) {
                 atomicAdd(&wt[c1], 1);
-                ax += atomicAdd(&wni[x1], 1) == 0;
-                ay += atomicAdd(&wnj[c1 - x1 * dy], 1) == 0;
+                nx1 = atomicAdd(&wni[x1], 1) == 0;
+                ny1 = atomicAdd(&wnj[y1], 1) == 0;
             }
-            __syncwarp();
-            if (c0 >= 0) {
+            ax = __popc(__ballot_sync(full, nx0)) + __popc(__ballot_sync(full, nx1));
+            ay = __popc(__ballot_sync(full, ny0)) + __popc(__ballot_sync(full, ny1));
+            __syncwarp();  // the lanes' counts are visible before they are read back
+            if (p0 >= 0) {
                 const int O = atomicExch(&wt[c0], 0);
                 if (O > 0) {
-                    ta.add(O, wni[x0], wnj[c0 - x0 * dy], m);
-                    if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x0) * (uint64_t)dy + (c0 - x0 * dy), (uint32_t)O);
+                    ta.add(O, wni[x0], wnj[y0], m);
+                    if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x0) * (uint64_t)dy + y0, (uint32_t)O);
                 }
             }
-            if (c1 >= 0) {
+            if (p1 >= 0) {
                 const int O = atomicExch(&wt[c1], 0);
                 if (O > 0) {
-                    ta.add(O, wni[x1], wnj[c1 - x1 * dy], m);
-                    if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x1) * (uint64_t)dy + (c1 - x1 * dy), (uint32_t)O);
+                    ta.add(O, wni[x1], wnj[y1], m);
+                    if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x1) * (uint64_t)dy + y1, (uint32_t)O);
                 }
             }
             __syncwarp();
-            if (c0 >= 0) {
+            if (p0 >= 0) {
                 wni[x0] = 0;
-                wnj[c0 - x0 * dy] = 0;
+                wnj[y0] = 0;
             }
-            if (c1 >= 0) {
+            if (p1 >= 0) {
                 wni[x1] = 0;
-                wnj[c1 - x1 * dy] = 0;
+                wnj[y1] = 0;
             }
         } else {
+            const int o1 = o0 + m;
             for (int i = o0 + lane; i < o1; i += 32) {
-                const int c = gord[i];
-                const int x = c / dy;
-                atomicAdd(&wt[c], 1);
+                const int p = gord[i];
+                const int x = p >> 8, y = p & 0xff;
+                atomicAdd(&wt[x * dy + y], 1);
                 ax += atomicAdd(&wni[x], 1) == 0;
-                ay += atomicAdd(&wnj[c - x * dy], 1) == 0;
+                ay += atomicAdd(&wnj[y], 1) == 0;
             }
             __syncwarp();
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                ax += __shfl_xor_sync(full, ax, o);
+                ay += __shfl_xor_sync(full, ay, o);
+            }
             for (int i = o0 + lane; i < o1; i += 32) {
-                const int c = gord[i];
-                const int O = atomicExch(&wt[c], 0);
+                const int p = gord[i];
+                const int x = p >> 8, y = p & 0xff;
+                const int O = atomicExch(&wt[x * dy + y], 0);
                 if (O > 0) {
-                    const int x = c / dy, y = c - x * dy;
                     ta.add(O, wni[x], wnj[y], m);
                     if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x) * (uint64_t)dy + y, (uint32_t)O);
                 }
             }
             __syncwarp();
             for (int i = o0 + lane; i < o1; i += 32) {
-                const int c = gord[i];
-                const int x = c / dy;
-                wni[x] = 0;
-                wnj[c - x * dy] = 0;
+                const int p = gord[i];
+                wni[p >> 8] = 0;
+                wnj[p & 0xff] = 0;
             }
         }
         __syncwarp();
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            ax += __shfl_xor_sync(0xffffffffu, ax, o);
-            ay += __shfl_xor_sync(0xffffffffu, ay, o);
-        }
         if (lane == 0) acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
+        k = kn;
+        m = mn;
+        o0 = on;
+        p0 = n0;
+        p1 = n1;
     }
     ta.into(acc);
     return acc;
@@ -644,7 +661,7 @@ __device__ __forceinline__ unsigned long long gtimer() {
 // Tier 2: joint tables too large for shared memory, counted in O(samples):
 //  1. the observed Z strata are hashed, each new one taking the next id (shared-memory
 //     hash of kZCap slots; a global one sized >= 2 n_samples when more than kZStrata);
-//  2. samples are counting-sorted by stratum (x*dy + y codes);
+//  2. samples are counting-sorted by stratum, stored as packed (x << 8) | y;
 //  3. a stratum of at most kLaneStratum samples is scored by one thread with pairwise
 //     comparisons; a larger one by one warp that counts its x,y cells in a small dense
 //     table and reads each touched cell back with atomicExch(.., 0), so every distinct
@@ -813,13 +830,13 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
 #pragma unroll
                 for (int b = 0; b < 4; ++b) {
                     const int pos = atomicAdd(&cur[sv[b]], 1);
-                    gord[pos] = (uint16_t)(((xx[q] >> (8 * b)) & 0xffu) * dy + ((yy[q] >> (8 * b)) & 0xffu));
+                    gord[pos] = (uint16_t)((((xx[q] >> (8 * b)) & 0xffu) << 8) | ((yy[q] >> (8 * b)) & 0xffu));
                 }
             }
         }
         for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
             const int pos = atomicAdd(&cur[gsid[s]], 1);
-            gord[pos] = (uint16_t)(colx[s] * dy + coly[s]);
+            gord[pos] = (uint16_t)((colx[s] << 8) | coly[s]);
         }
         __syncthreads();
         FPGM_PHASE(3);
