@@ -351,7 +351,6 @@ constexpr int kZTabOff = (kZCurOff + (kZStrata + 1) * 4 + 15) / 16 * 16;
 constexpr int kSparseWarpTab = (kSmemBytes - kZTabOff) / 4 / kWarps;  // ints per warp
 constexpr int kLaneStratum = 8;   // strata of up to this many samples: one lane each
 constexpr int kRegStratum = 64;   // larger strata up to this size keep their codes in registers
-constexpr int kCtaStratum = 512;  // strata above this many samples: the whole CTA scores them
 
 __device__ __forceinline__ uint32_t zhash(uint64_t z, uint32_t cap) {
     return (uint32_t)((z * 0x9E3779B97F4A7C15ull) >> 32) & (cap - 1);
@@ -493,18 +492,13 @@ struct TermAcc {
 // Larger strata are appended to big[] when collect.
 template <bool kFp64>
 __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gord, int n_obs, int dx, int dy, int *big,
-                                             int *n_big, int list_cap, const uint64_t *gzk, bool want_hash,
-                                             bool collect) {
+                                             int *n_big, const uint64_t *gzk, bool want_hash, bool collect) {
     Partial acc{0, 0.0, 0.0, 0.0, 0ull};
     TermAcc<kFp64> ta;
     for (int k = threadIdx.x; k < n_obs; k += kThreads) {
         const int o0 = cnt[k], m = cnt[k + 1] - o0;
         if (m > kLaneStratum) {
-            // warp-scored strata from the front of big[], CTA-scored ones from the back
-            if (collect) {
-                if (m > kCtaStratum) big[list_cap - 1 - atomicAdd(n_big + 1, 1)] = k;
-                else big[atomicAdd(n_big, 1)] = k;
-            }
+            if (collect) big[atomicAdd(n_big, 1)] = k;
             continue;
         }
         // one register per sample: (x << 8) | y; equal cells <=> equal words
@@ -657,52 +651,6 @@ __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const ui
     return acc;
 }
 
-// Strata of more than kCtaStratum samples, listed at big[list_cap - n_huge .. list_cap):
-// the whole CTA counts each into one dense x,y table T (dxy + dx + dy ints), then reads
-// every touched cell back once with atomicExch.  s_ax: two shared ints.
-template <bool kFp64>
-__device__ inline Partial score_huge_strata(Partial acc, const int *cnt, const uint16_t *gord, const int *big,
-                                            int list_cap, int n_huge, int dx, int dy, int *T, const uint64_t *gzk,
-                                            bool want_hash, int *s_ax) {
-    const int tid = threadIdx.x;
-    const int dxy = dx * dy;
-    int *ni = T + dxy, *nj = ni + dx;
-    TermAcc<kFp64> ta;
-    for (int h = 0; h < n_huge; ++h) {
-        const int k = big[list_cap - 1 - h];
-        const int o0 = cnt[k], m = cnt[k + 1] - o0;
-        int ax = 0, ay = 0;
-        for (int i = tid; i < m; i += kThreads) {
-            const int p = gord[o0 + i];
-            const int x = p >> 8, y = p & 0xff;
-            atomicAdd(&T[x * dy + y], 1);
-            ax += atomicAdd(&ni[x], 1) == 0;
-            ay += atomicAdd(&nj[y], 1) == 0;
-        }
-        if (ax) atomicAdd(&s_ax[0], ax);
-        if (ay) atomicAdd(&s_ax[1], ay);
-        __syncthreads();
-        for (int i = tid; i < m; i += kThreads) {
-            const int p = gord[o0 + i];
-            const int x = p >> 8, y = p & 0xff;
-            const int O = atomicExch(&T[x * dy + y], 0);
-            if (O > 0) {
-                ta.add(O, ni[x], nj[y], m);
-                if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x) * (uint64_t)dy + y, (uint32_t)O);
-            }
-        }
-        __syncthreads();
-        for (int i = tid; i < dx + dy; i += kThreads) ni[i] = 0;  // nj follows ni
-        if (tid == 0) {
-            acc.df += (long long)(max(s_ax[0], 1) - 1) * (max(s_ax[1], 1) - 1);
-            s_ax[0] = s_ax[1] = 0;
-        }
-        __syncthreads();
-    }
-    ta.into(acc);
-    return acc;
-}
-
 // Phase timers (ns per phase, summed over tests) when a.dbg is set; off in normal runs.
 __device__ __forceinline__ unsigned long long gtimer() {
     unsigned long long t;
@@ -729,8 +677,6 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     __shared__ const uint8_t *s_col[kMaxCols];
     __shared__ uint32_t s_dim[kMaxCols];
     __shared__ int s_idx, s_over, s_distinct, s_flag;
-    __shared__ int s_nbig[2];  // strata scored by warps, by the whole CTA
-    __shared__ int s_ax[2];
     __shared__ int s_w[kWarps];
     __shared__ Partial scratch[kWarps];
     const int tid = threadIdx.x;
@@ -896,27 +842,18 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         FPGM_PHASE(3);
         // 3. score the strata: FP32 terms first, FP64 only inside the recheck band
         const int dxy = dx * dy;
-        const bool wsmem = dxy + dx + dy <= kSparseWarpTab;           // per-warp tables in shared memory
-        const bool tsmem = dxy + dx + dy <= kWarps * kSparseWarpTab;  // the CTA's table in shared memory
+        const bool wsmem = dxy + dx + dy <= kSparseWarpTab;
         int *wt = wsmem ? swt + (threadIdx.x >> 5) * kSparseWarpTab : gwt + (int64_t)(threadIdx.x >> 5) * kGlobalWarpTab;
-        if (tsmem)  // the table region held hash ids until now (the global tables are kept zeroed)
+        if (wsmem)  // the table region held ids or cursors until now
             for (int i = tid; i < kWarps * kSparseWarpTab; i += kThreads) swt[i] = 0;
-        if (tid == 0) {
-            s_nbig[0] = s_nbig[1] = 0;
-            s_ax[0] = s_ax[1] = 0;
-        }
+        if (tid == 0) s_over = 0;
         __syncthreads();
         // stratum ids of larger strata: the dead cursors in shared memory, else the free gsid
         int *big = global ? gsid : scur;
-        const int list_cap = n_obs + 1;
-        Partial acc = score_small_strata<false>(cnt, gord, n_obs, dx, dy, big, s_nbig, list_cap, zk,
-                                                a.want_hash != 0, true);
+        Partial acc = score_small_strata<false>(cnt, gord, n_obs, dx, dy, big, &s_over, zk, a.want_hash != 0, true);
         __syncthreads();
-        const int n_big = s_nbig[0], n_huge = s_nbig[1];
+        const int n_big = s_over;
         FPGM_PHASE(4);
-        // the whole CTA takes the largest strata (one dense table for the block)
-        int *T = tsmem ? swt : gwt;
-        acc = score_huge_strata<false>(acc, cnt, gord, big, list_cap, n_huge, dx, dy, T, zk, a.want_hash != 0, s_ax);
         acc = score_big_strata<false>(acc, cnt, gord, big, n_big, dx, dy, wt, zk, a.want_hash != 0);
         Partial r = block_sum(acc, scratch);
         FPGM_PHASE(5);
@@ -936,8 +873,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         }
         Verdict v{r.df, r.g2, 1.0, 1, 0, 0.0, r.hash};
         if (dec < 0) {
-            Partial q = score_small_strata<true>(cnt, gord, n_obs, dx, dy, big, nullptr, list_cap, nullptr, false, false);
-            q = score_huge_strata<true>(q, cnt, gord, big, list_cap, n_huge, dx, dy, T, nullptr, false, s_ax);
+            Partial q = score_small_strata<true>(cnt, gord, n_obs, dx, dy, big, nullptr, nullptr, false, false);
             q = score_big_strata<true>(q, cnt, gord, big, n_big, dx, dy, wt, nullptr, false);
             const Partial r2 = block_sum(q, scratch);
             v.g2 = r2.g2;
