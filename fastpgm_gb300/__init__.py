@@ -39,7 +39,7 @@ class PCStats(ctypes.Structure):
                 ("near_ties", ctypes.c_int64), ("large_tests", ctypes.c_int64), ("max_abs_dp", ctypes.c_double),
                 ("count_ms", ctypes.c_double), ("count_bytes", ctypes.c_double), ("large_ms", ctypes.c_double),
                 ("count_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("span_ms", ctypes.c_double),
-                ("total_ms", ctypes.c_double)]
+                ("total_ms", ctypes.c_double), ("large_bytes", ctypes.c_double)]
 
     def to_dict(self):
         L = self.n_levels
@@ -52,7 +52,8 @@ class PCStats(ctypes.Structure):
                 "count_ms": float(self.count_ms), "count_bytes": float(self.count_bytes),
                 "large_ms": float(self.large_ms),
                 "count_launches": int(self.count_launches), "kernel_launches": int(self.kernel_launches),
-                "span_ms": float(self.span_ms), "total_ms": float(self.total_ms)}
+                "span_ms": float(self.span_ms), "total_ms": float(self.total_ms),
+                "large_bytes": float(self.large_bytes)}
 
 
 class GenSpec(ctypes.Structure):
@@ -182,6 +183,14 @@ class Engine:
 
     def result(self):
         """Returns dict(adj [n,n] uint8, removed [k,2] int32, sep_offsets, sep_vars, sepsets dict)."""
+        r = self.result_arrays()
+        off, var = r["sep_offsets"], r["sep_vars"]
+        r["sepsets"] = {(int(a), int(b)): tuple(int(v) for v in var[off[k]:off[k + 1]])
+                        for k, (a, b) in enumerate(r["removed"])}
+        return r
+
+    def result_arrays(self):
+        """The skeleton as arrays only: adj [n,n] uint8, removed [k,2] int32, sep_offsets [k+1], sep_vars."""
         L = load()
         nn, nr, nv = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
         _check(L.fpgm_pc_result_sizes(self._h, ctypes.byref(nn), ctypes.byref(nr), ctypes.byref(nv)))
@@ -191,10 +200,7 @@ class Engine:
         off = np.zeros(nr.value + 1, dtype=np.int32)
         var = np.zeros(max(1, nv.value), dtype=np.int32)
         _check(L.fpgm_pc_result_fetch(self._h, _u8(adj), _i32(removed), _i32(off), _i32(var)))
-        removed = removed[:nr.value]
-        seps = {(int(a), int(b)): tuple(int(v) for v in var[off[k]:off[k + 1]])
-                for k, (a, b) in enumerate(removed)}
-        return {"adj": adj, "removed": removed, "sep_offsets": off, "sep_vars": var[:nv.value], "sepsets": seps}
+        return {"adj": adj, "removed": removed[:nr.value], "sep_offsets": off, "sep_vars": var[:nv.value]}
 
 
 def orient_cpdag(adj, removed, sep_offsets, sep_vars):

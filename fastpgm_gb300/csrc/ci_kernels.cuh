@@ -6,9 +6,11 @@
 //                              per-warp slice of shared memory (<= 3072 ints)
 //   tier 1  ci_cta_kernel      one CTA per test, table in 96 KB of shared memory
 //   tier 2  ci_compact_kernel  one CTA per test; the observed Z strata are hashed
-//                              to compact ids, the samples counting-sorted by
-//                              stratum, and one warp per stratum scores it --
-//                              work O(samples), never O(dz) or O(strata * dx * dy)
+//                              to compact ids, then either counted into a dense
+//                              strata x (x,y) table (when it has at most 8 cells
+//                              per sample and 32 per stratum) or counting-sorted
+//                              by stratum and scored per stratum -- work
+//                              O(samples + strata * dx * dy), never O(dz)
 //
 // Tiers 0/1 count with 128-bit column loads folded into packed 16-bit Horner
 // codes (two samples per 32-bit multiply-add) and shared-memory atomics into R
@@ -59,7 +61,8 @@ struct WaveArgs {
     // compact tier: per-CTA global slots
     char *slot_mem;
     int64_t slot_bytes;
-    int32_t hash_cap_global;  // power of two >= 2 * n_samples
+    int64_t slot_S;           // sample count the slot layout was made for (>= S)
+    int32_t hash_cap_global;  // power of two >= 2 * slot_S
     unsigned long long *dbg;  // compact-tier phase timers (FPGM_PHASE_TIMERS), else null
 };
 
@@ -351,6 +354,7 @@ constexpr int kZTabOff = (kZCurOff + (kZStrata + 1) * 4 + 15) / 16 * 16;
 constexpr int kSparseWarpTab = (kSmemBytes - kZTabOff) / 4 / kWarps;  // ints per warp
 constexpr int kLaneStratum = 8;   // strata of up to this many samples: one lane each
 constexpr int kRegStratum = 64;   // larger strata up to this size keep their codes in registers
+constexpr int kDenseMul = 8;      // dense strata x cells table when it has at most this many cells per sample
 
 __device__ __forceinline__ uint32_t zhash(uint64_t z, uint32_t cap) {
     return (uint32_t)((z * 0x9E3779B97F4A7C15ull) >> 32) & (cap - 1);
@@ -407,7 +411,7 @@ __device__ __forceinline__ void zcodes16(uint64_t (&z)[16], const uint8_t *const
 
 // Byte offsets of one compact-tier global slot, every region 256-byte aligned.
 struct SlotLayout {
-    int64_t keys, zk, ids, cnt, cur, sid, wt, ord, total;
+    int64_t keys, zk, ids, cnt, cur, sid, wt, ord, tab, total;
 };
 __host__ __device__ inline int64_t align256(int64_t x) { return (x + 255) & ~(int64_t)255; }
 __host__ __device__ inline SlotLayout slot_layout(int64_t S, int64_t cap) {
@@ -421,6 +425,7 @@ __host__ __device__ inline SlotLayout slot_layout(int64_t S, int64_t cap) {
     L.sid = o;  o = align256(o + (S + 16) * 4);   // slot, then stratum id, per sample
     L.wt = o;   o = align256(o + (int64_t)kWarps * kGlobalWarpTab * 4);  // wide x,y tables, kept zeroed
     L.ord = o;  o = align256(o + S * 2);          // (x << 8) | y codes sorted by stratum
+    L.tab = o;  o = align256(o + ((int64_t)kDenseMul * S + 64) * 4);  // dense strata x cells counts, kept zeroed
     L.total = o;
     return L;
 }
@@ -651,6 +656,47 @@ __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const ui
     return acc;
 }
 
+// Dense strata x cells table T[k * dxy + x * dy + y] (k = stratum id), at most 32 cells per
+// stratum: lane groups of G = 2^ceil(log2 dxy) lanes, one stratum per group and one cell per
+// lane, the margins by shuffles within the group.  The next strata's cells are loaded while
+// the current ones are scored.
+template <bool kFp64>
+__device__ inline Partial score_dense_groups(const int *T, int n_obs, int dx, int dy, const uint64_t *gzk,
+                                             bool want_hash) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int dxy = dx * dy;
+    int lg = 0;
+    while ((1 << lg) < dxy) ++lg;
+    const int G = 1 << lg, gpw = 32 >> lg, gi = lane >> lg, gl = lane & (G - 1);
+    const unsigned gmask = G == 32 ? full : (((1u << G) - 1u) << (gi * G));
+    const int x = gl / dy, y = gl - x * dy;
+    const bool cell = gl < dxy;
+    Partial acc{0, 0.0, 0.0, 0.0, 0ull};
+    TermAcc<kFp64> ta;
+    const int step = kWarps * gpw;
+    int k = warp * gpw + gi;
+    int On = (cell && k < n_obs) ? __ldcg(T + (int64_t)k * dxy + gl) : 0;
+    for (int k0 = warp * gpw; k0 < n_obs; k0 += step, k += step) {
+        const int O = On;
+        On = (cell && k + step < n_obs) ? __ldcg(T + (int64_t)(k + step) * dxy + gl) : 0;
+        int Nx = 0, Ny = 0, m = O;
+        for (int j = 0; j < dy; ++j) Nx += __shfl_sync(full, O, x * dy + j, G);
+        for (int i = 0; i < dx; ++i) Ny += __shfl_sync(full, O, i * dy + y, G);
+        for (int o = G >> 1; o > 0; o >>= 1) m += __shfl_xor_sync(full, m, o, G);
+        const bool valid = cell && k < n_obs;
+        const int r = __popc(__ballot_sync(full, valid && y == 0 && Nx > 0) & gmask);
+        const int c = __popc(__ballot_sync(full, valid && x == 0 && Ny > 0) & gmask);
+        if (valid && gl == 0) acc.df += (long long)(max(r, 1) - 1) * (max(c, 1) - 1);
+        if (valid && O > 0) {
+            ta.add(O, Nx, Ny, m);
+            if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x) * (uint64_t)dy + y, (uint32_t)O);
+        }
+    }
+    ta.into(acc);
+    return acc;
+}
+
 // Phase timers (ns per phase, summed over tests) when a.dbg is set; off in normal runs.
 __device__ __forceinline__ unsigned long long gtimer() {
     unsigned long long t;
@@ -661,6 +707,10 @@ __device__ __forceinline__ unsigned long long gtimer() {
 // Tier 2: joint tables too large for shared memory, counted in O(samples):
 //  1. the observed Z strata are hashed, each new one taking the next id (shared-memory
 //     hash of kZCap slots; a global one sized >= 2 n_samples when more than kZStrata);
+//  dense path (strata x dx x dy <= kDenseMul n_samples, dx dy <= 32): every sample adds
+//     one to T[id][x][y] in the CTA's global slot, and lane groups score the strata from
+//     T (score_dense_groups); the table is zeroed again after the decision;
+//  otherwise:
 //  2. samples are counting-sorted by stratum, stored as packed (x << 8) | y;
 //  3. a stratum of at most kLaneStratum samples is scored by one thread with pairwise
 //     comparisons; a larger one by one warp that counts its x,y cells in a small dense
@@ -683,7 +733,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     const int64_t S = a.S;
     const uint32_t gcap = (uint32_t)a.hash_cap_global;
     char *slot = a.slot_mem + (int64_t)blockIdx.x * a.slot_bytes;
-    const SlotLayout L = slot_layout(S, gcap);
+    const SlotLayout L = slot_layout(a.slot_S, gcap);
     uint64_t *gkeys = reinterpret_cast<uint64_t *>(slot + L.keys);
     uint64_t *gzk = reinterpret_cast<uint64_t *>(slot + L.zk);
     int *gids = reinterpret_cast<int *>(slot + L.ids);
@@ -692,6 +742,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     int *gsid = reinterpret_cast<int *>(slot + L.sid);
     int *gwt = reinterpret_cast<int *>(slot + L.wt);
     uint16_t *gord = reinterpret_cast<uint16_t *>(slot + L.ord);
+    int *gtab = reinterpret_cast<int *>(slot + L.tab);
     const int n2 = a.counters[C_TIER2];
     const int d = a.d, ncols = d + 2;
     const int64_t nvec = S >> 4;
@@ -735,12 +786,26 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
                 if (*(volatile int *)&s_over) break;
                 uint64_t z[16];
                 zcodes16(z, s_col, s_dim, d, v);
+                // first probes of all 16 codes in flight at once; a code found there (the common
+                // case) is done, the others take the inserting path (a stale empty slot read
+                // here is resolved by its compare-and-swap)
                 int hs[16];
                 bool ok = true;
-                for (int b = 0; b < 16 && ok; ++b) {
-                    hs[b] = global ? zinsert(keys, gids, cap, z[b], &s_distinct, limit, max_probe, zk)
-                                   : zinsert(keys, hids, cap, z[b], &s_distinct, limit, max_probe, zk);
-                    ok = hs[b] >= 0;
+#pragma unroll
+                for (int b0 = 0; b0 < 16; b0 += 8) {  // eight at a time (register budget)
+                    uint64_t kk[8];
+#pragma unroll
+                    for (int b = 0; b < 8; ++b) {
+                        hs[b0 + b] = (int)zhash(z[b0 + b], cap);
+                        kk[b] = keys[hs[b0 + b]];
+                    }
+#pragma unroll
+                    for (int b = 0; b < 8; ++b) {
+                        if (!ok || kk[b] == z[b0 + b]) continue;
+                        hs[b0 + b] = global ? zinsert(keys, gids, cap, z[b0 + b], &s_distinct, limit, max_probe, zk)
+                                            : zinsert(keys, hids, cap, z[b0 + b], &s_distinct, limit, max_probe, zk);
+                        ok = hs[b0 + b] >= 0;
+                    }
                 }
                 if (!ok) {
                     s_over = 1;
@@ -783,80 +848,122 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             atomicAdd(&a.dbg[10], (unsigned long long)n_obs);
             atomicAdd(&a.dbg[11], 1ull);
         }
+        const int dy = s_dim[d + 1], dx = s_dim[d];
+        const int dxy = dx * dy;
+        const uint8_t *colx = s_col[d], *coly = s_col[d + 1];
+        // dense strata table when it is small next to the samples and a stratum's cells fit
+        // one warp (lane-group scoring); otherwise the counting-sort path
+        const bool dense = (int64_t)n_obs * dxy <= (int64_t)kDenseMul * S && dxy <= 32;
         int *cnt = global ? gcnt : scnt;
         int *cur = global ? gcur : scur;
-        // 2. counting sort of the samples by stratum
-        for (int i = tid; i <= n_obs; i += kThreads) cnt[i] = 0;
-        __syncthreads();
-        for (int64_t s4 = tid; s4 < (S >> 2); s4 += kThreads) {
-            int4 h = reinterpret_cast<int4 *>(gsid)[s4];
-            if (global) {
-                h.x = gids[h.x];
-                h.y = gids[h.y];
-                h.z = gids[h.z];
-                h.w = gids[h.w];
-            } else {
-                h.x = hids[h.x];
-                h.y = hids[h.y];
-                h.z = hids[h.z];
-                h.w = hids[h.w];
-            }
-            reinterpret_cast<int4 *>(gsid)[s4] = h;
-            atomicAdd(&cnt[h.x], 1);
-            atomicAdd(&cnt[h.y], 1);
-            atomicAdd(&cnt[h.z], 1);
-            atomicAdd(&cnt[h.w], 1);
-        }
-        for (int64_t s = (S & ~(int64_t)3) + tid; s < S; s += kThreads) {
-            const int sid = global ? gids[gsid[s]] : (int)hids[gsid[s]];
-            gsid[s] = sid;
-            atomicAdd(&cnt[sid], 1);
-        }
-        __syncthreads();
-        FPGM_PHASE(2);
-        block_exclusive_scan(cnt, n_obs + 1, s_w);  // cnt -> stratum offsets, cnt[n_obs] = S
-        for (int i = tid; i <= n_obs; i += kThreads) cur[i] = cnt[i];
-        __syncthreads();
-        const int dy = s_dim[d + 1], dx = s_dim[d];
-        const uint8_t *colx = s_col[d], *coly = s_col[d + 1];
-        for (int64_t v = tid; v < nvec; v += kThreads) {
-            const uint4 wx = __ldg(reinterpret_cast<const uint4 *>(colx) + v);
-            const uint4 wy = __ldg(reinterpret_cast<const uint4 *>(coly) + v);
-            const uint32_t xx[4] = {wx.x, wx.y, wx.z, wx.w}, yy[4] = {wy.x, wy.y, wy.z, wy.w};
+        // stratum ids of larger strata (sorted path): the dead cursors in shared memory, else the free gsid
+        int *big = global ? gsid : scur;
+        int n_big = 0;
+        int *wt = nullptr;           // sorted path: per-warp x,y table
+        Partial acc;
+        if (dense) {
+            if (a.dbg && tid == 0) atomicAdd(&a.dbg[12], 1ull);
+            // 2'. strata x cells counted straight into the dense table (kept zeroed between tests)
+            for (int64_t v = tid; v < nvec; v += kThreads) {
+                const uint4 wx = __ldg(reinterpret_cast<const uint4 *>(colx) + v);
+                const uint4 wy = __ldg(reinterpret_cast<const uint4 *>(coly) + v);
+                const uint32_t xx[4] = {wx.x, wx.y, wx.z, wx.w}, yy[4] = {wy.x, wy.y, wy.z, wy.w};
+                int sid[16];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int4 sid = reinterpret_cast<const int4 *>(gsid)[v * 4 + q];
-                const int sv[4] = {sid.x, sid.y, sid.z, sid.w};
+                for (int q = 0; q < 4; ++q) {
+                    const int4 h = reinterpret_cast<const int4 *>(gsid)[v * 4 + q];
+                    sid[4 * q] = h.x;
+                    sid[4 * q + 1] = h.y;
+                    sid[4 * q + 2] = h.z;
+                    sid[4 * q + 3] = h.w;
+                }
+                // all 16 id lookups before the first increment (the increments could alias them)
 #pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    const int pos = atomicAdd(&cur[sv[b]], 1);
-                    gord[pos] = (uint16_t)((((xx[q] >> (8 * b)) & 0xffu) << 8) | ((yy[q] >> (8 * b)) & 0xffu));
+                for (int b = 0; b < 16; ++b) sid[b] = global ? __ldcg(gids + sid[b]) : (int)hids[sid[b]];
+#pragma unroll
+                for (int b = 0; b < 16; ++b) {
+                    const int q = b >> 2, sh = 8 * (b & 3);
+                    const int c = (int)((xx[q] >> sh) & 0xffu) * dy + (int)((yy[q] >> sh) & 0xffu);
+                    atomicAdd(&gtab[(int64_t)sid[b] * dxy + c], 1);
                 }
             }
+            for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
+                const int sid = global ? gids[gsid[s]] : (int)hids[gsid[s]];
+                atomicAdd(&gtab[(int64_t)sid * dxy + colx[s] * dy + coly[s]], 1);
+            }
+            __syncthreads();
+            FPGM_PHASE(7);
+            acc = score_dense_groups<false>(gtab, n_obs, dx, dy, zk, a.want_hash != 0);
+            FPGM_PHASE(8);
+        } else {
+            // 2. counting sort of the samples by stratum
+            for (int i = tid; i <= n_obs; i += kThreads) cnt[i] = 0;
+            __syncthreads();
+            for (int64_t s4 = tid; s4 < (S >> 2); s4 += kThreads) {
+                int4 h = reinterpret_cast<int4 *>(gsid)[s4];
+                if (global) {
+                    h.x = gids[h.x];
+                    h.y = gids[h.y];
+                    h.z = gids[h.z];
+                    h.w = gids[h.w];
+                } else {
+                    h.x = hids[h.x];
+                    h.y = hids[h.y];
+                    h.z = hids[h.z];
+                    h.w = hids[h.w];
+                }
+                reinterpret_cast<int4 *>(gsid)[s4] = h;
+                atomicAdd(&cnt[h.x], 1);
+                atomicAdd(&cnt[h.y], 1);
+                atomicAdd(&cnt[h.z], 1);
+                atomicAdd(&cnt[h.w], 1);
+            }
+            for (int64_t s = (S & ~(int64_t)3) + tid; s < S; s += kThreads) {
+                const int sid = global ? gids[gsid[s]] : (int)hids[gsid[s]];
+                gsid[s] = sid;
+                atomicAdd(&cnt[sid], 1);
+            }
+            __syncthreads();
+            FPGM_PHASE(2);
+            block_exclusive_scan(cnt, n_obs + 1, s_w);  // cnt -> stratum offsets, cnt[n_obs] = S
+            for (int i = tid; i <= n_obs; i += kThreads) cur[i] = cnt[i];
+            __syncthreads();
+            for (int64_t v = tid; v < nvec; v += kThreads) {
+                const uint4 wx = __ldg(reinterpret_cast<const uint4 *>(colx) + v);
+                const uint4 wy = __ldg(reinterpret_cast<const uint4 *>(coly) + v);
+                const uint32_t xx[4] = {wx.x, wx.y, wx.z, wx.w}, yy[4] = {wy.x, wy.y, wy.z, wy.w};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int4 sid = reinterpret_cast<const int4 *>(gsid)[v * 4 + q];
+                    const int sv[4] = {sid.x, sid.y, sid.z, sid.w};
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) {
+                        const int pos = atomicAdd(&cur[sv[b]], 1);
+                        gord[pos] = (uint16_t)((((xx[q] >> (8 * b)) & 0xffu) << 8) | ((yy[q] >> (8 * b)) & 0xffu));
+                    }
+                }
+            }
+            for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
+                const int pos = atomicAdd(&cur[gsid[s]], 1);
+                gord[pos] = (uint16_t)((colx[s] << 8) | coly[s]);
+            }
+            __syncthreads();
+            FPGM_PHASE(3);
+            // 3. score the strata: FP32 terms first, FP64 only inside the recheck band
+            const bool wsmem = dxy + dx + dy <= kSparseWarpTab;
+            wt = wsmem ? swt + (threadIdx.x >> 5) * kSparseWarpTab : gwt + (int64_t)(threadIdx.x >> 5) * kGlobalWarpTab;
+            if (wsmem)  // the table region held ids or cursors until now
+                for (int i = tid; i < kWarps * kSparseWarpTab; i += kThreads) swt[i] = 0;
+            if (tid == 0) s_over = 0;
+            __syncthreads();
+            acc = score_small_strata<false>(cnt, gord, n_obs, dx, dy, big, &s_over, zk, a.want_hash != 0, true);
+            __syncthreads();
+            n_big = s_over;
+            FPGM_PHASE(4);
+            acc = score_big_strata<false>(acc, cnt, gord, big, n_big, dx, dy, wt, zk, a.want_hash != 0);
+            FPGM_PHASE(5);
         }
-        for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
-            const int pos = atomicAdd(&cur[gsid[s]], 1);
-            gord[pos] = (uint16_t)((colx[s] << 8) | coly[s]);
-        }
-        __syncthreads();
-        FPGM_PHASE(3);
-        // 3. score the strata: FP32 terms first, FP64 only inside the recheck band
-        const int dxy = dx * dy;
-        const bool wsmem = dxy + dx + dy <= kSparseWarpTab;
-        int *wt = wsmem ? swt + (threadIdx.x >> 5) * kSparseWarpTab : gwt + (int64_t)(threadIdx.x >> 5) * kGlobalWarpTab;
-        if (wsmem)  // the table region held ids or cursors until now
-            for (int i = tid; i < kWarps * kSparseWarpTab; i += kThreads) swt[i] = 0;
-        if (tid == 0) s_over = 0;
-        __syncthreads();
-        // stratum ids of larger strata: the dead cursors in shared memory, else the free gsid
-        int *big = global ? gsid : scur;
-        Partial acc = score_small_strata<false>(cnt, gord, n_obs, dx, dy, big, &s_over, zk, a.want_hash != 0, true);
-        __syncthreads();
-        const int n_big = s_over;
-        FPGM_PHASE(4);
-        acc = score_big_strata<false>(acc, cnt, gord, big, n_big, dx, dy, wt, zk, a.want_hash != 0);
-        Partial r = block_sum(acc, scratch);
-        FPGM_PHASE(5);
+        const Partial r = block_sum(acc, scratch);
         const double err = 2.0 * r.err + 1e-6 * r.abs_g2 + 1e-12;
         int dec = band_decide(r.df, r.g2, err, a.bt);
         if (dec < 0 && r.df > a.bt.dfmax) {
@@ -873,8 +980,13 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         }
         Verdict v{r.df, r.g2, 1.0, 1, 0, 0.0, r.hash};
         if (dec < 0) {
-            Partial q = score_small_strata<true>(cnt, gord, n_obs, dx, dy, big, nullptr, nullptr, false, false);
-            q = score_big_strata<true>(q, cnt, gord, big, n_big, dx, dy, wt, nullptr, false);
+            Partial q;
+            if (dense) {
+                q = score_dense_groups<true>(gtab, n_obs, dx, dy, nullptr, false);
+            } else {
+                q = score_small_strata<true>(cnt, gord, n_obs, dx, dy, big, nullptr, nullptr, false, false);
+                q = score_big_strata<true>(q, cnt, gord, big, n_big, dx, dy, wt, nullptr, false);
+            }
             const Partial r2 = block_sum(q, scratch);
             v.g2 = r2.g2;
             v.rechecked = 1;
@@ -890,6 +1002,13 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         if (tid == 0) {
             atomicAdd(&a.stats[ST_LARGE], 1ull);
             record(a, item, v, (int64_t)n_obs * dxy, 0, 2);
+        }
+        if (dense) {  // leave the table zeroed for the next test
+            __syncthreads();
+            const int64_t ncell = (int64_t)n_obs * dxy;
+            for (int64_t i = tid; i < (ncell >> 2); i += kThreads)
+                reinterpret_cast<int4 *>(gtab)[i] = make_int4(0, 0, 0, 0);
+            for (int64_t i = (ncell & ~(int64_t)3) + tid; i < ncell; i += kThreads) gtab[i] = 0;
         }
         FPGM_PHASE(6);
         __syncthreads();

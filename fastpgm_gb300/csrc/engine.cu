@@ -125,7 +125,7 @@ struct fpgm_engine {
     DevBuf slots, plain_ws, tests_buf, detail_buf, item_vars, lists, band, phase_timers;
     double band_alpha = -1.0;
     int n_slots = 0, hash_cap_global = 0;
-    int64_t slot_bytes = 0;
+    int64_t slot_bytes = 0, slot_S = 0;  // slot_S: the sample count the slots' layout was made for
     // result
     bool has_result = false;
     std::vector<uint8_t> res_adj;
@@ -468,6 +468,12 @@ extern "C" int fpgm_dataset_upload(fpgm_engine *e, const uint8_t *columns, int32
     e->h_card.resize(n_vars);
     CK(cudaMemcpyAsync(e->h_card.data(), e->card.p, n_vars, cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
+    for (int32_t v = 0; v < n_vars; ++v)
+        if (e->h_card[v] == 0) {  // 256 states wrap the uint8 cardinality to 0
+            e->n = 0;
+            return set_error(FPGM_ERR_UNSUPPORTED,
+                             "fpgm_dataset_upload: column %d has 256 states; at most 255 are supported", v);
+        }
     if (out_card) memcpy(out_card, e->h_card.data(), n_vars);
     return FPGM_OK;
 }
@@ -513,15 +519,18 @@ int64_t max_table_ints(const std::vector<uint8_t> &card, int d) {
 // The global strata hash must hold every sample's stratum at load <= 1/2, so it is
 // resized whenever a dataset with more samples is uploaded.
 int ensure_slots(fpgm_engine *e) {
+    // The regions are laid out for slot_S samples and reused, as they are, for any dataset of
+    // at most slot_S samples, so the regions kept zeroed between tests stay where they were.
+    if (e->slots.p && e->S <= e->slot_S) return FPGM_OK;
     uint32_t cap = 4096;
     while ((int64_t)cap < 2 * e->S) cap <<= 1;
-    if (e->slots.p && (uint32_t)e->hash_cap_global >= cap) return FPGM_OK;
     e->slots.release();
+    e->slot_S = e->S;
     e->hash_cap_global = (int)cap;
     e->n_slots = 2 * e->num_sms;
-    e->slot_bytes = slot_layout(e->S, cap).total;
+    e->slot_bytes = slot_layout(e->slot_S, cap).total;
     RET(e->slots.ensure((size_t)e->slot_bytes * e->n_slots));
-    CK(cudaMemsetAsync(e->slots.p, 0, (size_t)e->slot_bytes * e->n_slots, e->stream));  // warp tables start zeroed
+    CK(cudaMemsetAsync(e->slots.p, 0, (size_t)e->slot_bytes * e->n_slots, e->stream));  // zeroed tables
     return FPGM_OK;
 }
 
@@ -551,6 +560,7 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t ite
         RET(ensure_slots(e));
         a.slot_mem = e->slots.as<char>();
         a.slot_bytes = e->slot_bytes;
+        a.slot_S = e->slot_S;
         a.hash_cap_global = e->hash_cap_global;
     }
     return FPGM_OK;
@@ -629,9 +639,11 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
             if (h[11])
                 fprintf(stderr,
                         "compact d=%d tests=%llu strata/test=%.0f us/test: shared-hash=%.1f global-hash=%.1f "
-                        "count=%.1f sort=%.1f small=%.1f big=%.1f decide=%.1f\n",
+                        "count=%.1f sort=%.1f small=%.1f big=%.1f | dense tests=%llu scatter=%.1f score=%.1f | "
+                        "decide=%.1f\n",
                         d, h[11], (double)h[10] / h[11], h[0] / 1e3 / h[11], h[1] / 1e3 / h[11], h[2] / 1e3 / h[11],
-                        h[3] / 1e3 / h[11], h[4] / 1e3 / h[11], h[5] / 1e3 / h[11], h[6] / 1e3 / h[11]);
+                        h[3] / 1e3 / h[11], h[4] / 1e3 / h[11], h[5] / 1e3 / h[11], h[12], h[7] / 1e3 / h[11],
+                        h[8] / 1e3 / h[11], h[6] / 1e3 / h[11]);
         }
         CK(cudaEventRecord(e->ev2, e->stream));
         CK(cudaMemsetAsync(dstat + ST_UNRESOLVED, 0, 8, e->stream));
@@ -640,16 +652,19 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
             e->next.as<uint64_t>(), e->total.as<uint64_t>(), e->seprank.as<uint64_t>(), dstat);
         CK(cudaGetLastError());
         unsigned long long hs[ST_COUNT];
-        int32_t T = 0;
+        int32_t T = 0, tiers[C_COUNT];
         CK(cudaMemcpyAsync(hs, dstat, sizeof hs, cudaMemcpyDeviceToHost, e->stream));
         CK(cudaMemcpyAsync(&T, e->off.as<int32_t>() + n_active, 4, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaMemcpyAsync(tiers, e->counters.p, sizeof tiers, cudaMemcpyDeviceToHost, e->stream));
         CK(cudaStreamSynchronize(e->stream));
         float ms = 0.f, ms2 = 0.f;
         CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
         CK(cudaEventElapsedTime(&ms2, e->ev1, e->ev2));
         st->count_ms += ms;
         st->large_ms += ms2;
-        st->count_bytes += (double)T * (2.0 + d) * (double)e->S;
+        // algorithmic bytes: (2 + d) columns of n_samples per test, split by kernel
+        st->count_bytes += (double)(tiers[C_TIER0] + tiers[C_TIER1]) * (2.0 + d) * (double)e->S;
+        st->large_bytes += (double)tiers[C_TIER2] * (2.0 + d) * (double)e->S;
         st->count_launches += 1;
         if (hs[ST_UNSUPPORTED])
             return set_error(FPGM_ERR_UNSUPPORTED,
@@ -881,6 +896,7 @@ int plain_test(fpgm_engine *e, int x, int y, const int *z, int d, double alpha, 
         RET(ensure_slots(e));
         a.slot_mem = e->slots.as<char>();
         a.slot_bytes = e->slot_bytes;
+        a.slot_S = e->slot_S;
         a.hash_cap_global = e->hash_cap_global;
         a.detail = e->detail_buf.as<fpgm_ci_result>();
         a.want_hash = want_hash;

@@ -89,6 +89,7 @@ typedef struct {
     int64_t kernel_launches;     /* launches of this library's own kernels (library scans excluded) */
     double span_ms;              /* CUDA-event span of the whole call on the engine's stream */
     double total_ms;             /* host wall time of the whole skeleton call */
+    double large_bytes;          /* algorithmic bytes of the global-memory kernel's tests */
 } fpgm_pc_stats;
 
 typedef struct {

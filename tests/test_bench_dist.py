@@ -1,0 +1,68 @@
+"""bench.py's multi-process helpers on CPU: two gloo ranks over 127.0.0.1.
+
+The engine's multi-GPU mode is replicas only (no collective on the data path); what
+crosses ranks is the timing: a barrier around the timed region, the max of the ranks'
+times and the sum of their tests.  The reference arm runs on rank 0 alone."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+_WORKER = r"""
+import json, os, sys
+sys.path.insert(0, sys.argv[1])
+import bench
+d = bench.Dist()
+d.barrier()
+r = d.rank
+out = {"rank": r, "world": d.world, "max": d.max(1.5 + r), "sum": d.sum(10 * (r + 1))}
+d.barrier()
+d.close()
+print(json.dumps(out))
+"""
+
+
+def test_dist_helpers_two_gloo_ranks(tmp_path):
+    port = _free_port()
+    procs = []
+    for rank in range(2):
+        env = dict(os.environ, RANK=str(rank), LOCAL_RANK=str(rank), WORLD_SIZE="2", MASTER_ADDR="127.0.0.1",
+                   MASTER_PORT=str(port), FPGM_DIST_BACKEND="gloo")
+        procs.append(subprocess.Popen([sys.executable, "-c", _WORKER, ROOT], env=env, stdout=subprocess.PIPE,
+                                      stderr=subprocess.PIPE, text=True))
+    outs = []
+    for p in procs:
+        o, e = p.communicate(timeout=120)
+        assert p.returncode == 0, e
+        outs.append(json.loads(o.strip().splitlines()[-1]))
+    for o in outs:
+        assert o["world"] == 2
+        assert o["max"] == 2.5
+        assert o["sum"] == 30
+
+
+def test_reference_arm_prints_one_line_under_torchrun():
+    port = _free_port()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
+           "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"), "--impl", "reference",
+           "--gpus", "2", "--config", "c1", "--steps", "1", "--warmup", "0"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    j = json.loads(lines[0])
+    assert j["impl"] == "reference" and j["n_gpus"] == 2
+    assert j["cpu_baseline"]["kind"] == "port" and j["value"] > 0
+    assert j["e2e"]["h2d_bytes_per_step"] == 0 and j["e2e"]["d2h_bytes_per_step"] == 0

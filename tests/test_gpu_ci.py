@@ -160,3 +160,34 @@ def test_invalid_arguments_are_errors(eng):
         eng.ci_test(0, 1, (), alpha=1.5)
     with pytest.raises(F.FpgmError):
         eng.ci_test_batch(np.array([[0, 1, 40]], dtype=np.int32), 1)
+
+
+def test_256_state_column_is_rejected_at_upload(eng):
+    """Cardinalities are uint8: a column with all 256 byte values is refused, not wrapped."""
+    raw = np.zeros((3, 1024), dtype=np.uint8)
+    raw[0] = np.arange(1024) % 256
+    raw[1] = np.arange(1024) % 3
+    raw[2] = np.arange(1024) % 5
+    with pytest.raises(F.FpgmError, match="256 states"):
+        eng.upload(raw)
+    raw[0] = np.arange(1024) % 255
+    card = eng.upload(raw)
+    assert list(card) == [255, 3, 5]
+
+
+@pytest.mark.parametrize("card,d", [((2, 5), 5), ((6, 9), 3), ((6, 9), 4)])
+def test_compact_tier_across_dataset_sizes(eng, card, d):
+    """Compact-tier tests after datasets of other sample counts: the per-CTA slots are laid
+    out once for the largest dataset seen and reused; their zeroed tables must stay zeroed.
+    Cards 2-5 at |Z| = 5 take the dense strata table (at most 32 cells per stratum), cards
+    6-9 the counting-sort path, at |Z| = 4 also through the global strata hash."""
+    for S in (20000, 6000, 30000, 6000):
+        raw, _, _ = F.generate(n_nodes=10, n_samples=S, seed=S + d, n_edges=12, max_indegree=3, card=card)
+        cols, cd = O.relabel(raw)
+        eng.upload(raw)
+        rng = np.random.default_rng(S * 7 + d)
+        tests = random_tests(rng, 10, d, 16)
+        got = eng.ci_test_batch(tests, d, want_hash=True)
+        exp = O.ci_tests(cols, cd, tests, d, threads=8)
+        for g, o in zip(got, exp):
+            check(g, o, exact_p=g.rechecked == 1)

@@ -1,6 +1,7 @@
 """Host-side checks that need no GPU: the C-ABI library loads and exports every
 declared symbol, the host orientation reproduces the reference's CPDAG files,
 the command line and the Python binding parse like the reference's."""
+import ctypes
 import os
 import re
 import subprocess
@@ -32,6 +33,29 @@ def test_library_exports_every_declared_symbol():
     out = subprocess.run(["nm", "-D", "--defined-only", F.LIB_PATH], capture_output=True, text=True).stdout
     exported = set(re.findall(r" T (fpgm_\w+)", out))
     assert names <= exported, names - exported
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    """The Python binding's structures have the C header's sizes and field offsets."""
+    checks = {"fpgm_pc_stats": (F.PCStats, ["count_ms", "large_ms", "span_ms", "total_ms", "large_bytes"]),
+              "fpgm_ci_result": (F.CIResult, ["df", "g2", "p_value", "path"]),
+              "fpgm_gen_spec": (F.GenSpec, ["n_samples", "seed"])}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "fastpgm_gb300.h"', "int main(void) {"]
+    for c, (_, fields) in checks.items():
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (c, c))
+        for f in fields:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (c, f, c, f))
+    lines.append("return 0; }")
+    src = tmp_path / "sizes.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True, check=True)
+               .stdout.splitlines())
+    for c, (cls, fields) in checks.items():
+        assert int(got[c]) == ctypes.sizeof(cls), c
+        for f in fields:
+            assert int(got["%s.%s" % (c, f)]) == getattr(cls, f).offset, (c, f)
 
 
 def _orient_struct(tmp_path, names, adj, seps):
