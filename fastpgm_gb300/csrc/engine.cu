@@ -126,6 +126,7 @@ struct fpgm_engine {
     double band_alpha = -1.0;
     int n_slots = 0, hash_cap_global = 0;
     int64_t slot_bytes = 0, slot_S = 0;  // slot_S: the sample count the slots' layout was made for
+    bool wave_log = false;               // FPGM_WAVE_LOG: one stderr line per wave (tier sizes, kernel times)
     // result
     bool has_result = false;
     std::vector<uint8_t> res_adj;
@@ -418,6 +419,7 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     CK(cudaMemcpy(e->btab.p, bt.data(), bt.size() * 8, cudaMemcpyHostToDevice));
     RET(e->counters.ensure(64));
     RET(e->stats.ensure(ST_COUNT * 8));
+    e->wave_log = getenv("FPGM_WAVE_LOG") != nullptr;
     if (getenv("FPGM_PHASE_TIMERS")) {
         RET(e->phase_timers.ensure(16 * 8));
         CK(cudaMemset(e->phase_timers.p, 0, 16 * 8));
@@ -666,6 +668,13 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
         st->count_bytes += (double)(tiers[C_TIER0] + tiers[C_TIER1]) * (2.0 + d) * (double)e->S;
         st->large_bytes += (double)tiers[C_TIER2] * (2.0 + d) * (double)e->S;
         st->count_launches += 1;
+        if (e->wave_log)
+            fprintf(stderr,
+                    "wave level=%d tests=%d tier0=%d tier1=%d tier2=%d compact_launched=%d count_ms=%.4f "
+                    "compact_ms=%.4f count_bytes=%.0f compact_bytes=%.0f\n",
+                    d, T, tiers[C_TIER0], tiers[C_TIER1], tiers[C_TIER2], a.slot_mem != nullptr, ms, ms2,
+                    (double)(tiers[C_TIER0] + tiers[C_TIER1]) * (2.0 + d) * (double)e->S,
+                    (double)tiers[C_TIER2] * (2.0 + d) * (double)e->S);
         if (hs[ST_UNSUPPORTED])
             return set_error(FPGM_ERR_UNSUPPORTED,
                              "level %d: %llu CI test(s) are outside the engine's limits (joint table beyond 2^62 "
