@@ -658,8 +658,7 @@ __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const ui
 
 // Dense strata x cells table T[k * dxy + x * dy + y] (k = stratum id), at most 32 cells per
 // stratum: lane groups of G = 2^ceil(log2 dxy) lanes, one stratum per group and one cell per
-// lane, the margins by shuffles within the group.  The next strata's cells are loaded while
-// the current ones are scored.
+// lane, the margins by shuffles within the group, four strata sets per iteration.
 template <bool kFp64>
 __device__ inline Partial score_dense_groups(const int *T, int n_obs, int dx, int dy, const uint64_t *gzk,
                                              bool want_hash) {
@@ -674,23 +673,44 @@ __device__ inline Partial score_dense_groups(const int *T, int n_obs, int dx, in
     const bool cell = gl < dxy;
     Partial acc{0, 0.0, 0.0, 0.0, 0ull};
     TermAcc<kFp64> ta;
+    // four strata sets per iteration: their loads and shuffle chains are independent
+    constexpr int U = 4;
     const int step = kWarps * gpw;
-    int k = warp * gpw + gi;
-    int On = (cell && k < n_obs) ? __ldcg(T + (int64_t)k * dxy + gl) : 0;
-    for (int k0 = warp * gpw; k0 < n_obs; k0 += step, k += step) {
-        const int O = On;
-        On = (cell && k + step < n_obs) ? __ldcg(T + (int64_t)(k + step) * dxy + gl) : 0;
-        int Nx = 0, Ny = 0, m = O;
-        for (int j = 0; j < dy; ++j) Nx += __shfl_sync(full, O, x * dy + j, G);
-        for (int i = 0; i < dx; ++i) Ny += __shfl_sync(full, O, i * dy + y, G);
-        for (int o = G >> 1; o > 0; o >>= 1) m += __shfl_xor_sync(full, m, o, G);
-        const bool valid = cell && k < n_obs;
-        const int r = __popc(__ballot_sync(full, valid && y == 0 && Nx > 0) & gmask);
-        const int c = __popc(__ballot_sync(full, valid && x == 0 && Ny > 0) & gmask);
-        if (valid && gl == 0) acc.df += (long long)(max(r, 1) - 1) * (max(c, 1) - 1);
-        if (valid && O > 0) {
-            ta.add(O, Nx, Ny, m);
-            if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x) * (uint64_t)dy + y, (uint32_t)O);
+    for (int k0 = warp * gpw; k0 < n_obs; k0 += U * step) {
+        int O[U], Nx[U], Ny[U], m[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int k = k0 + u * step + gi;
+            O[u] = (cell && k < n_obs) ? __ldcg(T + (int64_t)k * dxy + gl) : 0;
+            Nx[u] = 0;
+            Ny[u] = 0;
+        }
+        for (int j = 0; j < dy; ++j) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) Nx[u] += __shfl_sync(full, O[u], x * dy + j, G);
+        }
+        for (int i = 0; i < dx; ++i) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) Ny[u] += __shfl_sync(full, O[u], i * dy + y, G);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) m[u] = O[u];
+        for (int o = G >> 1; o > 0; o >>= 1) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) m[u] += __shfl_xor_sync(full, m[u], o, G);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int k = k0 + u * step + gi;
+            const bool valid = cell && k < n_obs;
+            const int r = __popc(__ballot_sync(full, valid && y == 0 && Nx[u] > 0) & gmask);
+            const int c = __popc(__ballot_sync(full, valid && x == 0 && Ny[u] > 0) & gmask);
+            if (valid && gl == 0) acc.df += (long long)(max(r, 1) - 1) * (max(c, 1) - 1);
+            if (valid && O[u] > 0) {
+                ta.add(O[u], Nx[u], Ny[u], m[u]);
+                if (want_hash)
+                    acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x) * (uint64_t)dy + y, (uint32_t)O[u]);
+            }
         }
     }
     ta.into(acc);
@@ -726,7 +746,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     int *swt = reinterpret_cast<int *>(smem_raw + kZTabOff);
     __shared__ const uint8_t *s_col[kMaxCols];
     __shared__ uint32_t s_dim[kMaxCols];
-    __shared__ int s_idx, s_over, s_distinct, s_flag;
+    __shared__ int s_idx, s_over, s_distinct, s_flag, s_seen;
     __shared__ int s_w[kWarps];
     __shared__ Partial scratch[kWarps];
     const int tid = threadIdx.x;
@@ -752,7 +772,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     do {                                                                \
         if (a.dbg && tid == 0) {                                        \
             const unsigned long long t_ = gtimer();                     \
-            if (i >= 0) atomicAdd(&a.dbg[i], t_ - t_prev);              \
+            if ((i) >= 0) atomicAdd(&a.dbg[(i)], t_ - t_prev);          \
             t_prev = t_;                                                \
         }                                                               \
     } while (0)
@@ -770,14 +790,27 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         }
         // 1. strata -> ids (shared hash, global if more than kZStrata strata)
         bool global = false;
-        for (int attempt = 0; attempt < 2; ++attempt) {
-            global = attempt == 1;
-            const uint32_t cap = global ? gcap : (uint32_t)kZCap;
+        // attempt 0: shared hash; 1: global hash sized from where the shared one overflowed
+        // (distinct strata grow slower than the samples, so the linear extrapolation bounds
+        // them); 2: global hash for every sample (only if 1 overflows)
+        int seen = 0;  // vectors hashed when the previous attempt overflowed
+        uint32_t cap = (uint32_t)kZCap;
+        for (int attempt = 0; attempt < 3; ++attempt) {
+            global = attempt >= 1;
+            if (attempt == 1) {
+                const double est = (double)kZStrata * (double)(nvec > 1 ? nvec : 1) / (double)(seen > 1 ? seen : 1);
+                cap = 16384u < gcap ? 16384u : gcap;
+                while ((double)cap < 2.0 * est && cap < gcap) cap <<= 1;
+            } else if (attempt == 2) {
+                if (cap == gcap) break;  // attempt 1 had the full size already
+                cap = gcap;
+            }
             uint64_t *keys = global ? gkeys : hkeys;
             for (uint32_t i = tid; i < cap; i += kThreads) keys[i] = kEmptyKey;
             if (tid == 0) {
                 s_over = 0;
                 s_distinct = 0;
+                s_seen = 0;
             }
             __syncthreads();
             const int limit = global ? (int)(cap / 2) : kZStrata;
@@ -809,6 +842,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
                 }
                 if (!ok) {
                     s_over = 1;
+                    s_seen = (int)v + 1;
                     break;
                 }
                 // one 64-byte run per thread, written after the inserts
@@ -831,7 +865,8 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
                 gsid[s] = h;
             }
             __syncthreads();
-            FPGM_PHASE(attempt);
+            FPGM_PHASE(attempt > 0 ? 1 : 0);
+            seen = s_seen > 0 ? s_seen : (int)nvec;
             if (!s_over) break;
             __syncthreads();
         }

@@ -191,3 +191,30 @@ def test_compact_tier_across_dataset_sizes(eng, card, d):
         exp = O.ci_tests(cols, cd, tests, d, threads=8)
         for g, o in zip(got, exp):
             check(g, o, exact_p=g.rechecked == 1)
+
+
+@pytest.fixture(scope="module")
+def c4_data():
+    raw, _, _ = F.make_config("c4")
+    cols, cd = O.relabel(raw)
+    return raw, cols, cd
+
+
+@pytest.mark.parametrize("d", [5, 6, 7, 8])
+def test_compact_tier_at_c4_scale(eng, c4_data, d):
+    """1,041 nodes x 100,000 samples, cardinalities to 21: batches of 300 random tests keep
+    every CTA busy with thousands to tens of thousands of strata per test (shared hash,
+    global hash, dense table and counting-sort paths); a sample of them is checked bit for
+    bit against the oracle."""
+    raw, cols, cd = c4_data
+    eng.upload(raw)
+    n = raw.shape[0]
+    rng = np.random.default_rng(11 + d)
+    tests = random_tests(rng, n, d, 300)
+    got = eng.ci_test_batch(tests, d, want_hash=True)
+    idx = [i for i, g in enumerate(got) if g.path == 2][:10]
+    assert len(idx) == 10
+    exp = O.ci_tests(cols, cd, tests[idx], d, threads=8)
+    for i, o in zip(idx, exp):
+        check(got[i], o, exact_p=got[i].rechecked == 1)
+    assert all(np.isfinite(g.g2) and np.isfinite(g.p_value) for g in got)
