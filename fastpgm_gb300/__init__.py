@@ -20,6 +20,7 @@ FPGM_MODE_PLAIN = 1
 MAX_COND = 30
 
 EXPORTED = ["fpgm_last_error", "fpgm_engine_create", "fpgm_engine_destroy", "fpgm_dataset_upload",
+            "fpgm_dataset_upload_jobs",
             "fpgm_dataset_download", "fpgm_ci_test", "fpgm_ci_test_batch", "fpgm_pc_skeleton",
             "fpgm_pc_result_sizes", "fpgm_pc_result_fetch", "fpgm_orient_cpdag", "fpgm_write_struct",
             "fpgm_bnsl_pcstable", "fpgm_generate_network", "fpgm_write_csv", "fpgm_ci_test_noalloc"]
@@ -86,6 +87,8 @@ def load():
     L.fpgm_engine_create.argtypes = [ctypes.c_int32, ctypes.POINTER(vp)]
     L.fpgm_engine_destroy.argtypes = [vp]
     L.fpgm_dataset_upload.argtypes = [vp, u8p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, u8p]
+    L.fpgm_dataset_upload_jobs.argtypes = [vp, ctypes.c_int32, i32p, ctypes.POINTER(ctypes.c_int64),
+                                           ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, u8p]
     L.fpgm_dataset_download.argtypes = [vp, u8p]
     L.fpgm_ci_test.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, i32p, ctypes.c_int32, ctypes.c_double,
                                ctypes.c_int32, ctypes.POINTER(CIResult)]
@@ -157,6 +160,21 @@ class Engine:
         _check(load().fpgm_dataset_upload(self._h, _u8(columns), n, S, 1 if relabel else 0, _u8(card)))
         self.n, self.S = n, S
         return card
+
+    def upload_jobs(self, datasets, relabel=True):
+        """Several independent datasets (uint8 [n_vars_j, n_samples_j] each) in one engine; the
+        variables are numbered in dataset order.  Returns the per-dataset cardinalities."""
+        datasets = [np.ascontiguousarray(c, dtype=np.uint8) for c in datasets]
+        nv = np.array([c.shape[0] for c in datasets], dtype=np.int32)
+        ns = np.array([c.shape[1] for c in datasets], dtype=np.int64)
+        ptrs = (ctypes.c_void_p * len(datasets))(*[c.ctypes.data for c in datasets])
+        card = np.zeros(int(nv.sum()), dtype=np.uint8)
+        _check(load().fpgm_dataset_upload_jobs(self._h, len(datasets), _i32(nv),
+                                               ns.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), ptrs,
+                                               1 if relabel else 0, _u8(card)))
+        self.n, self.S = int(nv.sum()), int(ns.max())
+        self.job_offsets = np.concatenate([[0], np.cumsum(nv)]).astype(np.int64)
+        return [card[self.job_offsets[j]:self.job_offsets[j + 1]] for j in range(len(datasets))]
 
     def download(self):
         out = np.empty((self.n, self.S), dtype=np.uint8)
@@ -250,4 +268,4 @@ def bnsl_pcstable(verbose, n_threads, group_size, alpha, ref_net, train_set, sav
                                      int(bool(save_struct))))
 
 
-from .configs import CONFIGS, make_config  # noqa: E402
+from .configs import CONFIGS, c5_jobs, make_config, make_jobs, split_jobs  # noqa: E402

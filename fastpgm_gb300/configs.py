@@ -38,6 +38,32 @@ def c5_jobs(seed=5, n_jobs=64):
     return jobs
 
 
+def make_jobs(jobs):
+    """Generate the datasets of a list of job parameter dicts (c5_jobs()).  Returns
+    (list of raw uint8 [n_j, S_j], depth)."""
+    from . import generate
+    out, depth = [], 1000
+    for spec in jobs:
+        spec = dict(spec)
+        depth = spec.pop("depth")
+        cols, card, par = generate(**spec)
+        out.append(cols)
+    return out, depth
+
+
+def split_jobs(result, offsets):
+    """Per-dataset views of a multi-dataset skeleton result (Engine.result() with the
+    engine's job_offsets): [(adj [n_j, n_j], sepsets {(a, b): z} in local numbering)]."""
+    out = []
+    for j in range(len(offsets) - 1):
+        lo, hi = int(offsets[j]), int(offsets[j + 1])
+        adj = result["adj"][lo:hi, lo:hi]
+        seps = {(a - lo, b - lo): tuple(v - lo for v in z) for (a, b), z in result["sepsets"].items()
+                if lo <= a < hi}
+        out.append((adj, seps))
+    return out
+
+
 def make_config(name, n_samples=None, n_nodes=None):
     """Generate a config's data.  Returns (columns raw uint8 [n,S], depth, spec dict)."""
     from . import generate

@@ -25,13 +25,14 @@ namespace fpgm {
 enum { C_TIER0 = 0, C_TIER1, C_TIER2, C_WORK0, C_WORK1, C_WORK2, C_COUNT };
 // stats[] slots (unsigned long long)
 enum { ST_RECHECK = 0, ST_NEARTIE, ST_LARGE, ST_MAXDP, ST_UNSUPPORTED, ST_DET, ST_EXEC, ST_UNRESOLVED,
-       ST_REMOVED, ST_MAXDEG, ST_TIER0, ST_TIER1, ST_TIER2, ST_COUNT };
+       ST_REMOVED, ST_MAXDEG, ST_TIER0, ST_TIER1, ST_TIER2, ST_BYTES_SHARED, ST_BYTES_LARGE, ST_COUNT };
 
 enum { SRC_WAVE = 0, SRC_EXPLICIT = 1 };
 
 struct WaveArgs {
     const uint8_t *cols;
-    int64_t S, S_pad;
+    const int64_t *var_off;  // byte offset of each variable's column in cols
+    const int32_t *var_S;    // samples of each variable's dataset (all variables of a test share it)
     const uint8_t *card;
     int d;
     // wave source
@@ -80,6 +81,7 @@ template <int kSource>
 __global__ void classify_kernel(WaveArgs a) {
     const int T = kSource == SRC_EXPLICIT ? a.n_tests : a.off[a.n_edges];
     const int d = a.d, ncols = d + 2;
+    unsigned long long bytes_shared = 0, bytes_large = 0;  // algorithmic column bytes per tier group
     for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < T; item += gridDim.x * blockDim.x) {
         int x, y, z[kMaxCond];
         if (kSource == SRC_EXPLICIT) {
@@ -135,6 +137,17 @@ __global__ void classify_kernel(WaveArgs a) {
         }
         const int slot = atomicAdd(&a.counters[C_TIER0 + tier], 1);
         a.lists[tier * a.list_cap + slot] = item;
+        const unsigned long long b = (unsigned long long)(2 + d) * (unsigned long long)a.var_S[x];
+        if (tier < 2) bytes_shared += b; else bytes_large += b;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        bytes_shared += __shfl_xor_sync(0xffffffffu, bytes_shared, o);
+        bytes_large += __shfl_xor_sync(0xffffffffu, bytes_large, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (bytes_shared) atomicAdd(&a.stats[ST_BYTES_SHARED], bytes_shared);
+        if (bytes_large) atomicAdd(&a.stats[ST_BYTES_LARGE], bytes_large);
     }
 }
 
@@ -194,7 +207,6 @@ __global__ void __launch_bounds__(kThreads, 2) ci_warp_kernel(WaveArgs a) {
     int *wreg = smem + warp * kWarpInts;
     const int n0 = a.counters[C_TIER0];
     const int d = a.d, ncols = d + 2;
-    const int64_t nvec = a.S >> 4;
     const WarpGroup g{lane};
     for (;;) {
         int idx = 0;
@@ -202,11 +214,13 @@ __global__ void __launch_bounds__(kThreads, 2) ci_warp_kernel(WaveArgs a) {
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= n0) break;
         const int item = a.lists[idx];
+        const int64_t S = a.var_S[a.item_vars[(int64_t)item * ncols + d]];
+        const int64_t nvec = S >> 4;
         uint32_t dim = 1;
         if (lane < ncols) {
             const int var = a.item_vars[(int64_t)item * ncols + lane];
             dim = a.card[var];
-            s_col[warp][lane] = a.cols + (int64_t)var * a.S_pad;
+            s_col[warp][lane] = a.cols + a.var_off[var];
             s_dim[warp][lane] = dim;
         }
         uint32_t cells = dim;
@@ -242,7 +256,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_warp_kernel(WaveArgs a) {
                 }
             }
         }
-        for (int64_t s = (a.S & ~(int64_t)15) + lane; s < a.S; s += 32) {
+        for (int64_t s = (S & ~(int64_t)15) + lane; s < S; s += 32) {
             uint32_t c = 0;
             for (int j = 0; j < ncols; ++j) c = c * s_dim[warp][j] + s_col[warp][j][s];
             atomicAdd(&mytab[c], 1);
@@ -273,7 +287,6 @@ __global__ void __launch_bounds__(kThreads, 2) ci_cta_kernel(WaveArgs a) {
     const int tid = threadIdx.x, lane = tid & 31;
     const int n1 = a.counters[C_TIER1];
     const int d = a.d, ncols = d + 2;
-    const int64_t nvec = a.S >> 4;
     const CtaGroup g{tid};
     for (;;) {
         if (tid == 0) s_idx = atomicAdd(&a.counters[C_WORK1], 1);
@@ -281,10 +294,12 @@ __global__ void __launch_bounds__(kThreads, 2) ci_cta_kernel(WaveArgs a) {
         const int idx = s_idx;
         if (idx >= n1) break;
         const int item = a.lists[a.list_cap + idx];
+        const int64_t S = a.var_S[a.item_vars[(int64_t)item * ncols + d]];
+        const int64_t nvec = S >> 4;
         if (tid < ncols) {
             const int var = a.item_vars[(int64_t)item * ncols + tid];
             s_dim[tid] = a.card[var];
-            s_col[tid] = a.cols + (int64_t)var * a.S_pad;
+            s_col[tid] = a.cols + a.var_off[var];
         }
         __syncthreads();
         int cells = 1;
@@ -318,7 +333,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_cta_kernel(WaveArgs a) {
                 }
             }
         }
-        for (int64_t s = (a.S & ~(int64_t)15) + tid; s < a.S; s += kThreads) {
+        for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
             uint32_t c = 0;
             for (int j = 0; j < ncols; ++j) c = c * s_dim[j] + s_col[j][s];
             atomicAdd(&mytab[c], 1);
@@ -750,7 +765,6 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     __shared__ int s_w[kWarps];
     __shared__ Partial scratch[kWarps];
     const int tid = threadIdx.x;
-    const int64_t S = a.S;
     const uint32_t gcap = (uint32_t)a.hash_cap_global;
     char *slot = a.slot_mem + (int64_t)blockIdx.x * a.slot_bytes;
     const SlotLayout L = slot_layout(a.slot_S, gcap);
@@ -765,7 +779,6 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     int *gtab = reinterpret_cast<int *>(slot + L.tab);
     const int n2 = a.counters[C_TIER2];
     const int d = a.d, ncols = d + 2;
-    const int64_t nvec = S >> 4;
     uint64_t *zk = a.want_hash ? gzk : nullptr;
     unsigned long long t_prev = 0;
 #define FPGM_PHASE(i)                                                   \
@@ -783,10 +796,12 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         if (idx >= n2) break;
         FPGM_PHASE(-1);
         const int item = a.lists[2 * a.list_cap + idx];
+        const int64_t S = a.var_S[a.item_vars[(int64_t)item * ncols + d]];  // <= the slots' layout size
+        const int64_t nvec = S >> 4;
         if (tid < ncols) {
             const int var = a.item_vars[(int64_t)item * ncols + tid];
             s_dim[tid] = a.card[var];
-            s_col[tid] = a.cols + (int64_t)var * a.S_pad;
+            s_col[tid] = a.cols + a.var_off[var];
         }
         // 1. strata -> ids (shared hash, global if more than kZStrata strata)
         bool global = false;
@@ -1067,10 +1082,11 @@ __global__ void band_table_kernel(double alpha, double *lo, double *hi, int dfma
 // ---------------------------------------------------------------- plain: one test, whole grid, one launch
 struct PlainArgs {
     const uint8_t *cols;
-    int64_t S, S_pad;
+    int64_t S;                  // samples of the test's dataset
     const uint8_t *card;
     int32_t ncols;
-    int32_t vars[kMaxCols];  // Horner order: z..., x, y
+    int32_t vars[kMaxCols];     // Horner order: z..., x, y
+    int64_t col_off[kMaxCols];  // byte offset of each of those columns in cols
     double alpha;
     BandTables bt;
     int32_t want_hash;
@@ -1090,7 +1106,7 @@ __global__ void __launch_bounds__(kThreads) ci_plain_kernel(PlainArgs p) {
     const int ncols = p.ncols, d = ncols - 2;
     if (tid < ncols) {
         s_dim[tid] = p.card[p.vars[tid]];
-        s_col[tid] = p.cols + (int64_t)p.vars[tid] * p.S_pad;
+        s_col[tid] = p.cols + p.col_off[tid];
     }
     __syncthreads();
     int64_t cells = 1;

@@ -115,9 +115,13 @@ struct fpgm_engine {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     // data
     int n = 0;
-    int64_t S = 0, S_pad = 0;
-    DevBuf cols, card;
+    int64_t S = 0, S_pad = 0;  // one dataset: its samples and column pitch; several: the largest
+    int n_jobs = 1;            // independent datasets sharing the engine (variables in job order)
+    int64_t E = 0;             // level-0 pairs: within each dataset
+    DevBuf cols, card, var_off, var_S, var_lo, var_hi;
     std::vector<uint8_t> h_card;
+    std::vector<int64_t> h_var_off;         // byte offset of each variable's column
+    std::vector<int32_t> h_var_S, h_var_lo, h_var_hi;  // its dataset's samples and variable range
     DevBuf btab;
     // level workspace
     DevBuf bits, deg, adjl, edges_x, edges_y, pxy, pyx, cntx, total, next, status, seprank, g, off, flag,
@@ -138,11 +142,13 @@ namespace {
 
 // ---- data preparation
 // First-appearance ids per column (Dataset.cpp:459-467) and observed cardinality.
-__global__ void relabel_kernel(uint8_t *cols, int64_t S, int64_t S_pad, uint8_t *card, int relabel) {
+__global__ void relabel_kernel(uint8_t *cols, const int64_t *var_off, const int32_t *var_S, uint8_t *card,
+                               int relabel) {
     __shared__ unsigned first[256];
     __shared__ uint8_t map[256];
     __shared__ unsigned s_max;
-    uint8_t *c = cols + (int64_t)blockIdx.x * S_pad;
+    uint8_t *c = cols + var_off[blockIdx.x];
+    const int64_t S = var_S[blockIdx.x];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) first[i] = 0xffffffffu;
     if (threadIdx.x == 0) s_max = 0;
     __syncthreads();
@@ -178,15 +184,41 @@ __global__ void relabel_kernel(uint8_t *cols, int64_t S, int64_t S_pad, uint8_t 
 }
 
 // ---- level machinery
-__global__ void init_bits_kernel(uint32_t *bits, int n, int W) {
+// complete graph within each dataset: v is adjacent to [var_lo[v], var_hi[v]) minus itself
+__global__ void init_bits_kernel(uint32_t *bits, int n, int W, const int32_t *var_lo, const int32_t *var_hi) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= (int64_t)n * W) return;
     int v = (int)(i / W), w = (int)(i % W);
-    uint32_t m = 0xffffffffu;
-    int lo = w * 32;
-    if (lo + 32 > n) m = (n - lo) >= 32 ? 0xffffffffu : ((1u << (n - lo)) - 1u);
+    const int lo = w * 32, a = max(var_lo[v], lo), b = min(var_hi[v], lo + 32);
+    uint32_t m = 0u;
+    if (b > a) m = (b - a >= 32 ? 0xffffffffu : ((1u << (b - a)) - 1u)) << (a - lo);
     if (v >= lo && v < lo + 32) m &= ~(1u << (v - lo));
     bits[i] = m;
+}
+
+// level-0 pairs of several datasets: v with each higher neighbour of the initial bitset, in
+// (v, u) order like the complete graph's (Network.cpp:270-283), one test each
+__global__ void level0_csr_edges_kernel(int n, const int32_t *adjl, int stride, const int32_t *deg,
+                                        const int32_t *node_off, int32_t *ex, int32_t *ey, int32_t *pxy,
+                                        int32_t *pyx, uint64_t *cntx, uint64_t *total, uint64_t *next,
+                                        uint8_t *status) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const int32_t *L = adjl + (int64_t)v * stride;
+    int64_t e = node_off[v];
+    for (int k = 0; k < deg[v]; ++k) {
+        const int u = L[k];
+        if (u <= v) continue;
+        ex[e] = v;
+        ey[e] = u;
+        pxy[e] = 0;
+        pyx[e] = 0;
+        cntx[e] = 1;
+        total[e] = 1;
+        next[e] = 0;
+        status[e] = kStatusActive;
+        ++e;
+    }
 }
 
 // all pairs i<j in complete-graph order (Network.cpp:270-283)
@@ -446,6 +478,77 @@ extern "C" int fpgm_engine_destroy(fpgm_engine *e) {
     return FPGM_OK;
 }
 
+namespace {
+// Column layout of `jobs` datasets (variables in job order): offsets, samples, variable
+// ranges on the host and the device, then the relabelling and the cardinality check.
+// job_vars[j] variables of job_samples[j] samples each, column-major in cols[j].
+int load_datasets(fpgm_engine *e, int32_t n_jobs, const int32_t *job_vars, const int64_t *job_samples,
+                  const uint8_t *const *cols, int32_t relabel, uint8_t *out_card, const char *fn) {
+    int64_t n = 0, bytes = 0, smax = 0, pairs = 0;
+    for (int32_t j = 0; j < n_jobs; ++j) {
+        if (!cols[j]) return set_error(FPGM_ERR_INVALID, "%s: NULL columns for dataset %d", fn, j);
+        if (job_vars[j] < 2 || job_samples[j] < 1 || job_samples[j] > ((int64_t)1 << 31) - 16)
+            return set_error(FPGM_ERR_INVALID, "%s: dataset %d has %d variables and %lld samples", fn, j, job_vars[j],
+                             (long long)job_samples[j]);
+        n += job_vars[j];
+        bytes += (int64_t)job_vars[j] * ((job_samples[j] + 63) & ~(int64_t)63);
+        smax = std::max<int64_t>(smax, job_samples[j]);
+        pairs += (int64_t)job_vars[j] * (job_vars[j] - 1) / 2;
+    }
+    if (n > 65535) return set_error(FPGM_ERR_INVALID, "%s: %lld variables in all (at most 65535)", fn, (long long)n);
+    CK(cudaSetDevice(e->device));
+    e->n = 0;
+    e->has_result = false;
+    e->n_jobs = n_jobs;
+    e->S = smax;
+    e->S_pad = (smax + 63) & ~(int64_t)63;
+    e->E = pairs;
+    e->h_var_off.resize(n);
+    e->h_var_S.resize(n);
+    e->h_var_lo.resize(n);
+    e->h_var_hi.resize(n);
+    RET(e->cols.ensure((size_t)bytes + 64));
+    RET(e->card.ensure(std::max<size_t>(256, (size_t)n)));
+    CK(cudaMemsetAsync(e->cols.p, 0, (size_t)bytes, e->stream));
+    int64_t off = 0;
+    int32_t v0 = 0;
+    for (int32_t j = 0; j < n_jobs; ++j) {
+        const int64_t Sj = job_samples[j], pitch = (Sj + 63) & ~(int64_t)63;
+        CK(cudaMemcpy2DAsync(e->cols.as<uint8_t>() + off, (size_t)pitch, cols[j], (size_t)Sj, (size_t)Sj,
+                             (size_t)job_vars[j], cudaMemcpyHostToDevice, e->stream));
+        for (int32_t k = 0; k < job_vars[j]; ++k) {
+            e->h_var_off[v0 + k] = off + k * pitch;
+            e->h_var_S[v0 + k] = (int32_t)Sj;
+            e->h_var_lo[v0 + k] = v0;
+            e->h_var_hi[v0 + k] = v0 + job_vars[j];
+        }
+        off += job_vars[j] * pitch;
+        v0 += job_vars[j];
+    }
+    RET(e->var_off.ensure((size_t)n * 8));
+    RET(e->var_S.ensure((size_t)n * 4));
+    RET(e->var_lo.ensure((size_t)n * 4));
+    RET(e->var_hi.ensure((size_t)n * 4));
+    CK(cudaMemcpyAsync(e->var_off.p, e->h_var_off.data(), (size_t)n * 8, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync(e->var_S.p, e->h_var_S.data(), (size_t)n * 4, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync(e->var_lo.p, e->h_var_lo.data(), (size_t)n * 4, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync(e->var_hi.p, e->h_var_hi.data(), (size_t)n * 4, cudaMemcpyHostToDevice, e->stream));
+    relabel_kernel<<<(int)n, 256, 0, e->stream>>>(e->cols.as<uint8_t>(), e->var_off.as<int64_t>(),
+                                                  e->var_S.as<int32_t>(), e->card.as<uint8_t>(), relabel);
+    CK(cudaGetLastError());
+    e->h_card.resize(n);
+    CK(cudaMemcpyAsync(e->h_card.data(), e->card.p, n, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    for (int64_t v = 0; v < n; ++v)
+        if (e->h_card[v] == 0)  // 256 states wrap the uint8 cardinality to 0
+            return set_error(FPGM_ERR_UNSUPPORTED, "%s: column %lld has 256 states; at most 255 are supported", fn,
+                             (long long)v);
+    e->n = (int)n;
+    if (out_card) memcpy(out_card, e->h_card.data(), n);
+    return FPGM_OK;
+}
+}  // namespace
+
 extern "C" int fpgm_dataset_upload(fpgm_engine *e, const uint8_t *columns, int32_t n_vars, int64_t n_samples,
                                    int32_t relabel, uint8_t *out_card) {
     if (!e || !columns) return set_error(FPGM_ERR_INVALID, "fpgm_dataset_upload: NULL argument");
@@ -454,35 +557,23 @@ extern "C" int fpgm_dataset_upload(fpgm_engine *e, const uint8_t *columns, int32
     if (n_samples < 1 || n_samples > ((int64_t)1 << 31) - 16)
         return set_error(FPGM_ERR_INVALID, "fpgm_dataset_upload: n_samples %lld outside [1, 2^31-16]",
                          (long long)n_samples);
-    CK(cudaSetDevice(e->device));
-    e->n = n_vars;
-    e->S = n_samples;
-    e->S_pad = (n_samples + 63) & ~(int64_t)63;
-    e->has_result = false;
-    RET(e->cols.ensure((size_t)e->n * e->S_pad));
-    RET(e->card.ensure(std::max<size_t>(256, (size_t)n_vars)));
-    CK(cudaMemsetAsync(e->cols.p, 0, (size_t)e->n * e->S_pad, e->stream));
-    CK(cudaMemcpy2DAsync(e->cols.p, (size_t)e->S_pad, columns, (size_t)n_samples, (size_t)n_samples, (size_t)n_vars,
-                         cudaMemcpyHostToDevice, e->stream));
-    relabel_kernel<<<n_vars, 256, 0, e->stream>>>(e->cols.as<uint8_t>(), e->S, e->S_pad, e->card.as<uint8_t>(),
-                                                  relabel);
-    CK(cudaGetLastError());
-    e->h_card.resize(n_vars);
-    CK(cudaMemcpyAsync(e->h_card.data(), e->card.p, n_vars, cudaMemcpyDeviceToHost, e->stream));
-    CK(cudaStreamSynchronize(e->stream));
-    for (int32_t v = 0; v < n_vars; ++v)
-        if (e->h_card[v] == 0) {  // 256 states wrap the uint8 cardinality to 0
-            e->n = 0;
-            return set_error(FPGM_ERR_UNSUPPORTED,
-                             "fpgm_dataset_upload: column %d has 256 states; at most 255 are supported", v);
-        }
-    if (out_card) memcpy(out_card, e->h_card.data(), n_vars);
-    return FPGM_OK;
+    return load_datasets(e, 1, &n_vars, &n_samples, &columns, relabel, out_card, "fpgm_dataset_upload");
+}
+
+extern "C" int fpgm_dataset_upload_jobs(fpgm_engine *e, int32_t n_jobs, const int32_t *job_vars,
+                                        const int64_t *job_samples, const uint8_t *const *job_columns,
+                                        int32_t relabel, uint8_t *out_card) {
+    if (!e || !job_vars || !job_samples || !job_columns || n_jobs < 1)
+        return set_error(FPGM_ERR_INVALID, "fpgm_dataset_upload_jobs: NULL argument or no dataset");
+    return load_datasets(e, n_jobs, job_vars, job_samples, job_columns, relabel, out_card,
+                         "fpgm_dataset_upload_jobs");
 }
 
 extern "C" int fpgm_dataset_download(fpgm_engine *e, uint8_t *columns) {
     if (!e || !columns) return set_error(FPGM_ERR_INVALID, "fpgm_dataset_download: NULL argument");
     if (!e->n) return set_error(FPGM_ERR_STATE, "fpgm_dataset_download: no dataset uploaded");
+    if (e->n_jobs != 1)
+        return set_error(FPGM_ERR_UNSUPPORTED, "fpgm_dataset_download: the engine holds %d datasets", e->n_jobs);
     CK(cudaSetDevice(e->device));
     CK(cudaMemcpy2DAsync(columns, (size_t)e->S, e->cols.p, (size_t)e->S_pad, (size_t)e->S, (size_t)e->n,
                          cudaMemcpyDeviceToHost, e->stream));
@@ -539,8 +630,8 @@ int ensure_slots(fpgm_engine *e) {
 int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t items) {
     memset(&a, 0, sizeof a);
     a.cols = e->cols.as<uint8_t>();
-    a.S = e->S;
-    a.S_pad = e->S_pad;
+    a.var_off = e->var_off.as<int64_t>();
+    a.var_S = e->var_S.as<int32_t>();
     a.card = e->card.as<uint8_t>();
     a.d = d;
     a.btab = e->btab.as<uint64_t>();
@@ -617,6 +708,7 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
         CK(cub::DeviceScan::ExclusiveSum(e->scan_tmp.p, sb, e->g.as<int32_t>(), e->off.as<int32_t>(),
                                          (int)(n_active + 1), e->stream));
         CK(cudaMemsetAsync(e->counters.p, 0, 64, e->stream));
+        CK(cudaMemsetAsync(dstat + ST_BYTES_SHARED, 0, 16, e->stream));  // this wave's bytes
         a.off = e->off.as<int32_t>();
         a.n_edges = (int32_t)n_active;
         CK(cudaEventRecord(e->ev0, e->stream));
@@ -664,17 +756,16 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
         CK(cudaEventElapsedTime(&ms2, e->ev1, e->ev2));
         st->count_ms += ms;
         st->large_ms += ms2;
-        // algorithmic bytes: (2 + d) columns of n_samples per test, split by kernel
-        st->count_bytes += (double)(tiers[C_TIER0] + tiers[C_TIER1]) * (2.0 + d) * (double)e->S;
-        st->large_bytes += (double)tiers[C_TIER2] * (2.0 + d) * (double)e->S;
+        // algorithmic bytes: (2 + d) columns of the test's samples per test, split by kernel
+        st->count_bytes += (double)hs[ST_BYTES_SHARED];
+        st->large_bytes += (double)hs[ST_BYTES_LARGE];
         st->count_launches += 1;
         if (e->wave_log)
             fprintf(stderr,
                     "wave level=%d tests=%d tier0=%d tier1=%d tier2=%d compact_launched=%d count_ms=%.4f "
                     "compact_ms=%.4f count_bytes=%.0f compact_bytes=%.0f\n",
                     d, T, tiers[C_TIER0], tiers[C_TIER1], tiers[C_TIER2], a.slot_mem != nullptr, ms, ms2,
-                    (double)(tiers[C_TIER0] + tiers[C_TIER1]) * (2.0 + d) * (double)e->S,
-                    (double)tiers[C_TIER2] * (2.0 + d) * (double)e->S);
+                    (double)hs[ST_BYTES_SHARED], (double)hs[ST_BYTES_LARGE]);
         if (hs[ST_UNSUPPORTED])
             return set_error(FPGM_ERR_UNSUPPORTED,
                              "level %d: %llu CI test(s) are outside the engine's limits (joint table beyond 2^62 "
@@ -690,11 +781,12 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
 int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
     const int n = e->n;
     const int W = (n + 31) / 32;
-    const int64_t E = (int64_t)n * (n - 1) / 2;
+    const int64_t E = e->E;  // level-0 pairs (within each dataset)
     unsigned long long *dstat = e->stats.as<unsigned long long>();
     CK(cudaMemsetAsync(dstat, 0, ST_COUNT * 8, e->stream));
     RET(e->bits.ensure((size_t)n * W * 4));
-    init_bits_kernel<<<blocks_for((int64_t)n * W, 256), 256, 0, e->stream>>>(e->bits.as<uint32_t>(), n, W);
+    init_bits_kernel<<<blocks_for((int64_t)n * W, 256), 256, 0, e->stream>>>(
+        e->bits.as<uint32_t>(), n, W, e->var_lo.as<int32_t>(), e->var_hi.as<int32_t>());
     CK(cudaGetLastError());
     st->kernel_launches += 1;
     RET(e->log_pair.ensure((size_t)E * 8 + 16));
@@ -704,7 +796,8 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
     RET(e->node_cnt.ensure((size_t)(n + 1) * 4));
     RET(e->node_off.ensure((size_t)(n + 1) * 4));
     int64_t log_count = 0, var_count = 0;
-    int max_deg = n - 1;
+    int max_deg = 0;  // largest dataset - 1
+    for (int v = 0; v < n; ++v) max_deg = std::max(max_deg, e->h_var_hi[v] - e->h_var_lo[v] - 1);
     bool more = true;
     st->n_levels = 0;
     for (int d = 0; d < depth && d < 64; ++d) {
@@ -715,9 +808,9 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
                              kMaxCond);
         int64_t n_active;
         int stride = 1;
-        if (d == 0) {
+        if (d == 0 && e->n_jobs == 1) {
             n_active = E;
-        } else {
+        } else {  // the level's snapshot (several datasets: also at level 0)
             stride = std::max(1, max_deg);
             RET(e->adjl.ensure((size_t)n * stride * 4));
             csr_kernel<<<blocks_for(n, 128), 128, 0, e->stream>>>(e->bits.as<uint32_t>(), n, W, e->adjl.as<int32_t>(),
@@ -751,10 +844,16 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
         RET(e->g.ensure(ne * 4));
         RET(e->off.ensure(ne * 4));
         if (n_active > 0) {
-            if (d == 0) {
+            if (d == 0 && e->n_jobs == 1) {
                 level0_edges_kernel<<<blocks_for(E, 256), 256, 0, e->stream>>>(
                     n, e->edges_x.as<int32_t>(), e->edges_y.as<int32_t>(), e->pxy.as<int32_t>(),
                     e->pyx.as<int32_t>(), e->cntx.as<uint64_t>(), e->total.as<uint64_t>(), e->next.as<uint64_t>(),
+                    e->status.as<uint8_t>());
+            } else if (d == 0) {
+                level0_csr_edges_kernel<<<blocks_for(n, 128), 128, 0, e->stream>>>(
+                    n, e->adjl.as<int32_t>(), stride, e->deg.as<int32_t>(), e->node_off.as<int32_t>(),
+                    e->edges_x.as<int32_t>(), e->edges_y.as<int32_t>(), e->pxy.as<int32_t>(), e->pyx.as<int32_t>(),
+                    e->cntx.as<uint64_t>(), e->total.as<uint64_t>(), e->next.as<uint64_t>(),
                     e->status.as<uint8_t>());
             } else {
                 level_edges_kernel<<<blocks_for(n, 128), 128, 0, e->stream>>>(
@@ -858,8 +957,8 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
 }
 
 // ------------------------------------------------------------------ plain path
-int plain_grid(const fpgm_engine *e) {
-    int64_t nvec = e->S >> 4;
+int plain_grid(const fpgm_engine *e, int64_t S) {
+    int64_t nvec = S >> 4;
     int64_t g = nvec / kThreads;
     return (int)std::max<int64_t>(1, std::min<int64_t>(g, e->ci_blocks));
 }
@@ -881,13 +980,13 @@ int plain_test(fpgm_engine *e, int x, int y, const int *z, int d, double alpha, 
         PlainArgs p;
         memset(&p, 0, sizeof p);
         p.cols = e->cols.as<uint8_t>();
-        p.S = e->S;
-        p.S_pad = e->S_pad;
+        p.S = e->h_var_S[x];
         p.card = e->card.as<uint8_t>();
         p.ncols = d + 2;
         for (int k = 0; k < d; ++k) p.vars[k] = z[k];
         p.vars[d] = x;
         p.vars[d + 1] = y;
+        for (int k = 0; k < d + 2; ++k) p.col_off[k] = e->h_var_off[p.vars[k]];
         p.alpha = alpha;
         p.bt.lo = e->band.as<double>();
         p.bt.hi = p.bt.lo + kBandDfMax + 1;
@@ -897,7 +996,7 @@ int plain_test(fpgm_engine *e, int x, int y, const int *z, int d, double alpha, 
         p.done = reinterpret_cast<int32_t *>(e->plain_ws.as<char>() + (size_t)kPlainInts * 4);
         p.out = e->detail_buf.as<fpgm_ci_result>();
         p.stats = e->stats.as<unsigned long long>();
-        ci_plain_kernel<<<plain_grid(e), kThreads, kSmemBytes, e->stream>>>(p);
+        ci_plain_kernel<<<plain_grid(e, p.S), kThreads, kSmemBytes, e->stream>>>(p);
         CK(cudaGetLastError());
     } else {
         WaveArgs a;
@@ -940,8 +1039,9 @@ int run_plain(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
     const int n = e->n;
     unsigned long long *dstat = e->stats.as<unsigned long long>();
     CK(cudaMemsetAsync(dstat, 0, ST_COUNT * 8, e->stream));
-    std::vector<uint8_t> adj((size_t)n * n, 1);
-    for (int i = 0; i < n; ++i) adj[(size_t)i * n + i] = 0;
+    std::vector<uint8_t> adj((size_t)n * n, 0);  // complete graph within each dataset
+    for (int i = 0; i < n; ++i)
+        for (int j = e->h_var_lo[i]; j < e->h_var_hi[i]; ++j) adj[(size_t)i * n + j] = i != j;
     struct Rem { int a, b; std::vector<int> z; };
     std::vector<Rem> rem;
     fpgm_ci_result r;
@@ -949,7 +1049,7 @@ int run_plain(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
     int64_t tests = 0;
     std::vector<std::pair<int, int>> kill;
     for (int i = 0; i < n; ++i)
-        for (int j = i + 1; j < n; ++j) {
+        for (int j = i + 1; j < e->h_var_hi[i]; ++j) {
             RET(plain_test(e, i, j, nullptr, 0, alpha, 0, &r, st));
             ++tests;
             if (r.independent) {
@@ -958,7 +1058,7 @@ int run_plain(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
             }
         }
     for (auto &k : kill) adj[(size_t)k.first * n + k.second] = adj[(size_t)k.second * n + k.first] = 0;
-    int64_t edges = (int64_t)n * (n - 1) / 2 - (int64_t)kill.size();
+    int64_t edges = e->E - (int64_t)kill.size();
     st->n_levels = 1;
     st->tests[0] = st->tests_executed[0] = tests;
     st->edges_after[0] = (int32_t)edges;
@@ -1047,6 +1147,11 @@ extern "C" int fpgm_ci_test(fpgm_engine *e, int32_t x, int32_t y, const int32_t 
     if (x < 0 || x >= e->n || y < 0 || y >= e->n) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test: variable out of range");
     for (int k = 0; k < nz; ++k)
         if (z[k] < 0 || z[k] >= e->n) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test: variable out of range");
+    for (int k = 0; k < nz; ++k)
+        if (e->h_var_lo[z[k]] != e->h_var_lo[x])
+            return set_error(FPGM_ERR_INVALID, "fpgm_ci_test: the variables belong to different datasets");
+    if (e->h_var_lo[y] != e->h_var_lo[x])
+        return set_error(FPGM_ERR_INVALID, "fpgm_ci_test: the variables belong to different datasets");
     CK(cudaSetDevice(e->device));
     return plain_test(e, x, y, z, nz, alpha, want_hash, out);
 }
@@ -1062,6 +1167,10 @@ extern "C" int fpgm_ci_test_batch(fpgm_engine *e, const int32_t *tests, int32_t 
     if (n_tests == 0) return FPGM_OK;
     for (int64_t i = 0; i < (int64_t)n_tests * (2 + d); ++i)
         if (tests[i] < 0 || tests[i] >= e->n) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_batch: variable out of range");
+    for (int64_t t = 0; t < n_tests; ++t)
+        for (int k = 1; k < 2 + d; ++k)
+            if (e->h_var_lo[tests[t * (2 + d) + k]] != e->h_var_lo[tests[t * (2 + d)]])
+                return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_batch: test %lld mixes datasets", (long long)t);
     CK(cudaSetDevice(e->device));
     RET(e->tests_buf.ensure((size_t)n_tests * (2 + d) * 4));
     RET(e->detail_buf.ensure((size_t)n_tests * sizeof(fpgm_ci_result)));
@@ -1259,7 +1368,7 @@ extern "C" int fpgm_ci_test_noalloc(const uint8_t *columns, int64_t pitch, int32
     CK(cudaMemsetAsync(scratch + kNoAllocStatsOff, 0, (size_t)ST_COUNT * 8, st));
     p.cols = columns;
     p.S = n_samples;
-    p.S_pad = pitch;
+    for (int k = 0; k < p.ncols; ++k) p.col_off[k] = (int64_t)p.vars[k] * pitch;
     p.card = card;
     p.alpha = alpha;
     p.bt.lo = nullptr;  // no band tables: every df > 0 is decided by the FP64 recheck path

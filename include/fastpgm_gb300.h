@@ -120,7 +120,17 @@ int fpgm_engine_destroy(fpgm_engine *eng);
  * out_card may be NULL. */
 int fpgm_dataset_upload(fpgm_engine *eng, const uint8_t *columns, int32_t n_vars, int64_t n_samples,
                         int32_t relabel, uint8_t *out_card);
-/* Copies the (relabelled) device columns back, n_vars*n_samples bytes. */
+/* Several independent datasets in one engine (no counterpart in the reference, which
+ * learns one dataset per call): dataset j has job_vars[j] variables of job_samples[j]
+ * samples, column-major at job_columns[j].  The engine numbers the variables in dataset
+ * order (dataset 0's first, then dataset 1's, ...); fpgm_pc_skeleton then learns every
+ * dataset's skeleton at once -- the complete graph within each dataset, never across --
+ * with every level's tests of all datasets in the same waves, and its results use that
+ * numbering.  CI tests must keep to one dataset.  out_card receives all variables'
+ * cardinalities.  At most 65,535 variables in all (16,384 for the batched skeleton). */
+int fpgm_dataset_upload_jobs(fpgm_engine *eng, int32_t n_jobs, const int32_t *job_vars, const int64_t *job_samples,
+                             const uint8_t *const *job_columns, int32_t relabel, uint8_t *out_card);
+/* Copies the (relabelled) device columns back, n_vars*n_samples bytes (one dataset only). */
 int fpgm_dataset_download(fpgm_engine *eng, uint8_t *columns);
 
 /* ---- single / batched CI tests (G^2) ----

@@ -110,3 +110,52 @@ def test_cli_and_python_binding_reproduce_alarm(alarm, tmp_path):
     out = subprocess.run([F.CLI_PATH, "-j", "0", "-m", "0", "-e", "1", "-f2", csv], capture_output=True, text=True)
     assert out.returncode == 0
     assert open(csv + "_struct").read() == golden
+
+
+def _small_jobs(n_jobs, seed, max_samples):
+    jobs = F.c5_jobs(seed=seed, n_jobs=n_jobs)
+    for j in jobs:  # the c5 generator with smaller datasets, so that the oracle stays quick
+        j["n_nodes"] = min(j["n_nodes"], 60)
+        j["n_samples"] = min(j["n_samples"], max_samples)
+    return jobs
+
+
+def test_several_datasets_match_each_oracle(eng):
+    """Several independent datasets learned in one skeleton call (every level's tests of all
+    datasets in the same waves) give each dataset's own skeleton, sepsets and test counts."""
+    data, depth = F.make_jobs(_small_jobs(6, seed=55, max_samples=20000))
+    eng.upload_jobs(data)
+    st = eng.pc_skeleton(depth=depth).to_dict()
+    res = eng.result()
+    per_job = F.split_jobs(res, eng.job_offsets)
+    levels = [0] * st["n_levels"]
+    for raw, (adj, seps) in zip(data, per_job):
+        cols, card = O.relabel(raw)
+        ref = O.pc_skeleton(cols, card, depth=depth, threads=16)
+        assert np.array_equal(adj, ref["adj"])
+        assert seps == ref["sepsets"]
+        assert ref["stats"]["n_levels"] <= st["n_levels"]
+        for lv, t in enumerate(ref["stats"]["tests"]):
+            levels[lv] += t
+    assert st["tests"] == levels
+
+
+def test_several_datasets_plain_matches_batched(eng):
+    data, depth = F.make_jobs(_small_jobs(3, seed=56, max_samples=3000))
+    eng.upload_jobs(data)
+    sb = eng.pc_skeleton(depth=depth).to_dict()
+    rb = eng.result()
+    sp = eng.pc_skeleton(depth=depth, mode=F.FPGM_MODE_PLAIN).to_dict()
+    rp = eng.result()
+    assert np.array_equal(rb["adj"], rp["adj"]) and rb["sepsets"] == rp["sepsets"]
+    assert sb["tests"] == sp["tests"]
+
+
+def test_tests_across_datasets_are_rejected(eng):
+    data, _ = F.make_jobs(_small_jobs(2, seed=57, max_samples=2000))
+    eng.upload_jobs(data)
+    n0 = data[0].shape[0]
+    with pytest.raises(F.FpgmError, match="different datasets"):
+        eng.ci_test(0, n0, ())
+    with pytest.raises(F.FpgmError, match="mixes datasets"):
+        eng.ci_test_batch(np.array([[0, 1, n0]], dtype=np.int32), 1)
