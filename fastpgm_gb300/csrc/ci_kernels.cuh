@@ -371,8 +371,11 @@ constexpr int kLaneStratum = 8;   // strata of up to this many samples: one lane
 constexpr int kRegStratum = 64;   // larger strata up to this size keep their codes in registers
 constexpr int kDenseMul = 8;      // dense strata x cells table when it has at most this many cells per sample
 
+// Fibonacci hashing: the top log2(cap) bits of z times 2^64/phi (cap a power of two).
+// The top bits mix every bit of the mixed-radix stratum code; the middle bits used before
+// left long probe runs (c4: 1.8x longer global-hash phase).
 __device__ __forceinline__ uint32_t zhash(uint64_t z, uint32_t cap) {
-    return (uint32_t)((z * 0x9E3779B97F4A7C15ull) >> 32) & (cap - 1);
+    return (uint32_t)((z * 0x9E3779B97F4A7C15ull) >> (64 - __popc(cap - 1)));
 }
 
 // Inserts stratum code z; a new code takes the next id from *counter, written to ids[slot]
