@@ -356,16 +356,19 @@ __global__ void __launch_bounds__(kThreads, 2) ci_cta_kernel(WaveArgs a) {
 
 // ---------------------------------------------------------------- tier 2: compact strata
 // Shared-memory plan of the compact kernel (kSmemBytes), phase by phase:
-//   phase 1  strata hash: keys u64[kZCap] at 0, 16-bit ids u16[kZCap] at kZIdsOff
+//   phase 1  strata hash: keys u64[kZCap64] or u32[kZCap32] at 0 (32-bit when every stratum
+//            code fits), 16-bit ids at kZIdsOff
 //   phase 2  per-stratum counts cnt[] at 0 and cursors cur[] at kZCurOff (over the dead keys)
 //   phase 3  per-warp x,y tables from kZTabOff (over the dead ids)
 // Up to kZStrata strata stay in shared memory; beyond that the same arrays live in the
 // CTA's global slot (hash sized >= 2 n_samples).
-constexpr int kZCap = 8192;
-constexpr int kZStrata = kZCap / 2;
-constexpr int kZIdsOff = kZCap * 8;
+constexpr int kZCap64 = 8192;    // shared hash slots with 64-bit stratum codes
+constexpr int kZCap32 = 16384;   // ... with 32-bit codes (same 64 KB)
+constexpr int kZStrata = kZCap32 / 2;  // most strata kept in shared memory (load <= 1/2)
+constexpr int kZIdsOff = kZCap64 * 8;
 constexpr int kZCurOff = ((kZStrata + 1) * 4 + 15) / 16 * 16;
 constexpr int kZTabOff = (kZCurOff + (kZStrata + 1) * 4 + 15) / 16 * 16;
+static_assert(kZIdsOff + kZCap32 * 2 <= kSmemBytes, "shared hash ids");
 constexpr int kSparseWarpTab = (kSmemBytes - kZTabOff) / 4 / kWarps;  // ints per warp
 constexpr int kLaneStratum = 8;   // strata of up to this many samples: one lane each
 constexpr int kRegStratum = 64;   // larger strata up to this size keep their codes in registers
@@ -381,21 +384,26 @@ __device__ __forceinline__ uint32_t zhash(uint64_t z, uint32_t cap) {
 // Inserts stratum code z; a new code takes the next id from *counter, written to ids[slot]
 // (16- or 32-bit ids) and, when gzk is given, its code to gzk[id].  Returns the slot, or -1
 // after max_probe probes or once more than id_limit strata exist.
-template <class Id>
-__device__ inline int zinsert(uint64_t *keys, Id *ids, uint32_t cap, uint64_t z, int *counter, int id_limit,
+__device__ __forceinline__ uint64_t key_cas(uint64_t *p, uint64_t e, uint64_t v) {
+    return atomicCAS(reinterpret_cast<unsigned long long *>(p), (unsigned long long)e, (unsigned long long)v);
+}
+__device__ __forceinline__ uint32_t key_cas(uint32_t *p, uint32_t e, uint32_t v) { return atomicCAS(p, e, v); }
+
+template <class K, class Id>
+__device__ inline int zinsert(K *keys, Id *ids, uint32_t cap, uint64_t zz, int *counter, int id_limit,
                               uint32_t max_probe, uint64_t *gzk) {
-    uint32_t h = zhash(z, cap);
+    const K z = (K)zz, empty = (K)kEmptyKey;
+    uint32_t h = zhash(zz, cap);
     for (uint32_t p = 0; p < max_probe; ++p) {
-        const uint64_t k = keys[h];
+        const K k = keys[h];
         if (k == z) return (int)h;
-        if (k == kEmptyKey) {
-            const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long *>(&keys[h]),
-                                                     (unsigned long long)kEmptyKey, (unsigned long long)z);
-            if (old == kEmptyKey) {
+        if (k == empty) {
+            const K old = key_cas(&keys[h], empty, z);
+            if (old == empty) {
                 const int id = atomicAdd(counter, 1);
                 if (id >= id_limit) return -1;
                 ids[h] = (Id)id;
-                if (gzk) gzk[id] = z;
+                if (gzk) gzk[id] = zz;
                 return (int)h;
             }
             if (old == z) return (int)h;
@@ -744,7 +752,7 @@ __device__ __forceinline__ unsigned long long gtimer() {
 
 // Tier 2: joint tables too large for shared memory, counted in O(samples):
 //  1. the observed Z strata are hashed, each new one taking the next id (shared-memory
-//     hash of kZCap slots; a global one sized >= 2 n_samples when more than kZStrata);
+//     hash of kZCap32 32-bit or kZCap64 64-bit codes; a global one beyond that);
 //  dense path (strata x dx x dy <= kDenseMul n_samples, dx dy <= 32): every sample adds
 //     one to T[id][x][y] in the CTA's global slot, and lane groups score the strata from
 //     T (score_dense_groups); the table is zeroed again after the decision;
@@ -812,11 +820,18 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         // (distinct strata grow slower than the samples, so the linear extrapolation bounds
         // them); 2: global hash for every sample (only if 1 overflows)
         int seen = 0;  // vectors hashed when the previous attempt overflowed
-        uint32_t cap = (uint32_t)kZCap;
+        __syncthreads();  // s_dim of this test
+        uint64_t dz = 1;
+        for (int j = 0; j < d; ++j) dz *= s_dim[j];  // < 2^62 (classified)
+        const bool code32 = dz <= 0xFFFFFFFFull;     // codes < dz fit 32 bits, below the empty key
+        const int zlimit = code32 ? kZStrata : kZCap64 / 2;
+        uint32_t cap = code32 ? (uint32_t)kZCap32 : (uint32_t)kZCap64;
+        uint32_t *hkeys32 = reinterpret_cast<uint32_t *>(hkeys);
         for (int attempt = 0; attempt < 3; ++attempt) {
             global = attempt >= 1;
+            const bool k32 = !global && code32;
             if (attempt == 1) {
-                const double est = (double)kZStrata * (double)(nvec > 1 ? nvec : 1) / (double)(seen > 1 ? seen : 1);
+                const double est = (double)zlimit * (double)(nvec > 1 ? nvec : 1) / (double)(seen > 1 ? seen : 1);
                 cap = 16384u < gcap ? 16384u : gcap;
                 while ((double)cap < 2.0 * est && cap < gcap) cap <<= 1;
             } else if (attempt == 2) {
@@ -824,14 +839,17 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
                 cap = gcap;
             }
             uint64_t *keys = global ? gkeys : hkeys;
-            for (uint32_t i = tid; i < cap; i += kThreads) keys[i] = kEmptyKey;
+            if (k32)
+                for (uint32_t i = tid; i < cap; i += kThreads) hkeys32[i] = (uint32_t)kEmptyKey;
+            else
+                for (uint32_t i = tid; i < cap; i += kThreads) keys[i] = kEmptyKey;
             if (tid == 0) {
                 s_over = 0;
                 s_distinct = 0;
                 s_seen = 0;
             }
             __syncthreads();
-            const int limit = global ? (int)(cap / 2) : kZStrata;
+            const int limit = global ? (int)(cap / 2) : zlimit;
             const uint32_t max_probe = global ? cap : 64u;
             for (int64_t v = tid; v < nvec; v += kThreads) {
                 if (*(volatile int *)&s_over) break;
@@ -848,12 +866,13 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
 #pragma unroll
                     for (int b = 0; b < 8; ++b) {
                         hs[b0 + b] = (int)zhash(z[b0 + b], cap);
-                        kk[b] = keys[hs[b0 + b]];
+                        kk[b] = k32 ? (uint64_t)hkeys32[hs[b0 + b]] : keys[hs[b0 + b]];
                     }
 #pragma unroll
                     for (int b = 0; b < 8; ++b) {
                         if (!ok || kk[b] == z[b0 + b]) continue;
                         hs[b0 + b] = global ? zinsert(keys, gids, cap, z[b0 + b], &s_distinct, limit, max_probe, zk)
+                                     : k32  ? zinsert(hkeys32, hids, cap, z[b0 + b], &s_distinct, limit, max_probe, zk)
                                             : zinsert(keys, hids, cap, z[b0 + b], &s_distinct, limit, max_probe, zk);
                         ok = hs[b0 + b] >= 0;
                     }
@@ -875,6 +894,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
                 uint64_t z = 0;
                 for (int j = 0; j < d; ++j) z = z * s_dim[j] + s_col[j][s];
                 const int h = global ? zinsert(keys, gids, cap, z, &s_distinct, limit, max_probe, zk)
+                              : k32  ? zinsert(hkeys32, hids, cap, z, &s_distinct, limit, max_probe, zk)
                                      : zinsert(keys, hids, cap, z, &s_distinct, limit, max_probe, zk);
                 if (h < 0) {
                     s_over = 1;
