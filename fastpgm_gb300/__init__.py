@@ -15,12 +15,14 @@ LIB_PATH = os.path.join(PKG, "lib", "libfastpgm_gb300.so")
 CLI_PATH = os.path.join(PKG, "bin", "fastpgm")
 
 FPGM_OK = 0
+FPGM_ERR_INVALID, FPGM_ERR_OOM, FPGM_ERR_CUDA, FPGM_ERR_TIMEOUT, FPGM_ERR_IO, FPGM_ERR_UNSUPPORTED, FPGM_ERR_STATE = (
+    -1, -2, -3, -4, -5, -6, -7)
 FPGM_MODE_BATCHED = 0
 FPGM_MODE_PLAIN = 1
 MAX_COND = 30
 
 EXPORTED = ["fpgm_last_error", "fpgm_engine_create", "fpgm_engine_destroy", "fpgm_dataset_upload",
-            "fpgm_dataset_upload_jobs",
+            "fpgm_dataset_upload_jobs", "fpgm_mle_cpts",
             "fpgm_dataset_download", "fpgm_ci_test", "fpgm_ci_test_batch", "fpgm_pc_skeleton",
             "fpgm_pc_result_sizes", "fpgm_pc_result_fetch", "fpgm_orient_cpdag", "fpgm_write_struct",
             "fpgm_bnsl_pcstable", "fpgm_generate_network", "fpgm_write_csv", "fpgm_ci_test_noalloc"]
@@ -87,6 +89,8 @@ def load():
     L.fpgm_engine_create.argtypes = [ctypes.c_int32, ctypes.POINTER(vp)]
     L.fpgm_engine_destroy.argtypes = [vp]
     L.fpgm_dataset_upload.argtypes = [vp, u8p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, u8p]
+    L.fpgm_mle_cpts.argtypes = [vp, i32p, i32p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
+                                ctypes.POINTER(ctypes.c_double)]
     L.fpgm_dataset_upload_jobs.argtypes = [vp, ctypes.c_int32, i32p, ctypes.POINTER(ctypes.c_int64),
                                            ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, u8p]
     L.fpgm_dataset_download.argtypes = [vp, u8p]
@@ -175,6 +179,27 @@ class Engine:
         self.n, self.S = int(nv.sum()), int(ns.max())
         self.job_offsets = np.concatenate([[0], np.cumsum(nv)]).astype(np.int64)
         return [card[self.job_offsets[j]:self.job_offsets[j + 1]] for j in range(len(datasets))]
+
+    def mle_cpts(self, parents, alpha=1):
+        """Maximum-likelihood tables with Laplace smoothing for a known DAG over the uploaded
+        data.  parents: per variable an iterable of parent ids (order and repeats ignored).
+        Returns a list of float64 arrays, variable v's over (v, sorted parents), v slowest."""
+        off = [0]
+        flat = []
+        for p in parents:
+            q = sorted(set(int(x) for x in p if int(x) >= 0))
+            flat += q
+            off.append(len(flat))
+        off = np.array(off, dtype=np.int32)
+        flat = np.array(flat if flat else [0], dtype=np.int32)
+        toff = np.zeros(len(off), dtype=np.int64)
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        L = load()
+        _check(L.fpgm_mle_cpts(self._h, _i32(off), _i32(flat), int(alpha), toff.ctypes.data_as(i64p), None))
+        pot = np.zeros(int(toff[-1]), dtype=np.float64)
+        _check(L.fpgm_mle_cpts(self._h, _i32(off), _i32(flat), int(alpha), toff.ctypes.data_as(i64p),
+                               pot.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return [pot[toff[v]:toff[v + 1]] for v in range(len(off) - 1)]
 
     def download(self):
         out = np.empty((self.n, self.S), dtype=np.uint8)

@@ -127,6 +127,7 @@ struct fpgm_engine {
     DevBuf bits, deg, adjl, edges_x, edges_y, pxy, pyx, cntx, total, next, status, seprank, g, off, flag,
         counters, stats, scan_tmp, log_pair, log_vars, log_meta, node_cnt, node_off;
     DevBuf slots, plain_ws, tests_buf, detail_buf, item_vars, lists, band, phase_timers;
+    DevBuf mle_counts, mle_pot, mle_meta;  // parameter learning: counts, potentials, per-node tables
     double band_alpha = -1.0;
     int n_slots = 0, hash_cap_global = 0;
     int64_t slot_bytes = 0, slot_S = 0;  // slot_S: the sample count the slots' layout was made for
@@ -468,7 +469,8 @@ extern "C" int fpgm_engine_destroy(fpgm_engine *e) {
                       &e->off, &e->flag, &e->counters, &e->stats, &e->scan_tmp, &e->log_pair,
                       &e->log_vars, &e->log_meta, &e->node_cnt, &e->node_off, &e->slots, &e->plain_ws,
                       &e->tests_buf, &e->detail_buf, &e->item_vars, &e->lists, &e->band,
-                      &e->phase_timers};
+                      &e->phase_timers, &e->var_off, &e->var_S, &e->var_lo, &e->var_hi, &e->mle_counts,
+                      &e->mle_pot, &e->mle_meta};
     for (DevBuf *b : bufs) b->release();
     if (e->ev0) cudaEventDestroy(e->ev0);
     if (e->ev1) cudaEventDestroy(e->ev1);
@@ -1135,6 +1137,158 @@ int run_plain(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
 }
 
 }  // namespace
+
+// ------------------------------------------------------------------ parameter learning
+// Maximum-likelihood tables with Laplace smoothing for a known DAG
+// (ParameterLearning::LearnParamsKnowStructCompData, parameter_learning/ParameterLearning.cpp:22-86):
+// node v's table is over (v, parents ascending), v slowest (PotentialTableBase.cpp:102-130).
+namespace {
+struct MleNode {
+    int64_t off;    // table offset in the counts / potentials
+    int32_t np;     // parents
+    int32_t par0;   // first parent in the parent list
+    int32_t cum0;   // parent configurations (table size / card[v])
+    int32_t smem;   // 1: the table fits in shared memory
+};
+
+// One CTA per (node, slice of its samples): every sample's configuration code (Horner,
+// node first) counted in a shared-memory copy of the table when it fits, else in global
+// memory directly; 16 samples per thread step from 128-bit column loads.
+__global__ void __launch_bounds__(kThreads) mle_count_kernel(const uint8_t *cols, const int64_t *var_off,
+                                                             const int32_t *var_S, const uint8_t *card,
+                                                             const MleNode *nodes, const int32_t *parents,
+                                                             int32_t *counts) {
+    extern __shared__ int smem[];
+    __shared__ const uint8_t *s_col[kMaxCols];
+    __shared__ uint32_t s_dim[kMaxCols];
+    const int v = blockIdx.x;
+    const MleNode nd = nodes[v];
+    const int ncols = nd.np + 1;
+    const int64_t S = var_S[v];
+    if (threadIdx.x < ncols) {
+        const int var = threadIdx.x == 0 ? v : parents[nd.par0 + threadIdx.x - 1];
+        s_col[threadIdx.x] = cols + var_off[var];
+        s_dim[threadIdx.x] = card[var];
+    }
+    const int64_t size = (int64_t)nd.cum0 * card[v];
+    int32_t *tab = nd.smem ? smem : counts + nd.off;
+    if (nd.smem)
+        for (int64_t i = threadIdx.x; i < size; i += blockDim.x) smem[i] = 0;
+    __syncthreads();
+    const int64_t nvec = S >> 4;
+    const int64_t per = (nvec + gridDim.y - 1) / gridDim.y;
+    const int64_t v0 = min(nvec, per * blockIdx.y), v1 = min(nvec, v0 + per);
+    for (int64_t q = v0 + threadIdx.x; q < v1; q += blockDim.x) {
+        uint32_t code[16];
+#pragma unroll
+        for (int b = 0; b < 16; ++b) code[b] = 0;
+        for (int j = 0; j < ncols; ++j) {
+            const uint4 w = __ldg(reinterpret_cast<const uint4 *>(s_col[j]) + q);
+            const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+            const uint32_t dm = s_dim[j];
+#pragma unroll
+            for (int b = 0; b < 16; ++b) code[b] = code[b] * dm + ((ww[b >> 2] >> (8 * (b & 3))) & 0xffu);
+        }
+#pragma unroll
+        for (int b = 0; b < 16; ++b) atomicAdd(&tab[code[b]], 1);
+    }
+    if (blockIdx.y == gridDim.y - 1)  // the ragged tail
+        for (int64_t s = (S & ~(int64_t)15) + threadIdx.x; s < S; s += blockDim.x) {
+            uint32_t c = 0;
+            for (int j = 0; j < ncols; ++j) c = c * s_dim[j] + s_col[j][s];
+            atomicAdd(&tab[c], 1);
+        }
+    if (nd.smem) {
+        __syncthreads();
+        for (int64_t i = threadIdx.x; i < size; i += blockDim.x)
+            if (smem[i]) atomicAdd(&counts[nd.off + i], smem[i]);
+    }
+}
+
+// potential[j] = (N[j] + alpha) / (N(B of j) + alpha * card[v]), the reference's expression
+// (ParameterLearning.cpp:73-83) in FP64; N(B) sums the node's states for j's parent configuration.
+__global__ void mle_prob_kernel(const uint8_t *card, const MleNode *nodes, const int32_t *counts, int alpha,
+                                double *pot) {
+    const int v = blockIdx.x;
+    const MleNode nd = nodes[v];
+    const int dv = card[v];
+    const int64_t size = (int64_t)nd.cum0 * dv;
+    for (int64_t j = threadIdx.x; j < size; j += blockDim.x) {
+        const int64_t b = j % nd.cum0;
+        int num2 = 0;
+        for (int a = 0; a < dv; ++a) num2 += counts[nd.off + (int64_t)a * nd.cum0 + b];
+        const int num1 = counts[nd.off + j];
+        pot[nd.off + j] = ((double)num1 + alpha) / ((double)num2 + alpha * dv);
+    }
+}
+}  // namespace
+
+extern "C" int fpgm_mle_cpts(fpgm_engine *e, const int32_t *parent_off, const int32_t *parents, int32_t alpha,
+                             int64_t *table_off, double *potentials) {
+    if (!e || !parent_off || !table_off) return set_error(FPGM_ERR_INVALID, "fpgm_mle_cpts: NULL argument");
+    if (!e->n) return set_error(FPGM_ERR_STATE, "fpgm_mle_cpts: no dataset uploaded");
+    if (alpha < 0) return set_error(FPGM_ERR_INVALID, "fpgm_mle_cpts: alpha %d < 0", alpha);
+    const int n = e->n;
+    if (parent_off[0] != 0) return set_error(FPGM_ERR_INVALID, "fpgm_mle_cpts: parent_off[0] must be 0");
+    std::vector<MleNode> nodes(n);
+    int64_t total = 0;
+    table_off[0] = 0;
+    for (int v = 0; v < n; ++v) {
+        const int np = parent_off[v + 1] - parent_off[v];
+        if (np < 0 || np > kMaxCols - 1 || (np > 0 && !parents))
+            return set_error(FPGM_ERR_INVALID, "fpgm_mle_cpts: node %d has %d parents (at most %d)", v, np,
+                             kMaxCols - 1);
+        double cum0 = 1.0;
+        for (int k = 0; k < np; ++k) {
+            const int p = parents[parent_off[v] + k];
+            if (p < 0 || p >= n || p == v || e->h_var_lo[p] != e->h_var_lo[v] ||
+                (k > 0 && p <= parents[parent_off[v] + k - 1]))
+                return set_error(FPGM_ERR_INVALID,
+                                 "fpgm_mle_cpts: parents of node %d must be other variables of its dataset, ascending",
+                                 v);
+            cum0 *= e->h_card[p];
+        }
+        const double size = cum0 * e->h_card[v];
+        if (size > (double)((int64_t)1 << 30))
+            return set_error(FPGM_ERR_UNSUPPORTED, "fpgm_mle_cpts: node %d's table has %.0f entries (at most 2^30)", v,
+                             size);
+        nodes[v].off = total;
+        nodes[v].np = np;
+        nodes[v].par0 = parent_off[v];
+        nodes[v].cum0 = (int32_t)cum0;
+        nodes[v].smem = size <= (double)(kSmemBytes / 4);
+        total += (int64_t)size;
+        table_off[v + 1] = total;
+    }
+    if (!potentials) return FPGM_OK;
+    CK(cudaSetDevice(e->device));
+    const int64_t npar = std::max<int64_t>(parent_off[n], 1);
+    RET(e->mle_meta.ensure(sizeof(MleNode) * n + npar * 4 + 64));
+    RET(e->mle_counts.ensure((size_t)total * 4 + 16));
+    RET(e->mle_pot.ensure((size_t)total * 8 + 16));
+    MleNode *d_nodes = e->mle_meta.as<MleNode>();
+    int32_t *d_par = reinterpret_cast<int32_t *>(e->mle_meta.as<char>() + (sizeof(MleNode) * n + 15) / 16 * 16);
+    CK(cudaMemcpyAsync(d_nodes, nodes.data(), sizeof(MleNode) * n, cudaMemcpyHostToDevice, e->stream));
+    if (parent_off[n] > 0)
+        CK(cudaMemcpyAsync(d_par, parents, (size_t)parent_off[n] * 4, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemsetAsync(e->mle_counts.p, 0, (size_t)total * 4, e->stream));
+    // slices per node: enough CTAs to fill the GPU, at least 64 vectors each
+    int64_t smax = 0;
+    for (int v = 0; v < n; ++v) smax = std::max<int64_t>(smax, e->h_var_S[v]);
+    const int want = std::max(1, (4 * e->num_sms + n - 1) / n);
+    const int slices = (int)std::max<int64_t>(1, std::min<int64_t>(want, (smax >> 4) / 64));
+    CK(cudaFuncSetAttribute(mle_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    mle_count_kernel<<<dim3(n, slices), kThreads, kSmemBytes, e->stream>>>(
+        e->cols.as<uint8_t>(), e->var_off.as<int64_t>(), e->var_S.as<int32_t>(), e->card.as<uint8_t>(), d_nodes, d_par,
+        e->mle_counts.as<int32_t>());
+    CK(cudaGetLastError());
+    mle_prob_kernel<<<n, kThreads, 0, e->stream>>>(e->card.as<uint8_t>(), d_nodes, e->mle_counts.as<int32_t>(), alpha,
+                                                  e->mle_pot.as<double>());
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(potentials, e->mle_pot.p, (size_t)total * 8, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return FPGM_OK;
+}
 
 // ------------------------------------------------------------------ C ABI: tests and skeleton
 extern "C" int fpgm_ci_test(fpgm_engine *e, int32_t x, int32_t y, const int32_t *z, int32_t nz, double alpha,

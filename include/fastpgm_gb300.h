@@ -130,6 +130,20 @@ int fpgm_dataset_upload(fpgm_engine *eng, const uint8_t *columns, int32_t n_vars
  * cardinalities.  At most 65,535 variables in all (16,384 for the batched skeleton). */
 int fpgm_dataset_upload_jobs(fpgm_engine *eng, int32_t n_jobs, const int32_t *job_vars, const int64_t *job_samples,
                              const uint8_t *const *job_columns, int32_t relabel, uint8_t *out_card);
+/* ---- parameter learning for a known DAG ----
+ * Maximum-likelihood tables with Laplace smoothing alpha over the uploaded data, as
+ * ParameterLearning::LearnParamsKnowStructCompData (src/fastpgm/parameter_learning/
+ * ParameterLearning.cpp:10-109, job -j 1 of the reference's command line): node v's table is
+ * over (v, its parents ascending), v's state slowest, parent configurations in mixed radix with
+ * the last parent fastest (PotentialTableBase.cpp:102-130), and
+ *   potentials[table_off[v] + j] = (N[j] + alpha) / (N(parents of j) + alpha * card[v]).
+ * parent_off[n_vars+1] / parents: each node's parents, ascending, no repeats, from its own
+ * dataset.  table_off[n_vars+1] is always filled; potentials (table_off[n_vars] doubles) only
+ * when not NULL, so a first call with NULL sizes the buffer.  Tables beyond 2^30 entries:
+ * FPGM_ERR_UNSUPPORTED. */
+int fpgm_mle_cpts(fpgm_engine *eng, const int32_t *parent_off, const int32_t *parents, int32_t alpha,
+                  int64_t *table_off, double *potentials);
+
 /* Copies the (relabelled) device columns back, n_vars*n_samples bytes (one dataset only). */
 int fpgm_dataset_download(fpgm_engine *eng, uint8_t *columns);
 

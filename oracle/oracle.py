@@ -56,6 +56,10 @@ def lib():
         L.oracle_pc_skeleton.argtypes = [u8p, u8p, ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_int,
                                          ctypes.c_int, ctypes.c_int, u8p, i32p, i32p, ctypes.POINTER(PCStats)]
         L.oracle_pc_skeleton.restype = ctypes.c_int
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        L.oracle_mle_cpts.argtypes = [u8p, u8p, ctypes.c_int, ctypes.c_int64, i32p, i32p, ctypes.c_int, i64p,
+                                      ctypes.POINTER(ctypes.c_double)]
+        L.oracle_mle_cpts.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -154,3 +158,52 @@ def read_sepsets(path):
             i, j = a.split()
             seps[(int(i), int(j))] = tuple(int(v) for v in rest.split())
     return seps
+
+
+def parent_csr(parents):
+    """Parent lists (any iterables; duplicates and order ignored, as in the reference's
+    parent set) -> (offsets int32 [n+1], sorted parents int32)."""
+    off = [0]
+    flat = []
+    for p in parents:
+        q = sorted(set(int(x) for x in p if int(x) >= 0))
+        flat += q
+        off.append(len(flat))
+    return np.array(off, dtype=np.int32), np.array(flat if flat else [0], dtype=np.int32)
+
+
+def mle_cpts(cols, card, parents, alpha=1):
+    """Maximum-likelihood tables with Laplace smoothing alpha for a known DAG (relabelled
+    columns).  Returns a list of float64 arrays, node v's over (v, sorted parents), v slowest."""
+    cols = np.ascontiguousarray(cols, dtype=np.uint8)
+    card = np.ascontiguousarray(card, dtype=np.uint8)
+    n, S = cols.shape
+    off, flat = parent_csr(parents)
+    toff = np.zeros(n + 1, dtype=np.int64)
+    i64p = ctypes.POINTER(ctypes.c_int64)
+    dp = ctypes.POINTER(ctypes.c_double)
+    rc = lib().oracle_mle_cpts(_u8(cols), _u8(card), n, S, _i32(off), _i32(flat), int(alpha),
+                               toff.ctypes.data_as(i64p), None)
+    if rc != 0:
+        raise RuntimeError("oracle_mle_cpts: table too large")
+    pot = np.zeros(int(toff[-1]), dtype=np.float64)
+    lib().oracle_mle_cpts(_u8(cols), _u8(card), n, S, _i32(off), _i32(flat), int(alpha), toff.ctypes.data_as(i64p),
+                          pot.ctypes.data_as(dp))
+    return [pot[toff[v]:toff[v + 1]] for v in range(n)]
+
+
+def ref_mle(csv, alpha, edges, workdir):
+    """The reference's own ParameterLearning on csv for the directed edges [(parent, child)]
+    (oracle/_ref/ref_driver mle).  Returns {node: (related variables, potentials)}."""
+    ein = os.path.join(workdir, "mle_edges")
+    out = os.path.join(workdir, "mle_out")
+    with open(ein, "w") as f:
+        for p, c in edges:
+            f.write("%d %d\n" % (p, c))
+    subprocess.run([REF_DRIVER, "mle", csv, str(int(alpha)), ein, out], check=True, capture_output=True)
+    res = {}
+    for line in open(out):
+        head, pots = line.split(":")
+        h = [int(x) for x in head.split()]
+        res[h[0]] = (h[2:2 + h[1]], np.array([float(x) for x in pots.split()]))
+    return res

@@ -433,3 +433,45 @@ int oracle_pc_skeleton(const uint8_t *cols, const uint8_t *card, int n, int64_t 
     free_int_columns(c, n);
     return err;
 }
+
+/* ---- maximum-likelihood parameters with Laplace smoothing for a known DAG
+ * ParameterLearning::LearnParamsKnowStructCompData
+ * (src/fastpgm/parameter_learning/ParameterLearning.cpp:22-86): node v's table is over
+ * (v, its parents in ascending order) -- PotentialTableBase.cpp:102-130, mixed radix with
+ * the last variable fastest, v slowest -- N counts every sample's configuration, N(B) the
+ * parent configuration (index mod cum_levels[0]), and
+ *   potential[j] = (N[j] + alpha) / (N(B of j) + alpha * card[v]).
+ * parent_off[n+1] / parents: each node's parent list (sorted, no repeats: a set in the
+ * reference).  out_off[n+1] receives the table offsets; out_pot (when not NULL) the tables.
+ * Returns 0, or -1 when a table would exceed 2^31 entries. */
+int oracle_mle_cpts(const uint8_t *cols, const uint8_t *card, int n, int64_t S, const int32_t *parent_off,
+                    const int32_t *parents, int alpha, int64_t *out_off, double *out_pot) {
+    out_off[0] = 0;
+    for (int v = 0; v < n; ++v) {
+        double size = card[v];
+        for (int k = parent_off[v]; k < parent_off[v + 1]; ++k) size *= card[parents[k]];
+        if (size > 2147483647.0) return -1;
+        out_off[v + 1] = out_off[v] + (int64_t)size;
+    }
+    if (!out_pot) return 0;
+    for (int v = 0; v < n; ++v) {
+        const int np = parent_off[v + 1] - parent_off[v];
+        const int32_t *par = parents + parent_off[v];
+        const int64_t size = out_off[v + 1] - out_off[v];
+        const int64_t cum0 = size / card[v]; /* parent configurations */
+        int32_t *N = (int32_t *)calloc((size_t)size, sizeof(int32_t));
+        int32_t *NB = (int32_t *)calloc((size_t)cum0, sizeof(int32_t));
+        if (!N || !NB) { free(N); free(NB); return -1; }
+        for (int64_t s = 0; s < S; ++s) {
+            int64_t idx = cols[(int64_t)v * S + s];
+            for (int k = 0; k < np; ++k) idx = idx * card[par[k]] + cols[(int64_t)par[k] * S + s];
+            N[idx]++;
+            NB[idx % cum0]++;
+        }
+        for (int64_t j = 0; j < size; ++j)
+            out_pot[out_off[v] + j] = ((double)N[j] + alpha) / ((double)NB[j % cum0] + alpha * card[v]);
+        free(N);
+        free(NB);
+    }
+    return 0;
+}

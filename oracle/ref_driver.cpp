@@ -20,6 +20,14 @@
 //       430-455), and writes "hash df g2 p indep" where hash is FNV-1a-64 over
 //       the reference's int32 joint table n[] in its own cell order, and df/g2
 //       follow IndependenceTest.cpp:94-138 on that table.
+//
+//   ref_driver mle <csv> <alpha> <edges_in> <out>
+//       Builds the network's nodes from the dataset as StructureLearning::AssignNodeInformation
+//       does (StructureLearning.cpp:11-33), adds the directed edges "parent child" of
+//       <edges_in> with Network::AddDirectedEdge, runs the reference's
+//       ParameterLearning::LearnParamsKnowStructCompData (ParameterLearning.cpp:10-109) and
+//       writes per node "node k v1..vk : p0 p1 ..." (related variables, node first, then
+//       its potentials with %.17g).
 #include <cstdio>
 #include <cstdint>
 #include <cstdlib>
@@ -35,6 +43,7 @@
 #include "fastpgm/structure_learning/PCStable.h"
 #include "fastpgm/structure_learning/IndependenceTest.h"
 #include "fastpgm/structure_learning/CellTable.h"
+#include "fastpgm/parameter_learning/ParameterLearning.h"
 
 static uint64_t fnv1a_i32(const int *v, long n) {
     uint64_t h = 1469598103934665603ull;
@@ -74,6 +83,39 @@ static int run_pc(int argc, char **argv) {
     }
     out.close();
     printf("ref_pc_seconds %.6f num_ci_test %d\n", t1 - t0, pc->num_ci_test);
+    return 0;
+}
+
+static int run_mle(int argc, char **argv) {
+    if (argc < 6) { fprintf(stderr, "mle: bad args\n"); return 2; }
+    Dataset *d = new Dataset();
+    d->LoadCSVTrainingData(argv[2], true, 0);
+    const int alpha = atoi(argv[3]);
+    Network *net = new Network(true);
+    net->num_nodes = d->num_vars;
+    for (int i = 0; i < net->num_nodes; ++i) {  // as StructureLearning::AssignNodeInformation
+        DiscreteNode *node = new DiscreteNode(i);
+        node->node_name = d->vec_var_names.size() == (size_t)net->num_nodes ? d->vec_var_names[i] : std::to_string(i);
+        node->possible_values_ids = d->vars_possible_values_ids[i];
+        node->SetDomainSize(d->num_of_possible_values_of_disc_vars[i]);
+        net->map_idx_node_ptr[i] = node;
+    }
+    std::ifstream in(argv[4]);
+    int p, c;
+    while (in >> p >> c) net->AddDirectedEdge(p, c);
+    ParameterLearning *pl = new ParameterLearning(net);
+    pl->LearnParamsKnowStructCompData(d, alpha, false, "", 0);
+    FILE *out = fopen(argv[5], "w");
+    if (!out) return 1;
+    for (int i = 0; i < net->num_nodes; ++i) {
+        const PotentialTableBase &pt = net->pts[i];
+        fprintf(out, "%d %d", i, pt.num_variables);
+        for (int v : pt.vec_related_variables) fprintf(out, " %d", v);
+        fprintf(out, " :");
+        for (double x : pt.potentials) fprintf(out, " %.17g", x);
+        fprintf(out, "\n");
+    }
+    fclose(out);
     return 0;
 }
 
@@ -160,6 +202,7 @@ static int run_tests(int argc, char **argv) {
 int main(int argc, char **argv) {
     if (argc < 2) { fprintf(stderr, "usage: ref_driver pc|tests ...\n"); return 2; }
     std::string mode = argv[1];
+    if (mode == "mle") return run_mle(argc, argv);
     if (mode == "pc") return run_pc(argc, argv);
     if (mode == "tests") return run_tests(argc, argv);
     fprintf(stderr, "unknown mode %s\n", mode.c_str());

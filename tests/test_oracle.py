@@ -13,6 +13,7 @@ import pytest
 
 from conftest import GOLDEN, read_sepsets, read_tests
 from oracle import oracle as O
+import fastpgm_gb300 as F
 
 
 def test_igamma_matches_scipy():
@@ -144,3 +145,23 @@ def test_wilson_hilferty_router_bound():
         wh = 0.5 * sp.erfc((np.cbrt(xs / k) - (1 - v)) / np.sqrt(v) / np.sqrt(2))
         assert np.abs(wh - exact).max() < 1e-6
         assert st.chi2.pdf(xs, k).max() < 0.3 / np.sqrt(k)
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference-built driver needs the reference tree")
+@pytest.mark.parametrize("alpha", [0, 1, 3])
+def test_mle_oracle_matches_reference_parameter_learning(tmp_path, alpha):
+    """The oracle's maximum-likelihood tables equal the reference's own
+    ParameterLearning::LearnParamsKnowStructCompData bit for bit, for the true DAG of a
+    generated network (nodes with 0 to 4 parents)."""
+    raw, _, par = F.generate(n_nodes=37, n_samples=5000, seed=1, n_edges=46, max_indegree=4, card=(2, 4))
+    csv = str(tmp_path / "d.csv")
+    F.write_csv(csv, raw)
+    edges = [(int(p), c) for c in range(par.shape[0]) for p in par[c] if p >= 0]
+    ref = O.ref_mle(csv, alpha, edges, str(tmp_path))
+    cols, card = O.relabel(raw)
+    got = O.mle_cpts(cols, card, [par[c] for c in range(par.shape[0])], alpha=alpha)
+    assert any(len(v) > 3 for v, _ in ref.values())
+    for v in range(raw.shape[0]):
+        rel, pots = ref[v]
+        assert rel[0] == v and rel[1:] == sorted(int(p) for p in par[v] if p >= 0)
+        assert np.array_equal(got[v], pots), v
