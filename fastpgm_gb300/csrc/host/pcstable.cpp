@@ -474,3 +474,99 @@ extern "C" int fpgm_bnsl_pcstable(int32_t verbose, int32_t n_threads, int32_t gr
     if (!train_set) return fpgm::set_error(FPGM_ERR_INVALID, "fpgm_bnsl_pcstable: train_set is NULL");
     return bnsl_impl(verbose, n_threads, group_size, alpha, ref_net ? ref_net : "", train_set, save_struct != 0);
 }
+
+// ------------------------------------------------------------------ ParameterLearning
+void PotentialTableBase::GetConfigValueByTableIndex(const int &table_index, int *config_value) const {
+    int a = table_index;  // PotentialTableBase.cpp:1179-1187
+    for (int i = 0; i < num_variables; ++i) {
+        config_value[i] = a / cum_levels[i];
+        a %= cum_levels[i];
+    }
+}
+
+namespace {
+string value_name(const Node *node, int id) {  // DiscreteNode::GetValueNameByIndex
+    for (const auto &kv : node->possible_values_ids)
+        if (kv.second == id) return kv.first;
+    return std::to_string(id);
+}
+}  // namespace
+
+void ParameterLearning::LearnParamsKnowStructCompData(const Dataset *dts, int alpha, bool save_param,
+                                                      string param_file, int verbose) {
+    if (verbose > 0)
+        cout << "--------------------------------------------------" << '\n'
+             << "Parameter learning with maximum likelihood estimation... " << endl
+             << "Laplace smoothing param alpha = " << alpha << endl;
+    const auto t0 = std::chrono::steady_clock::now();
+    const int n = dts->num_vars;
+    if (network->num_nodes != n) {
+        fprintf(stderr, "Error in function %s! The network has %d nodes and the dataset %d variables (a ROOT node is "
+                        "not supported here)\n", __FUNCTION__, network->num_nodes, n);
+        exit(1);
+    }
+    vector<int32_t> off(n + 1, 0), par;
+    for (int v = 0; v < n; ++v) {
+        const Node *node = network->FindNodePtrByIndex(v);
+        for (int p : node->set_parent_indexes) par.push_back(p);  // a set: ascending
+        off[v + 1] = (int32_t)par.size();
+    }
+    if (par.empty()) par.push_back(0);
+    fpgm_engine *eng = nullptr;
+    die_on(shared_engine(device, &eng));
+    die_on(fpgm_dataset_upload(eng, dts->columns.data(), n, dts->num_instance, 0, nullptr));
+    vector<int64_t> toff(n + 1);
+    die_on(fpgm_mle_cpts(eng, off.data(), par.data(), alpha, toff.data(), nullptr));
+    vector<double> pot((size_t)toff[n] + 1);
+    die_on(fpgm_mle_cpts(eng, off.data(), par.data(), alpha, toff.data(), pot.data()));
+    network->pts.assign(n, PotentialTableBase());
+    for (int v = 0; v < n; ++v) {  // PotentialTableBase.cpp:102-130 layout
+        PotentialTableBase &pt = network->pts[v];
+        pt.num_variables = off[v + 1] - off[v] + 1;
+        pt.vec_related_variables.push_back(v);
+        for (int k = off[v]; k < off[v + 1]; ++k) pt.vec_related_variables.push_back(par[k]);
+        for (int u : pt.vec_related_variables) pt.var_dims.push_back(dts->num_of_possible_values_of_disc_vars[u]);
+        pt.cum_levels.assign(pt.num_variables, 1);
+        for (int i = pt.num_variables - 2; i >= 0; --i) pt.cum_levels[i] = pt.cum_levels[i + 1] * pt.var_dims[i + 1];
+        pt.table_size = (int)(toff[v + 1] - toff[v]);
+        pt.potentials.assign(pot.begin() + toff[v], pot.begin() + toff[v + 1]);
+    }
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    cout << "parameter_learning: " << secs << " s " << endl;
+    if (save_param) SaveBNParameter(param_file);
+}
+
+void ParameterLearning::SaveBNParameter(string param_file) {  // ParameterLearning.cpp:111-152
+    std::ofstream out_file(param_file);
+    if (!out_file.is_open()) {
+        fprintf(stderr, "Error in function %s!", __FUNCTION__);
+        fprintf(stderr, "Unable to open file %s!", param_file.c_str());
+        exit(1);
+    }
+    for (int i = 0; i < network->num_nodes; ++i) {
+        const Node *node = network->FindNodePtrByIndex(i);
+        const string head = "P (" + node->node_name + "/v" + std::to_string(i) + "=";
+        const PotentialTableBase &pt = network->pts[i];
+        if (pt.num_variables == 1) {
+            for (int j = 0; j < pt.table_size; ++j)
+                out_file << head + value_name(node, j) + "/" + std::to_string(j) + ") = " +
+                                std::to_string(pt.potentials[j])
+                         << endl;
+        } else {
+            vector<int> config(pt.num_variables);
+            for (int j = 0; j < pt.table_size; ++j) {
+                pt.GetConfigValueByTableIndex(j, config.data());
+                string prob = head + value_name(node, config[0]) + "/" + std::to_string(config[0]) + " | ";
+                for (int k = 1; k < pt.num_variables; ++k) {
+                    const Node *par = network->FindNodePtrByIndex(pt.vec_related_variables[k]);
+                    prob += par->node_name + "/v" + std::to_string(pt.vec_related_variables[k]) + "=" +
+                            value_name(par, config[k]) + "/" + std::to_string(config[k]) + ", ";
+                }
+                prob.pop_back();
+                prob.pop_back();
+                out_file << prob + ") = " + std::to_string(pt.potentials[j]) << endl;
+            }
+        }
+    }
+    cout << "Learned parameters have been saved in " << param_file << endl;
+}

@@ -7,6 +7,8 @@
 //
 // Reference declarations mirrored (paths inside the FastPGM tree):
 //   Node                include/fastpgm/Node.h            (index, name, parent/child index sets)
+//   PotentialTableBase  include/fastpgm/PotentialTableBase.h (potentials, variables, radix)
+//   ParameterLearning   include/fastpgm/parameter_learning/ParameterLearning.h
 //   Edge, EndPoint      include/fastpgm/Edge.h:13-44      (node1/node2, end points, IsDirected)
 //   Network             include/fastpgm/Network.h         (num_nodes, num_edges, vec_edges,
 //                                                          map_idx_node_ptr, FindNodePtrByIndex,
@@ -85,8 +87,21 @@ public:
     }
 };
 
+// include/fastpgm/PotentialTableBase.h: the fields parameter learning fills
+class PotentialTableBase {
+public:
+    std::vector<double> potentials;
+    std::vector<int> vec_related_variables;  // the node, then its parents ascending
+    std::vector<int> var_dims;
+    std::vector<int> cum_levels;             // mixed radix, last variable fastest
+    int num_variables = 0;
+    int table_size = 0;
+    void GetConfigValueByTableIndex(const int &table_index, int *config_value) const;
+};
+
 class Network {
 public:
+    std::vector<PotentialTableBase> pts;  // one per node after parameter learning
     std::string network_name;
     int num_nodes = 0;
     int num_edges = 0;
@@ -160,6 +175,20 @@ public:
                                      bool save_struct, std::string struct_file, int verbose);
     // Same work, returning an FPGM status instead of exiting on failure.
     int Run(Dataset *dts, bool dag, bool add_root, bool save_struct, const std::string &struct_file, int verbose);
+};
+
+// parameter_learning/ParameterLearning.h:14-23: maximum-likelihood tables with Laplace
+// smoothing for the network's known DAG (the parents in Node::set_parent_indexes), counted on
+// the GPU (fpgm_mle_cpts).  A virtual ROOT node (add_root) is not supported here.
+class ParameterLearning {
+public:
+    Network *network;
+    int device = 0;  // CUDA device (not in the reference)
+
+    explicit ParameterLearning(Network *net) : network(net) {}
+    void LearnParamsKnowStructCompData(const Dataset *dts, int alpha, bool save_param, std::string param_file,
+                                       int verbose);
+    void SaveBNParameter(std::string param_file);
 };
 
 // fastpgm_api.cpp:18-44

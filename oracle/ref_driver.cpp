@@ -21,13 +21,13 @@
 //       the reference's int32 joint table n[] in its own cell order, and df/g2
 //       follow IndependenceTest.cpp:94-138 on that table.
 //
-//   ref_driver mle <csv> <alpha> <edges_in> <out>
+//   ref_driver mle <csv> <alpha> <edges_in> <out> [param_file]
 //       Builds the network's nodes from the dataset as StructureLearning::AssignNodeInformation
 //       does (StructureLearning.cpp:11-33), adds the directed edges "parent child" of
 //       <edges_in> with Network::AddDirectedEdge, runs the reference's
 //       ParameterLearning::LearnParamsKnowStructCompData (ParameterLearning.cpp:10-109) and
 //       writes per node "node k v1..vk : p0 p1 ..." (related variables, node first, then
-//       its potentials with %.17g).
+//       its potentials with %.17g), and with param_file the reference's SaveBNParameter file.
 #include <cstdio>
 #include <cstdint>
 #include <cstdlib>
@@ -104,7 +104,8 @@ static int run_mle(int argc, char **argv) {
     int p, c;
     while (in >> p >> c) net->AddDirectedEdge(p, c);
     ParameterLearning *pl = new ParameterLearning(net);
-    pl->LearnParamsKnowStructCompData(d, alpha, false, "", 0);
+    const bool save = argc > 6;  // optional: the reference's own SaveBNParameter file
+    pl->LearnParamsKnowStructCompData(d, alpha, save, save ? argv[6] : "", 0);
     FILE *out = fopen(argv[5], "w");
     if (!out) return 1;
     for (int i = 0; i < net->num_nodes; ++i) {

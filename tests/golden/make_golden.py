@@ -12,8 +12,11 @@ driver (oracle/Makefile `ref` target).  Writes, under tests/golden/:
   <cfg>_meta.json        sha256 of the generated raw columns, shape, reference test count
   <set>_tests.txt        per-test golden vectors from the reference's IndependenceTest and
                          Counts2D/Counts3D: "x y d z.. | hash df g2 p indep"
+  c1_dag                 the generating DAG of c1 as "parent child" lines
+  c1_param_alpha1        the reference's ParameterLearning (Laplace alpha 1) for that DAG,
+                         written by its own SaveBNParameter
 
-Run:  python tests/golden/make_golden.py
+Run:  python tests/golden/make_golden.py [--mle-only]
 """
 import hashlib
 import json
@@ -62,9 +65,32 @@ def ref_tests(csv, tests, out_path):
         shutil.rmtree(tmp)
 
 
+def mle_golden():
+    """c1's true DAG and the reference's parameter file for it."""
+    spec = dict(F.CONFIGS["c1"])
+    spec.pop("depth")
+    raw, _, par = F.generate(**spec)
+    edges = [(int(p), c) for c in range(par.shape[0]) for p in par[c] if p >= 0]
+    with open(os.path.join(HERE, "c1_dag"), "w") as f:
+        for p, c in edges:
+            f.write("%d %d\n" % (p, c))
+    tmp = tempfile.mkdtemp()
+    try:
+        csv = os.path.join(tmp, "c1.csv")
+        F.write_csv(csv, raw)
+        import subprocess
+        subprocess.check_call([O.REF_DRIVER, "mle", csv, "1", os.path.join(HERE, "c1_dag"), os.path.join(tmp, "o"),
+                               os.path.join(HERE, "c1_param_alpha1")], stdout=subprocess.DEVNULL)
+    finally:
+        shutil.rmtree(tmp)
+
+
 def main():
     O.build()
     assert O.ref_available(), "reference-built driver missing"
+    mle_golden()
+    if "--mle-only" in sys.argv:
+        return
     rng = np.random.default_rng(1234)
     # alarm
     alarm_csv = os.path.join(REF, "dataset/alarm/alarm_s5000")

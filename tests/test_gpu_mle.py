@@ -90,3 +90,46 @@ def test_invalid_parent_lists(eng):
         rc = L.fpgm_mle_cpts(eng._h, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
                              flat.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), 1, toff.ctypes.data_as(i64), None)
         assert rc == F.FPGM_ERR_INVALID
+
+
+_PROGRAM = r"""
+#include <cstdlib>
+#include <fstream>
+#include "fastpgm_gb300_cxx.h"
+int main(int argc, char **argv) {
+    Dataset *d = new Dataset();
+    d->LoadCSVTrainingData(argv[1], true, 0);
+    Network *net = new Network(true);
+    PCStable pc(net, 0.05);     // only to build the nodes from the dataset
+    pc.AssignNodeInformation(d);
+    std::ifstream in(argv[2]);
+    int p, c;
+    while (in >> p >> c) {
+        net->FindNodePtrByIndex(c)->set_parent_indexes.insert(p);
+        net->FindNodePtrByIndex(p)->set_children_indexes.insert(c);
+    }
+    ParameterLearning pl(net);
+    pl.LearnParamsKnowStructCompData(d, atoi(argv[3]), true, argv[4], 0);
+    return 0;
+}
+"""
+
+
+def test_cxx_parameter_learning_reproduces_reference_file(tmp_path):
+    """The C++ drop-in ParameterLearning writes, for c1's generating DAG, the same file the
+    reference's own ParameterLearning + SaveBNParameter wrote (tests/golden/c1_param_alpha1)."""
+    import os
+    import subprocess
+    from conftest import GOLDEN, ROOT
+    raw, _, _ = F.make_config("c1")
+    csv = str(tmp_path / "c1.csv")
+    F.write_csv(csv, raw)
+    src = tmp_path / "pl.cpp"
+    src.write_text(_PROGRAM)
+    exe = str(tmp_path / "pl")
+    libdir = os.path.dirname(F.LIB_PATH)
+    subprocess.run(["g++", "-O1", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", exe,
+                    "-L", libdir, "-lfastpgm_gb300", "-Wl,-rpath," + libdir], check=True)
+    out = str(tmp_path / "param")
+    subprocess.run([exe, csv, os.path.join(GOLDEN, "c1_dag"), "1", out], check=True, capture_output=True)
+    assert open(out).read() == open(os.path.join(GOLDEN, "c1_param_alpha1")).read()
