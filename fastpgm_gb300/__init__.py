@@ -22,7 +22,7 @@ FPGM_MODE_PLAIN = 1
 MAX_COND = 30
 
 EXPORTED = ["fpgm_last_error", "fpgm_engine_create", "fpgm_engine_destroy", "fpgm_dataset_upload",
-            "fpgm_dataset_upload_jobs", "fpgm_mle_cpts",
+            "fpgm_dataset_upload_jobs", "fpgm_mle_cpts", "fpgm_shd_bif",
             "fpgm_dataset_download", "fpgm_ci_test", "fpgm_ci_test_batch", "fpgm_pc_skeleton",
             "fpgm_pc_result_sizes", "fpgm_pc_result_fetch", "fpgm_orient_cpdag", "fpgm_write_struct",
             "fpgm_bnsl_pcstable", "fpgm_generate_network", "fpgm_write_csv", "fpgm_ci_test_noalloc"]
@@ -89,6 +89,7 @@ def load():
     L.fpgm_engine_create.argtypes = [ctypes.c_int32, ctypes.POINTER(vp)]
     L.fpgm_engine_destroy.argtypes = [vp]
     L.fpgm_dataset_upload.argtypes = [vp, u8p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, u8p]
+    L.fpgm_shd_bif.argtypes = [ctypes.c_char_p, ctypes.c_int32, i32p, ctypes.c_int32, i32p]
     L.fpgm_mle_cpts.argtypes = [vp, i32p, i32p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
                                 ctypes.POINTER(ctypes.c_double)]
     L.fpgm_dataset_upload_jobs.argtypes = [vp, ctypes.c_int32, i32p, ctypes.POINTER(ctypes.c_int64),
@@ -281,6 +282,16 @@ def generate(n_nodes, n_samples, seed, n_edges=0, avg_indegree=2.0, max_indegree
     par = np.full((n_nodes, max(1, max_indegree)), -1, dtype=np.int32)
     _check(load().fpgm_generate_network(ctypes.byref(spec), _u8(cols), _u8(c), _i32(par)))
     return cols, c, par
+
+
+def shd_bif(bif_path, n_nodes, edges):
+    """Structural Hamming distance of learned edges ([m, 3] (a, b, directed), as orient_cpdag
+    returns them) against the network of a BIF file, as BNSL_PCStable reports it."""
+    edges = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1, 3)
+    flat = edges if len(edges) else np.zeros((1, 3), dtype=np.int32)
+    out = ctypes.c_int32()
+    _check(load().fpgm_shd_bif(bif_path.encode(), int(n_nodes), _i32(flat), len(edges), ctypes.byref(out)))
+    return out.value
 
 
 def write_csv(path, columns, prefix="V"):

@@ -451,11 +451,22 @@ int bnsl_impl(int verbose, int n_threads, int group_size, double alpha, const st
     int rc = bnsl->Run(trainer, false, false, save_struct, train_set + "_struct", verbose);
     delete trainer;
     if (rc == FPGM_OK) {
-        if (!ref_net.empty())
-            cout << "The reference BN comparison (SHD) is not part of the GPU PC-stable engine; skipped." << endl;
-        else
+        if (!ref_net.empty()) {  // fastpgm_api.cpp:32-38: LoadBIFFile + BNSLComparison::GetSHD
+            vector<int32_t> edges;
+            for (const Edge &e : network->vec_edges) {
+                edges.push_back(e.node1->GetNodeIndex());
+                edges.push_back(e.node2->GetNodeIndex());
+                edges.push_back(e.end_point2 == ARROW ? 1 : 0);
+            }
+            if (edges.empty()) edges.assign(3, 0);
+            int32_t shd = 0;
+            rc = fpgm_shd_bif(ref_net.c_str(), network->num_nodes, edges.data(),
+                              (int32_t)network->vec_edges.size(), &shd);
+            if (rc == FPGM_OK) cout << "SHD = " << shd << endl;
+        } else {
             cout << "There is no reference BN (ground-truth) provided, comparison (showing accuracy) is skipped."
                  << endl;
+        }
     }
     bnsl->network = nullptr;  // the reference deletes the network itself and never deletes bnsl
     delete network;

@@ -130,6 +130,15 @@ int fpgm_dataset_upload(fpgm_engine *eng, const uint8_t *columns, int32_t n_vars
  * cardinalities.  At most 65,535 variables in all (16,384 for the batched skeleton). */
 int fpgm_dataset_upload_jobs(fpgm_engine *eng, int32_t n_jobs, const int32_t *job_vars, const int64_t *job_samples,
                              const uint8_t *const *job_columns, int32_t relabel, uint8_t *out_card);
+/* ---- accuracy against a reference network ----
+ * Structural Hamming distance of a learned graph -- edges as fpgm_orient_cpdag returns them,
+ * (a, b, directed) in the reference's record order -- against the network of a BIF file, as
+ * BNSL_PCStable reports it (fastpgm_api.cpp:32-41: CustomNetwork::LoadBIFFile,
+ * BNSLComparison::GetSHD, structure_learning/BNSLComparison.cpp:12-73): when the learned
+ * graph's first edge is undirected, the reference DAG is first turned into its CPDAG
+ * (Network::OrderEdge/FindCompelled, Network.cpp:547-690). */
+int fpgm_shd_bif(const char *bif_path, int32_t n_nodes, const int32_t *edges, int32_t n_edges, int32_t *shd);
+
 /* ---- parameter learning for a known DAG ----
  * Maximum-likelihood tables with Laplace smoothing alpha over the uploaded data, as
  * ParameterLearning::LearnParamsKnowStructCompData (src/fastpgm/parameter_learning/

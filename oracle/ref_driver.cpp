@@ -21,6 +21,8 @@
 //       the reference's int32 joint table n[] in its own cell order, and df/g2
 //       follow IndependenceTest.cpp:94-138 on that table.
 //
+//   ref_driver shd <csv> <alpha> <bif>     (see run_shd)
+//
 //   ref_driver mle <csv> <alpha> <edges_in> <out> [param_file]
 //       Builds the network's nodes from the dataset as StructureLearning::AssignNodeInformation
 //       does (StructureLearning.cpp:11-33), adds the directed edges "parent child" of
@@ -44,6 +46,8 @@
 #include "fastpgm/structure_learning/IndependenceTest.h"
 #include "fastpgm/structure_learning/CellTable.h"
 #include "fastpgm/parameter_learning/ParameterLearning.h"
+#include "fastpgm/CustomNetwork.h"
+#include "fastpgm/structure_learning/BNSLComparison.h"
 
 static uint64_t fnv1a_i32(const int *v, long n) {
     uint64_t h = 1469598103934665603ull;
@@ -83,6 +87,23 @@ static int run_pc(int argc, char **argv) {
     }
     out.close();
     printf("ref_pc_seconds %.6f num_ci_test %d\n", t1 - t0, pc->num_ci_test);
+    return 0;
+}
+
+// ref_driver shd <csv> <alpha> <bif>: BNSL_PCStable with a reference network
+// (fastpgm_api.cpp:18-44): PC-stable as in `pc` mode (one thread), then
+// CustomNetwork::LoadBIFFile and BNSLComparison::GetSHD; prints "SHD = <n>".
+static int run_shd(int argc, char **argv) {
+    if (argc < 5) { fprintf(stderr, "shd: bad args\n"); return 2; }
+    Dataset *d = new Dataset();
+    d->LoadCSVTrainingData(argv[2], true, 0);
+    Network *net = new Network(true);
+    PCStable *pc = new PCStable(net, atof(argv[3]), 1000);
+    pc->StructLearnCompData(d, 1, 1, false, false, false, "", 0);
+    CustomNetwork *r_net = new CustomNetwork();
+    r_net->LoadBIFFile(argv[4]);
+    BNSLComparison comp(r_net, net);
+    printf("SHD = %d\n", comp.GetSHD());
     return 0;
 }
 
@@ -204,6 +225,7 @@ int main(int argc, char **argv) {
     if (argc < 2) { fprintf(stderr, "usage: ref_driver pc|tests ...\n"); return 2; }
     std::string mode = argv[1];
     if (mode == "mle") return run_mle(argc, argv);
+    if (mode == "shd") return run_shd(argc, argv);
     if (mode == "pc") return run_pc(argc, argv);
     if (mode == "tests") return run_tests(argc, argv);
     fprintf(stderr, "unknown mode %s\n", mode.c_str());

@@ -146,3 +146,66 @@ def test_python_binding_module_signature():
     import inspect
     params = list(inspect.signature(cmake_example.BNSL_PCStable).parameters)
     assert params == ["verbose", "n_threads", "group_size", "alpha", "ref_net", "train_set", "save_struct"]
+
+
+def _write_bif(path, card, parents):
+    """A minimal BIF file of a DAG (uniform tables), in the layout the reference's
+    CustomNetwork::LoadBIFFile reads."""
+    import itertools
+    n = len(card)
+    lines = ["network unknown {", "}"]
+    for v in range(n):
+        states = ", ".join("s%d" % k for k in range(card[v]))
+        lines += ["variable V%d {" % v, "  type discrete [ %d ] { %s };" % (card[v], states), "}"]
+    for v in range(n):
+        ps = [int(p) for p in parents[v] if p >= 0]
+        row = ", ".join(["%.4f" % (1.0 / card[v])] * card[v]) + ";"
+        if not ps:
+            lines += ["probability ( V%d ) {" % v, "  table " + row, "}"]
+            continue
+        lines.append("probability ( V%d | %s ) {" % (v, ", ".join("V%d" % p for p in ps)))
+        for cfg in itertools.product(*[range(card[p]) for p in ps]):
+            lines.append("  (%s) %s" % (", ".join("s%d" % c for c in cfg), row))
+        lines.append("}")
+    open(path, "w").write("\n".join(lines) + "\n")
+
+
+def _learned_edges(cols, card):
+    r = O.pc_skeleton(cols, card, threads=8)
+    removed, off, vs = sepset_arrays(r["sepsets"])
+    return F.orient_cpdag(r["adj"], removed, off, vs)
+
+
+def test_shd_of_a_dag_against_its_own_bif(tmp_path):
+    """A learned DAG (first edge directed: no CPDAG conversion) scores 0 against itself, and
+    one missing arc or one reversed arc cost 1 each."""
+    _, card, par = F.generate(n_nodes=12, n_samples=100, seed=5, n_edges=14, max_indegree=3, card=(2, 3))
+    bif = str(tmp_path / "g.bif")
+    _write_bif(bif, card, par)
+    arcs = [(int(p), c, 1) for c in range(12) for p in par[c] if p >= 0]
+    assert F.shd_bif(bif, 12, arcs) == 0
+    assert F.shd_bif(bif, 12, arcs[:-1]) == 1
+    a, b, _ = arcs[-1]
+    assert F.shd_bif(bif, 12, arcs[:-1] + [(b, a, 1)]) == 1
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference-built driver needs the reference tree")
+def test_shd_matches_reference_comparison(tmp_path):
+    """BNSL_PCStable's SHD report: the learned CPDAG against the reference network, equal to
+    the reference's own CustomNetwork::LoadBIFFile + BNSLComparison::GetSHD -- on alarm
+    (its shipped alarm.bif) and on c1 (its generating DAG written as BIF)."""
+    ref_root = "/root/reference/dataset/alarm/"
+    cases = [(ref_root + "alarm_s5000", ref_root + "alarm.bif", None)]
+    raw, card, par = F.generate(n_nodes=37, n_samples=5000, seed=1, n_edges=46, max_indegree=4, card=(2, 4))
+    c1_csv, c1_bif = str(tmp_path / "c1.csv"), str(tmp_path / "c1.bif")
+    F.write_csv(c1_csv, raw)
+    _write_bif(c1_bif, card, par)
+    cases.append((c1_csv, c1_bif, raw))
+    for csv, bif, raw in cases:
+        out = subprocess.run([O.REF_DRIVER, "shd", csv, "0.05", bif], capture_output=True, text=True, check=True)
+        ref = int(re.search(r"SHD = (\d+)", out.stdout).group(1))
+        if raw is None:
+            names, cols, cd = O.read_csv_columns(csv)
+        else:
+            cols, cd = O.relabel(raw)
+        assert F.shd_bif(bif, cols.shape[0], _learned_edges(cols, cd)) == ref
