@@ -61,7 +61,7 @@ def build(verbose=False):
         if src.endswith("main.cpp"):
             continue
         obj = os.path.join(OBJ, os.path.basename(src) + ".o")
-        extra = ["-ffp-contract=off", "-fopenmp"] if src.endswith("datagen.cpp") else []
+        extra = ["-ffp-contract=off", "-fopenmp"] if src.endswith("datagen.cpp") else ["-fopenmp"]
         units.append((src, obj, ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wextra"] + extra + inc
                       + ["-I" + cuda_inc, "-c", src, "-o", obj]))
     procs = []

@@ -7,8 +7,10 @@
 #include <fstream>
 #include <iostream>
 #include <mutex>
+#include <omp.h>
 #include <queue>
 #include <random>
+#include <string_view>
 
 #include "fastpgm_gb300.h"
 #include "fastpgm_gb300_cxx.h"
@@ -107,7 +109,138 @@ vector<string> split_commas(const string &s) {  // common.cpp Split
 }
 }  // namespace
 
+namespace {
+// Parallel CSV reading with the reference's semantics (Dataset.cpp:389-503): header = names,
+// each non-empty line (trailing characters below '!' trimmed) split at commas, and per
+// column the state ids in order of first appearance.  Threads parse contiguous row ranges
+// with their own per-column value lists (value, first row); the lists are then merged so the
+// ids follow the first appearance in the whole file, and each thread's ids are remapped.
+// Returns the number of rows, or -1 (and *bad_row = 0-based row) for a row with too few
+// fields, or -2 (and *bad_col) for a column with more than 255 states.
+int64_t parse_rows_parallel(const string &buf, size_t body, int num_vars, vector<unsigned char> &columns,
+                            vector<std::map<string, int>> &ids, int64_t *bad_row, int *bad_col) {
+    vector<std::pair<size_t, size_t>> rows;  // [begin, end) of each non-empty trimmed line
+    for (size_t b = body; b < buf.size();) {
+        size_t e = buf.find('\n', b);
+        if (e == string::npos) e = buf.size();
+        size_t t = e;
+        while (t > b && (unsigned char)buf[t - 1] < 33) --t;
+        if (t > b) rows.push_back({b, t});
+        b = e + 1;
+    }
+    const int64_t R = (int64_t)rows.size();
+    columns.assign((size_t)num_vars * R, 0);
+    const int T = std::max(1, omp_get_max_threads());
+    const int64_t chunk = (R + T - 1) / T;
+    using Seen = vector<std::pair<std::string_view, int64_t>>;  // value, first row
+    vector<vector<Seen>> seen(T, vector<Seen>(num_vars));
+    vector<int64_t> short_row(T, -1);
+#pragma omp parallel num_threads(T)
+    {
+        const int t = omp_get_thread_num();
+        const int64_t r0 = std::min(R, t * chunk), r1 = std::min(R, r0 + chunk);
+        for (int64_t r = r0; r < r1 && short_row[t] < 0; ++r) {
+            size_t b = rows[r].first;
+            const size_t e = rows[r].second;
+            for (int v = 0; v < num_vars; ++v) {
+                if (b > e) { short_row[t] = r; break; }
+                size_t c = buf.find(',', b);
+                if (c == string::npos || c > e) c = e;
+                const std::string_view f(buf.data() + b, c - b);
+                Seen &sv = seen[t][v];
+                size_t k = 0;
+                while (k < sv.size() && sv[k].first != f) ++k;
+                if (k == sv.size()) sv.push_back({f, r});
+                columns[(size_t)v * R + r] = (unsigned char)std::min<size_t>(k, 255);
+                b = c + 1;
+            }
+        }
+    }
+    for (int t = 0; t < T; ++t)
+        if (short_row[t] >= 0) { *bad_row = short_row[t]; return -1; }
+    // ids in order of first appearance in the whole file, and each thread's local -> global
+    vector<vector<vector<unsigned char>>> remap(T, vector<vector<unsigned char>>(num_vars));
+    ids.assign(num_vars, {});
+    for (int v = 0; v < num_vars; ++v) {
+        std::map<std::string_view, int64_t> first;
+        for (int t = 0; t < T; ++t)
+            for (auto &x : seen[t][v]) {
+                auto it = first.find(x.first);
+                if (it == first.end() || x.second < it->second) first[x.first] = x.second;
+            }
+        if (first.size() > 255) { *bad_col = v; return -2; }
+        vector<std::pair<int64_t, std::string_view>> order;
+        for (auto &kv : first) order.push_back({kv.second, kv.first});
+        std::sort(order.begin(), order.end());
+        std::map<std::string_view, int> gid;
+        for (size_t k = 0; k < order.size(); ++k) {
+            gid[order[k].second] = (int)k;
+            ids[v].emplace(string(order[k].second), (int)k);
+        }
+        for (int t = 0; t < T; ++t)
+            for (auto &x : seen[t][v]) remap[t][v].push_back((unsigned char)gid[x.first]);
+    }
+#pragma omp parallel num_threads(T)
+    {
+        const int t = omp_get_thread_num();
+        const int64_t r0 = std::min(R, t * chunk), r1 = std::min(R, r0 + chunk);
+        for (int v = 0; v < num_vars; ++v) {
+            const vector<unsigned char> &m = remap[t][v];
+            unsigned char *col = columns.data() + (size_t)v * R;
+            for (int64_t r = r0; r < r1; ++r) col[r] = m[col[r]];
+        }
+    }
+    return R;
+}
+}  // namespace
+
 void Dataset::LoadCSVTrainingData(string data_file_path, bool str_val, int cls_var_id, std::set<int> cont_vars) {
+    if (str_val && cont_vars.empty()) {  // the usual case, read in parallel
+        FILE *fp = fopen(data_file_path.c_str(), "rb");
+        if (!fp) {
+            fprintf(stderr, "Error in function %s!", __FUNCTION__);
+            fprintf(stderr, "Unable to open file %s!", data_file_path.c_str());
+            exit(1);
+        }
+        string buf;
+        char chunk[1 << 16];
+        fseek(fp, 0, SEEK_END);
+        const long size = ftell(fp);
+        fseek(fp, 0, SEEK_SET);
+        if (size > 0) buf.reserve((size_t)size);
+        for (size_t got; (got = fread(chunk, 1, sizeof chunk, fp)) > 0;) buf.append(chunk, got);
+        fclose(fp);
+        class_var_index = cls_var_id;
+        size_t e = buf.find('\n');
+        if (e == string::npos) e = buf.size();
+        vec_var_names = split_commas(trim_right(buf.substr(0, e)));
+        num_vars = (int)vec_var_names.size();
+        if (std::set<string>(vec_var_names.begin(), vec_var_names.end()).size() != vec_var_names.size()) {
+            fprintf(stderr, "Error in function [%s]\nDuplicate variable names in header!", __FUNCTION__);
+            exit(1);
+        }
+        int64_t bad_row = -1;
+        int bad_col = -1;
+        const int64_t R = parse_rows_parallel(buf, std::min(buf.size(), e + 1), num_vars, columns,
+                                              vars_possible_values_ids, &bad_row, &bad_col);
+        if (R == -1) {
+            fprintf(stderr, "Error in function %s!\nRow %lld has fewer than %d fields.", __FUNCTION__,
+                    (long long)bad_row + 2, num_vars);
+            exit(1);
+        }
+        if (R == -2) {
+            fprintf(stderr, "Error in function %s!\nVariable %s has more than 255 states; the GPU engine "
+                    "stores states as uint8.", __FUNCTION__, vec_var_names[bad_col].c_str());
+            exit(1);
+        }
+        num_instance = (int)R;
+        num_of_possible_values_of_disc_vars.resize(num_vars);
+        for (int v = 0; v < num_vars; ++v)
+            num_of_possible_values_of_disc_vars[v] = (int)vars_possible_values_ids[v].size();
+        cout << "Finish loading training data. Number of instances: " << num_instance
+             << ". Number of variables: " << num_vars << "." << endl;
+        return;
+    }
     std::ifstream in(data_file_path);
     if (!in.is_open()) {
         fprintf(stderr, "Error in function %s!", __FUNCTION__);

@@ -209,3 +209,59 @@ def test_shd_matches_reference_comparison(tmp_path):
         else:
             cols, cd = O.relabel(raw)
         assert F.shd_bif(bif, cols.shape[0], _learned_edges(cols, cd)) == ref
+
+
+_LOADER = r"""
+#include <cstdio>
+#include "fastpgm_gb300_cxx.h"
+int main(int argc, char **argv) {
+    Dataset d;
+    d.LoadCSVTrainingData(argv[1], true, 0);
+    FILE *f = fopen(argv[2], "wb");
+    fprintf(f, "%d %d\n", d.num_vars, d.num_instance);
+    for (auto &n : d.vec_var_names) fprintf(f, "%s\n", n.c_str());
+    for (int c : d.num_of_possible_values_of_disc_vars) fprintf(f, "%d\n", c);
+    fwrite(d.columns.data(), 1, d.columns.size(), f);
+    fclose(f);
+    return 0;
+}
+"""
+
+
+def test_parallel_csv_loader_matches_first_appearance_ids(tmp_path):
+    """The C++ drop-in Dataset::LoadCSVTrainingData (parallel parse) gives the reference's
+    first-appearance ids and cardinalities: string values, CRLF line ends, blank lines,
+    values whose first appearance falls late in the file (other threads' rows)."""
+    rng = np.random.default_rng(3)
+    n, S = 7, 20000
+    vals = [["a", "bb", "c c", "-1"], ["x"], ["0", "1"], ["u%d" % k for k in range(40)], ["p", "q", "r"],
+            ["7", "8"], ["late", "early"]]
+    cols = []
+    for v in range(n):
+        idx = rng.integers(0, len(vals[v]), S)
+        cols.append([vals[v][i] for i in idx])
+    cols[6] = ["early"] * (S - 3) + ["late"] * 3  # second value first appears at the end
+    path = tmp_path / "d.csv"
+    with open(path, "w", newline="") as f:
+        f.write(",".join("N%d" % v for v in range(n)) + "\r\n")
+        for s in range(S):
+            f.write(",".join(cols[v][s] for v in range(n)) + ("\r\n" if s % 3 else "  \n"))
+            if s % 5000 == 0:
+                f.write("\n")
+    names, ref_cols, ref_card = O.read_csv_columns(str(path))
+    src = tmp_path / "load.cpp"
+    src.write_text(_LOADER)
+    exe = str(tmp_path / "load")
+    libdir = os.path.dirname(F.LIB_PATH)
+    subprocess.run(["g++", "-O1", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", exe, "-L",
+                    libdir, "-lfastpgm_gb300", "-Wl,-rpath," + libdir], check=True)
+    out = tmp_path / "out.bin"
+    subprocess.run([exe, str(path), str(out)], check=True, capture_output=True)
+    data = out.read_bytes()
+    lines = data.split(b"\n", 1 + 2 * n)
+    nv, ni = map(int, lines[0].split())
+    assert (nv, ni) == (n, S)
+    assert [l.decode() for l in lines[1:1 + n]] == names
+    assert [int(l) for l in lines[1 + n:1 + 2 * n]] == list(ref_card)
+    got = np.frombuffer(lines[-1], dtype=np.uint8).reshape(n, S)
+    assert np.array_equal(got, ref_cols)
