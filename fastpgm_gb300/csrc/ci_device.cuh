@@ -96,16 +96,34 @@ constexpr double kWhMargin = 1e-5;
 
 // G^2 at which the p-value of df degrees of freedom equals target (bisection;
 // p is decreasing in G^2).  Returns 0 for target >= 1 and +inf for target <= 0.
+// x with P(chi2_df > x) = target, to 1e-10 relative: Newton's method on the upper tail
+// (derivative -pdf) from the Wilson-Hilferty estimate, kept inside a bisection bracket
+// (a step leaving the bracket bisects instead).
 __host__ __device__ inline double chisq_quantile_upper(double target, long long df) {
     if (target >= 1.0) return 0.0;
     if (target <= 0.0) return 1e300;
     double lo = 0.0, hi = (double)df + 10.0 * sqrt(2.0 * (double)df) + 50.0;
     while (chisq_pvalue(hi, df) > target) hi *= 2.0;
-    for (int it = 0; it < 200 && hi - lo > 1e-10 * hi; ++it) {
-        double mid = 0.5 * (lo + hi);
-        if (chisq_pvalue(mid, df) > target) lo = mid; else hi = mid;
+    double x = 0.5 * (lo + hi);
+#ifdef __CUDA_ARCH__
+    {  // Wilson-Hilferty: chi2_k ~ k (1 - 2/(9k) + z sqrt(2/(9k)))^3, z the normal upper quantile
+        const double z = normcdfinv(1.0 - target), c = 2.0 / (9.0 * (double)df);
+        const double w = 1.0 - c + z * sqrt(c);
+        const double x0 = (double)df * w * w * w;
+        if (x0 > lo && x0 < hi) x = x0;
     }
-    return 0.5 * (lo + hi);
+#endif
+    for (int it = 0; it < 200; ++it) {
+        const double p = chisq_pvalue(x, df);
+        if (p > target) lo = x; else hi = x;
+        if (hi - lo <= 1e-10 * hi) return 0.5 * (lo + hi);
+        const double d = chisq_pdf(x, df);
+        double xn = d > 0.0 ? x + (p - target) / d : 0.5 * (lo + hi);
+        if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
+        if (fabs(xn - x) <= 1e-11 * x) return xn;
+        x = xn;
+    }
+    return x;
 }
 
 struct BandTables {
