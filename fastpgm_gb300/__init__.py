@@ -22,7 +22,7 @@ FPGM_MODE_PLAIN = 1
 MAX_COND = 30
 
 EXPORTED = ["fpgm_last_error", "fpgm_engine_create", "fpgm_engine_destroy", "fpgm_dataset_upload",
-            "fpgm_dataset_upload_jobs", "fpgm_mle_cpts", "fpgm_shd_bif",
+            "fpgm_dataset_upload_jobs", "fpgm_mle_cpts", "fpgm_shd_bif", "fpgm_bnl_pcstable",
             "fpgm_dataset_download", "fpgm_ci_test", "fpgm_ci_test_batch", "fpgm_pc_skeleton",
             "fpgm_pc_result_sizes", "fpgm_pc_result_fetch", "fpgm_orient_cpdag", "fpgm_write_struct",
             "fpgm_bnsl_pcstable", "fpgm_generate_network", "fpgm_write_csv", "fpgm_ci_test_noalloc"]
@@ -89,6 +89,8 @@ def load():
     L.fpgm_engine_create.argtypes = [ctypes.c_int32, ctypes.POINTER(vp)]
     L.fpgm_engine_destroy.argtypes = [vp]
     L.fpgm_dataset_upload.argtypes = [vp, u8p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, u8p]
+    L.fpgm_bnl_pcstable.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_char_p,
+                                    ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32]
     L.fpgm_shd_bif.argtypes = [ctypes.c_char_p, ctypes.c_int32, i32p, ctypes.c_int32, i32p]
     L.fpgm_mle_cpts.argtypes = [vp, i32p, i32p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
                                 ctypes.POINTER(ctypes.c_double)]
@@ -292,6 +294,11 @@ def shd_bif(bif_path, n_nodes, edges):
     out = ctypes.c_int32()
     _check(load().fpgm_shd_bif(bif_path.encode(), int(n_nodes), _i32(flat), len(edges), ctypes.byref(out)))
     return out.value
+
+
+def bnl_pcstable(verbose, n_threads, group_size, alpha, ref_net, train_set, save_struct, save_param):
+    _check(load().fpgm_bnl_pcstable(verbose, n_threads, group_size, alpha, ref_net.encode(), train_set.encode(),
+                                    int(bool(save_struct)), int(bool(save_param))))
 
 
 def write_csv(path, columns, prefix="V"):

@@ -7,8 +7,9 @@
 //
 // A relative -f1/-f2 path is taken under the dataset root, like the reference:
 // $FASTPGM_DATASET_DIR if set, else ./dataset/ ; a path that exists as given is used as is.
-// Other jobs of the reference (-j 1..5: parameter learning, inference, ...) are
-// not part of this engine and exit with a message.
+// -j 1 -m 0 (PC-stable + maximum likelihood parameters, -sp 0|1) is provided too.  Other
+// jobs of the reference (-j 2..5: inference, ...) are not part of this engine and exit with
+// a message.
 #include <cstdio>
 #include <cstdlib>
 #include <iostream>
@@ -25,7 +26,7 @@ namespace {
 struct Parameter {  // defaults of Parameter.cpp:6-37 that the structure-learning job reads
     int job = 0, method = 0, num_threads = 1, verbose = 1, group_size = 1, engine = 0;
     double alpha = 0.05;
-    bool save_struct = true;
+    bool save_struct = true, save_param = true;
     string ref_net_file, train_set_file = "alarm/alarm_s5000";
 };
 
@@ -66,7 +67,7 @@ void parse(Parameter &p, int argc, char **argv) {
             case 's':
                 switch (argv[i][2]) {
                     case 's': if (atoi(need()) == 0) p.save_struct = false; break;
-                    case 'p': need(); break;
+                    case 'p': if (atoi(need()) == 0) p.save_param = false; break;
                 }
                 [[fallthrough]];  // as the reference's switch does
             case 'f':
@@ -100,9 +101,27 @@ string resolve(const string &f) {
 int main(int argc, char **argv) {
     Parameter p;
     parse(p, argc, argv);
-    if (p.job != 0) {
-        cout << "\tError! Only -j 0 (PC-stable structure learning) is provided by the GPU engine" << endl;
+    if (p.job != 0 && p.job != 1) {
+        cout << "\tError! Only -j 0 (PC-stable structure learning) and -j 1 (PC-stable + maximum likelihood "
+                "estimation) are provided by the GPU engine" << endl;
         exit(1);
+    }
+    if (p.job == 1) {  // main.cpp:66-89
+        if (p.method != 0) {
+            cout << "\tError! We currently only support -a 0 for PC-Stable structure learning + "
+                    "maximum likelihood estimation parameter learning" << endl;
+            exit(1);
+        }
+        cout << "==================================================" << endl
+             << "Job: PC-stable + maximum likelihood estimation for learning, #threads = " << p.num_threads << endl
+             << "\tgroup size = " << p.group_size << endl
+             << "\treference BN: " << p.ref_net_file << endl
+             << "\tsample set: " << p.train_set_file << endl
+             << "==================================================" << endl;
+        const string ref = p.ref_net_file.empty() ? string() : resolve(p.ref_net_file);
+        BNL_PCStable(p.verbose, p.num_threads, p.group_size, p.alpha, ref, resolve(p.train_set_file), p.save_struct,
+                     p.save_param);
+        return 0;
     }
     if (p.method != 0) {
         cout << "\tError! We currently only support -a 0 for PC-Stable structure learning" << endl;

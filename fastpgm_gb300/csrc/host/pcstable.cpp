@@ -571,7 +571,7 @@ void PCStable::StructLearnCompData(Dataset *dts, int group_size, int num_threads
 // ------------------------------------------------------------------ job API
 namespace {
 int bnsl_impl(int verbose, int n_threads, int group_size, double alpha, const string &ref_net, const string &train_set,
-              bool save_struct) {
+              bool save_struct, bool learn_params = false, bool save_param = false) {
     Dataset *trainer = new Dataset();
     trainer->LoadCSVTrainingData(train_set, true, 0);
     Network *network = new Network(true);
@@ -582,7 +582,6 @@ int bnsl_impl(int verbose, int n_threads, int group_size, double alpha, const st
         cout << "--------------------------------------------------\n"
              << "Structure learning with PC-Stable..." << endl;
     int rc = bnsl->Run(trainer, false, false, save_struct, train_set + "_struct", verbose);
-    delete trainer;
     if (rc == FPGM_OK) {
         if (!ref_net.empty()) {  // fastpgm_api.cpp:32-38: LoadBIFFile + BNSLComparison::GetSHD
             vector<int32_t> edges;
@@ -601,12 +600,29 @@ int bnsl_impl(int verbose, int n_threads, int group_size, double alpha, const st
                  << endl;
         }
     }
+    if (rc == FPGM_OK && learn_params) {  // fastpgm_api.cpp:70-71: MLE on the learned graph, alpha 1
+        ParameterLearning bnpl(network);
+        bnpl.LearnParamsKnowStructCompData(trainer, 1, save_param, train_set + "_param", verbose);
+    }
+    delete trainer;
     bnsl->network = nullptr;  // the reference deletes the network itself and never deletes bnsl
     delete network;
     delete bnsl;
     return rc;
 }
 }  // namespace
+
+void BNL_PCStable(int verbose, int n_threads, int group_size, double alpha, string ref_net, string train_set,
+                  bool save_struct, bool save_param) {  // fastpgm_api.cpp:46-75
+    die_on(bnsl_impl(verbose, n_threads, group_size, alpha, ref_net, train_set, save_struct, true, save_param));
+}
+
+extern "C" int fpgm_bnl_pcstable(int32_t verbose, int32_t n_threads, int32_t group_size, double alpha,
+                                 const char *ref_net, const char *train_set, int32_t save_struct, int32_t save_param) {
+    if (!train_set) return fpgm::set_error(FPGM_ERR_INVALID, "fpgm_bnl_pcstable: NULL train_set");
+    return bnsl_impl(verbose, n_threads, group_size, alpha, ref_net ? ref_net : "", train_set, save_struct != 0, true,
+                     save_param != 0);
+}
 
 void BNSL_PCStable(int verbose, int n_threads, int group_size, double alpha, string ref_net, string train_set,
                    bool save_struct) {

@@ -220,6 +220,11 @@ int fpgm_write_struct(const char *path, int32_t n, const char *const *names, con
 /* ---- drop-in job ---- */
 int fpgm_bnsl_pcstable(int32_t verbose, int32_t n_threads, int32_t group_size, double alpha,
                        const char *ref_net, const char *train_set, int32_t save_struct);
+/* BNL_PCStable (fastpgm_api.cpp:46-75, the command line's -j 1 -m 0): as fpgm_bnsl_pcstable,
+ * then maximum-likelihood parameters (Laplace alpha 1) for the learned graph's arcs, written to
+ * train_set + "_param" when save_param (ParameterLearning::SaveBNParameter's format). */
+int fpgm_bnl_pcstable(int32_t verbose, int32_t n_threads, int32_t group_size, double alpha, const char *ref_net,
+                      const char *train_set, int32_t save_struct, int32_t save_param);
 
 /* ---- seeded synthetic data ---- */
 int fpgm_generate_network(const fpgm_gen_spec *spec, uint8_t *out_columns, uint8_t *out_card,

@@ -191,6 +191,11 @@ public:
     void SaveBNParameter(std::string param_file);
 };
 
+// fastpgm_api.cpp:46-75: PC-stable, the SHD report, then maximum-likelihood parameters
+// (Laplace alpha 1) for the learned graph, written to train_set + "_param" when save_param.
+void BNL_PCStable(int verbose, int n_threads, int group_size, double alpha, std::string ref_net,
+                  std::string train_set, bool save_struct, bool save_param);
+
 // fastpgm_api.cpp:18-44
 void BNSL_PCStable(int verbose, int n_threads, int group_size, double alpha, std::string ref_net,
                    std::string train_set, bool save_struct);

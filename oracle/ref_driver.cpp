@@ -22,6 +22,7 @@
 //       follow IndependenceTest.cpp:94-138 on that table.
 //
 //   ref_driver shd <csv> <alpha> <bif>     (see run_shd)
+//   ref_driver bnl <csv> <alpha> <prefix>  (see run_bnl)
 //
 //   ref_driver mle <csv> <alpha> <edges_in> <out> [param_file]
 //       Builds the network's nodes from the dataset as StructureLearning::AssignNodeInformation
@@ -104,6 +105,22 @@ static int run_shd(int argc, char **argv) {
     r_net->LoadBIFFile(argv[4]);
     BNSLComparison comp(r_net, net);
     printf("SHD = %d\n", comp.GetSHD());
+    return 0;
+}
+
+// ref_driver bnl <csv> <alpha> <out_prefix>: BNL_PCStable without a reference network
+// (fastpgm_api.cpp:46-75): PC-stable (one thread) writing <out_prefix>_struct, then
+// ParameterLearning with Laplace alpha 1 on the learned graph writing <out_prefix>_param.
+static int run_bnl(int argc, char **argv) {
+    if (argc < 5) { fprintf(stderr, "bnl: bad args\n"); return 2; }
+    Dataset *d = new Dataset();
+    d->LoadCSVTrainingData(argv[2], true, 0);
+    Network *net = new Network(true);
+    PCStable *pc = new PCStable(net, atof(argv[3]), 1000);
+    const std::string prefix = argv[4];
+    pc->StructLearnCompData(d, 1, 1, false, false, true, prefix + "_struct", 0);
+    ParameterLearning *pl = new ParameterLearning(net);
+    pl->LearnParamsKnowStructCompData(d, 1, true, prefix + "_param", 0);
     return 0;
 }
 
@@ -226,6 +243,7 @@ int main(int argc, char **argv) {
     std::string mode = argv[1];
     if (mode == "mle") return run_mle(argc, argv);
     if (mode == "shd") return run_shd(argc, argv);
+    if (mode == "bnl") return run_bnl(argc, argv);
     if (mode == "pc") return run_pc(argc, argv);
     if (mode == "tests") return run_tests(argc, argv);
     fprintf(stderr, "unknown mode %s\n", mode.c_str());

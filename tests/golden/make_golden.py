@@ -15,6 +15,8 @@ driver (oracle/Makefile `ref` target).  Writes, under tests/golden/:
   c1_dag                 the generating DAG of c1 as "parent child" lines
   c1_param_alpha1        the reference's ParameterLearning (Laplace alpha 1) for that DAG,
                          written by its own SaveBNParameter
+  c1_bnl_param           BNL_PCStable's parameter file on c1: the reference's ParameterLearning
+                         (alpha 1) on the graph its PC-stable learned
 
 Run:  python tests/golden/make_golden.py [--mle-only]
 """
@@ -81,6 +83,9 @@ def mle_golden():
         import subprocess
         subprocess.check_call([O.REF_DRIVER, "mle", csv, "1", os.path.join(HERE, "c1_dag"), os.path.join(tmp, "o"),
                                os.path.join(HERE, "c1_param_alpha1")], stdout=subprocess.DEVNULL)
+        subprocess.check_call([O.REF_DRIVER, "bnl", csv, "0.05", os.path.join(tmp, "bnl")], stdout=subprocess.DEVNULL)
+        shutil.copyfile(os.path.join(tmp, "bnl_param"), os.path.join(HERE, "c1_bnl_param"))
+        assert open(os.path.join(tmp, "bnl_struct")).read() == open(os.path.join(HERE, "c1_struct")).read()
     finally:
         shutil.rmtree(tmp)
 

@@ -159,3 +159,21 @@ def test_tests_across_datasets_are_rejected(eng):
         eng.ci_test(0, n0, ())
     with pytest.raises(F.FpgmError, match="mixes datasets"):
         eng.ci_test_batch(np.array([[0, 1, n0]], dtype=np.int32), 1)
+
+
+def test_learning_job_reproduces_reference_files(tmp_path):
+    """-j 1 -m 0 (BNL_PCStable): the learned CPDAG and the parameter file of the reference's own
+    PC-stable + ParameterLearning run on c1 (tests/golden/c1_struct, c1_bnl_param), through
+    the command line and through the Python binding."""
+    raw, _, _ = F.make_config("c1")
+    csv = str(tmp_path / "c1.csv")
+    F.write_csv(csv, raw)
+    out = subprocess.run([F.CLI_PATH, "-j", "1", "-m", "0", "-f2", csv, "-sp", "1"], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert open(csv + "_struct").read() == open(os.path.join(GOLDEN, "c1_struct")).read()
+    golden = open(os.path.join(GOLDEN, "c1_bnl_param")).read()
+    assert open(csv + "_param").read() == golden
+    os.remove(csv + "_param")
+    from fastpgm_gb300 import cmake_example as fastpgm
+    fastpgm.BNL_PCStable(0, 1, 1, 0.05, "", csv, True, True)
+    assert open(csv + "_param").read() == golden

@@ -129,7 +129,7 @@ def test_cli_help_and_rejected_jobs():
     out = subprocess.run([F.CLI_PATH, "-h"], capture_output=True, text=True)
     assert out.returncode == 0 and "-j & -m" in out.stdout
     out = subprocess.run([F.CLI_PATH, "-j", "2", "-m", "0"], capture_output=True, text=True)
-    assert out.returncode == 1 and "Only -j 0" in out.stdout
+    assert out.returncode == 1 and "Only -j 0" in out.stdout and "-j 1" in out.stdout
     out = subprocess.run([F.CLI_PATH, "-v", "1"], capture_output=True, text=True)
     assert "Unrecognized option -v" in out.stdout  # the reference does not parse -v either
 
