@@ -802,7 +802,7 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
     for (int v = 0; v < n; ++v) max_deg = std::max(max_deg, e->h_var_hi[v] - e->h_var_lo[v] - 1);
     bool more = true;
     st->n_levels = 0;
-    for (int d = 0; d < depth && d < 64; ++d) {
+    for (int d = 0; (d == 0 || d < depth) && d < 64; ++d) {  // level 0 always runs (PCStable.cpp:133-177)
         if (d >= 2 && !more) break;
         auto t0 = std::chrono::steady_clock::now();
         if (d > kMaxCond)

@@ -177,3 +177,34 @@ def test_learning_job_reproduces_reference_files(tmp_path):
     from fastpgm_gb300 import cmake_example as fastpgm
     fastpgm.BNL_PCStable(0, 1, 1, 0.05, "", csv, True, True)
     assert open(csv + "_param").read() == golden
+
+
+@pytest.mark.parametrize("alpha,depth,n,S", [(0.0, 1000, 12, 3000), (1.0, 1000, 12, 3000), (0.05, 0, 12, 3000),
+                                             (0.05, 1, 12, 3000), (0.05, 1000, 2, 500), (0.05, 1000, 6, 1),
+                                             (0.05, 1000, 9, 17)])
+def test_edge_cases_match_oracle(eng, alpha, depth, n, S):
+    """alpha 0 and 1, depth 0 and 1, two variables, one sample, a ragged 17 samples."""
+    raw, _, _ = F.generate(n_nodes=n, n_samples=S, seed=21 + n + S, n_edges=max(1, n - 1),
+                           max_indegree=min(3, n - 1), card=(2, 4))
+    cols, card = O.relabel(raw)
+    eng.upload(raw)
+    st = eng.pc_skeleton(alpha=alpha, depth=depth).to_dict()
+    res = eng.result()
+    ref = O.pc_skeleton(cols, card, alpha=alpha, depth=depth, threads=4)
+    assert np.array_equal(res["adj"], ref["adj"])
+    assert res["sepsets"] == ref["sepsets"]
+    assert st["tests"] == ref["stats"]["tests"]
+
+
+def test_constant_column_in_skeleton(eng):
+    """A variable with a single observed state is independent of everything (df 0)."""
+    raw, _, _ = F.generate(n_nodes=10, n_samples=4000, seed=33, n_edges=12, max_indegree=3, card=(2, 4))
+    raw[4, :] = 7
+    cols, card = O.relabel(raw)
+    eng.upload(raw)
+    st = eng.pc_skeleton().to_dict()
+    res = eng.result()
+    ref = O.pc_skeleton(cols, card, threads=4)
+    assert not res["adj"][4].any()
+    assert np.array_equal(res["adj"], ref["adj"]) and res["sepsets"] == ref["sepsets"]
+    assert st["tests"] == ref["stats"]["tests"]
