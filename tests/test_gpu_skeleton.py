@@ -208,3 +208,69 @@ def test_constant_column_in_skeleton(eng):
     assert not res["adj"][4].any()
     assert np.array_equal(res["adj"], ref["adj"]) and res["sepsets"] == ref["sepsets"]
     assert st["tests"] == ref["stats"]["tests"]
+
+
+_DAG_PROGRAM = r"""
+#include <cstdio>
+#include <cstdlib>
+#include "fastpgm_gb300_cxx.h"
+int main(int argc, char **argv) {
+    Dataset *d = new Dataset();
+    d->LoadCSVTrainingData(argv[1], true, 0);
+    Network *net = new Network(true);
+    PCStable *pc = new PCStable(net, 0.05);
+    pc->StructLearnCompData(d, 1, 1, true, atoi(argv[2]) != 0, false, "", 0);
+    printf("nodes %d\n", net->num_nodes);
+    for (auto &e : net->vec_edges)
+        printf("%d %d %d\n", e.node1->GetNodeIndex(), e.node2->GetNodeIndex(), e.end_point2 == ARROW ? 1 : 0);
+    return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("add_root", [0, 1])
+def test_cxx_dag_and_root_options(tmp_path, add_root):
+    """StructLearnCompData(dag=true) directs the undirected records that lead the edge list
+    (randomly, as the reference's DirectLeftEdges does, stopping at the first directed record)
+    so the graph is acyclic over the learned skeleton; add_root adds a ROOT node as the parent
+    of each connected sub-graph's root (StructureLearning.cpp:110-240)."""
+    raw, _, _ = F.make_config("c1")
+    csv = str(tmp_path / "c1.csv")
+    F.write_csv(csv, raw)
+    src = tmp_path / "dag.cpp"
+    src.write_text(_DAG_PROGRAM)
+    exe = str(tmp_path / "dag")
+    libdir = os.path.dirname(F.LIB_PATH)
+    from conftest import ROOT
+    subprocess.run(["g++", "-O1", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", exe, "-L",
+                    libdir, "-lfastpgm_gb300", "-Wl,-rpath," + libdir], check=True)
+    out = subprocess.run([exe, csv, str(add_root)], capture_output=True, text=True, check=True).stdout.splitlines()
+    n = int([l for l in out if l.startswith("nodes")][0].split()[1])
+    edges = [tuple(map(int, l.split())) for l in out if l and l[0].isdigit()]
+    assert edges[0][2] == 1  # no undirected record leads any more
+    n0 = raw.shape[0]
+    cols, card = O.relabel(raw)
+    ref = O.pc_skeleton(cols, card, threads=4)
+    skel = {(min(a, b), max(a, b)) for a, b, _ in edges if a < n0 and b < n0}
+    assert skel == {(i, j) for i in range(n0) for j in range(i + 1, n0) if ref["adj"][i, j]}
+    # acyclic: Kahn's algorithm consumes every node
+    import collections
+    arcs = {(a, b) for a, b, d in edges if d == 1}
+    indeg = collections.Counter(b for _, b in arcs)
+    children = collections.defaultdict(list)
+    for a, b in arcs:
+        children[a].append(b)
+    ready = [v for v in range(n) if indeg[v] == 0]
+    seen = 0
+    while ready:
+        v = ready.pop()
+        seen += 1
+        for c in children[v]:
+            indeg[c] -= 1
+            if indeg[c] == 0:
+                ready.append(c)
+    assert seen == n
+    if add_root:
+        assert n == n0 + 1 and any(a == n0 for a, _, _ in edges)
+    else:
+        assert n == n0
