@@ -22,7 +22,9 @@
 namespace fpgm {
 
 // counters[] slots (int32)
-enum { C_TIER0 = 0, C_TIER1, C_TIER2, C_WORK0, C_WORK1, C_WORK2, C_COUNT };
+// C_PART / C_RETRY: tier-2 tests handed to the partitioned kernel, and from it back to the
+// compact kernel's global hash (lists 3-4 and 5 of WaveArgs::lists)
+enum { C_TIER0 = 0, C_TIER1, C_TIER2, C_WORK0, C_WORK1, C_WORK2, C_PART, C_WORKP, C_RETRY, C_WORKR, C_COUNT };
 // stats[] slots (unsigned long long)
 enum { ST_RECHECK = 0, ST_NEARTIE, ST_LARGE, ST_MAXDP, ST_UNSUPPORTED, ST_DET, ST_EXEC, ST_UNRESOLVED,
        ST_REMOVED, ST_MAXDEG, ST_TIER0, ST_TIER1, ST_TIER2, ST_BYTES_SHARED, ST_BYTES_LARGE, ST_COUNT };
@@ -49,7 +51,8 @@ struct WaveArgs {
     int32_t n_tests;
     // classified items
     uint16_t *item_vars;   // [T][2+d], Horner order: z1..zd, x, y
-    int32_t *lists;        // 3 lists of list_cap items
+    int32_t *lists;        // 6 lists of list_cap entries: tiers 0-2, partitioned items + their
+                           // strata estimates (float bits), items retried on the global hash
     int64_t list_cap;
     // outputs
     uint8_t *flag;         // 1 independent, 0 dependent, 2 unsupported
@@ -65,6 +68,7 @@ struct WaveArgs {
     int64_t slot_S;           // sample count the slot layout was made for (>= S)
     int32_t hash_cap_global;  // power of two >= 2 * slot_S
     unsigned long long *dbg;  // compact-tier phase timers (FPGM_PHASE_TIMERS), else null
+    int32_t part_max_log;     // partitioned kernel: at most 2^part_max_log partitions (<= kPartMaxLog)
 };
 
 __device__ inline int upper_bound_i32(const int32_t *a, int n, int v) {
@@ -450,7 +454,7 @@ __host__ __device__ inline SlotLayout slot_layout(int64_t S, int64_t cap) {
     L.cur = o;  o = align256(o + (S + 1) * 4);    // scatter cursors (overflow path)
     L.sid = o;  o = align256(o + (S + 16) * 4);   // slot, then stratum id, per sample
     L.wt = o;   o = align256(o + (int64_t)kWarps * kGlobalWarpTab * 4);  // wide x,y tables, kept zeroed
-    L.ord = o;  o = align256(o + S * 2);          // (x << 8) | y codes sorted by stratum
+    L.ord = o;  o = align256(o + (S + 2048) * 2);  // (x << 8) | y codes sorted by stratum (+ partition padding)
     L.tab = o;  o = align256(o + ((int64_t)kDenseMul * S + 64) * 4);  // dense strata x cells counts, kept zeroed
     L.total = o;
     return L;
@@ -528,6 +532,7 @@ __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gor
     TermAcc<kFp64> ta;
     for (int k = threadIdx.x; k < n_obs; k += kThreads) {
         const int o0 = cnt[k], m = cnt[k + 1] - o0;
+        if (m <= 1 && !want_hash) continue;  // one sample: no G^2 term, no degree of freedom
         if (m > kLaneStratum) {
             if (collect) big[atomicAdd(n_big, 1)] = k;
             continue;
@@ -750,6 +755,360 @@ __device__ __forceinline__ unsigned long long gtimer() {
     return t;
 }
 
+// ---------------------------------------------------------------- tier 2, partitioned strata
+// Tests whose strata overflow the shared hash are split into P = 2^lp partitions by the top
+// lp bits of the mixed stratum code z * 2^64/phi, so a stratum never spans two partitions.
+// One pass writes every sample once as a record (stratum code, (x << 8) | y) to its
+// partition's run in the CTA's slot; each partition is then counted and scored in shared
+// memory alone:
+//   pass 1  the partition's codes are hashed to slots (next bits of the mixed code); a new
+//           code appends its slot to occ[] (stratum i = occ[i]) and every slot counts its
+//           samples in A[slot];
+//   index   A[occ[i]] becomes i, and E[1 + i] its count, scanned to its first sorted position;
+//   pass 2  every record is found again and its (x << 8) | y code placed at its stratum's
+//           cursor E[1 + i], so afterwards stratum i's samples are ord[E[i] .. E[i + 1]);
+//   score   score_small_strata / score_big_strata over the strata.
+// No global hash, no per-sample id array and no global scatter of the sorted codes (unless a
+// partition holds more samples than the shared sorted array).
+// Shared-memory plan (kSmemBytes, PartPlan<K>): keys K[cap] at 0 and A int[cap] after them
+// (per-warp x,y tables once pass 2 is done), occ int[lim], E int[lim + 1], sorted codes u16[].
+constexpr int kPartMaxLog = 8;                     // at most 256 partitions
+constexpr int kPartMax = 1 << kPartMaxLog;
+constexpr int kPartProbe = 256;                   // probe bound of the first pass
+// Tests of fewer samples keep the compact kernel's global hash: measured on GB300, the
+// partitioned path wins at 100,000 samples (1,041 nodes, cards 2-21: 3.85 vs 3.40 M tests/s)
+// and loses at 50,000 (100 nodes, cards 2-5: 12.2 vs 13.4 M), where the global hash and the
+// dense strata table mostly stay in L2.
+constexpr int64_t kPartMinSamples = 65536;
+template <class K>
+struct PartPlan {
+    static constexpr int cap = sizeof(K) == 4 ? 4096 : 2048;  // slots per partition table
+    static constexpr int lcap = sizeof(K) == 4 ? 12 : 11;
+    static constexpr int lim = cap * 3 / 4;                   // strata per partition at most
+    static constexpr int a_off = cap * (int)sizeof(K);
+    static constexpr int occ_off = a_off + cap * 4;
+    static constexpr int e_off = occ_off + lim * 4;
+    static constexpr int ord_off = (e_off + (lim + 1) * 4 + 15) / 16 * 16;
+    static constexpr int ord_cap = (kSmemBytes - ord_off) / 2;  // sorted codes kept in shared memory
+    static constexpr int wtab = occ_off / 4 / kWarps;            // ints per warp over keys + A
+};
+static_assert(PartPlan<uint32_t>::ord_cap > 8192 && PartPlan<uint64_t>::ord_cap > 8192, "partition shared plan");
+static_assert((1 << PartPlan<uint32_t>::lcap) == PartPlan<uint32_t>::cap, "cap");
+static_assert((1 << PartPlan<uint64_t>::lcap) == PartPlan<uint64_t>::cap, "cap");
+static_assert(8 * kPartMax <= 2048, "partition padding fits the slot's sorted-code region");
+static_assert(PartPlan<uint32_t>::lim <= kPartMinSamples, "stratum-indexed codes fit the zk region");
+
+__device__ __forceinline__ uint64_t zmix(uint64_t z) { return z * 0x9E3779B97F4A7C15ull; }
+__device__ __forceinline__ int part_of(uint64_t z, int lp) { return (int)(zmix(z) >> (64 - lp)); }  // lp >= 1
+__device__ __forceinline__ uint32_t part_slot(uint64_t z, int lp, int lc) {
+    return (uint32_t)((zmix(z) << lp) >> (64 - lc));
+}
+
+// Slot of code z, probing from slot h (claimed when absent: the slot is appended to occ[]);
+// -1 after max_probe probes or beyond lim strata.
+template <class K>
+__device__ __forceinline__ int part_insert(K *keys, uint32_t cap, uint32_t h, K z, int max_probe, int *occ,
+                                           int *n_occ, int lim) {
+    const K empty = (K)kEmptyKey;
+    for (int p = 0; p < max_probe; ++p) {
+        const K k = keys[h];
+        if (k == z) return (int)h;
+        if (k == empty) {
+            const K old = key_cas(&keys[h], empty, z);
+            if (old == empty) {
+                const int i = atomicAdd(n_occ, 1);
+                if (i >= lim) return -1;
+                occ[i] = (int)h;
+                return (int)h;
+            }
+            if (old == z) return (int)h;
+        }
+        h = (h + 1) & (cap - 1);
+    }
+    return -1;
+}
+
+template <class K>
+__device__ __forceinline__ int part_find(const K *keys, uint32_t cap, uint32_t h, K z) {
+    for (uint32_t p = 0; p < cap; ++p) {
+        if (keys[h] == z) return (int)h;
+        h = (h + 1) & (cap - 1);
+    }
+    return 0;  // unreachable: every code was inserted in pass 1
+}
+
+// Eight consecutive records' codes (the run starts on a multiple of 8 records).
+template <class K>
+__device__ __forceinline__ void load8(K (&z)[8], const K *src) {
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    if constexpr (sizeof(K) == 4) {
+        const uint4 w0 = __ldcg(s4), w1 = __ldcg(s4 + 1);
+        z[0] = w0.x; z[1] = w0.y; z[2] = w0.z; z[3] = w0.w;
+        z[4] = w1.x; z[5] = w1.y; z[6] = w1.z; z[7] = w1.w;
+    } else {
+        uint4 w[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) w[i] = __ldcg(s4 + i);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            z[2 * i] = (K)w[i].x | ((K)w[i].y << 32);
+            z[2 * i + 1] = (K)w[i].z | ((K)w[i].w << 32);
+        }
+    }
+}
+
+// Partition histogram, offsets (every run padded to a multiple of 8 records) and the
+// record pass.  s_poff[P] = records written, padding included.
+template <class K>
+__device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint32_t *dim, int d, int64_t S, int lp, K *rec_z,
+                             uint16_t *rec_xy, int *s_pcnt, int *s_poff, int *s_pcur) {
+    const int tid = threadIdx.x, P = 1 << lp;
+    const int64_t nvec = S >> 4;
+    const uint8_t *colx = col[d], *coly = col[d + 1];
+    for (int i = tid; i < P; i += kThreads) s_pcnt[i] = 0;
+    __syncthreads();
+    for (int64_t v = tid; v < nvec; v += kThreads) {
+        uint64_t z[16];
+        zcodes16(z, col, dim, d, v);
+#pragma unroll
+        for (int b = 0; b < 16; ++b) atomicAdd(&s_pcnt[part_of(z[b], lp)], 1);
+    }
+    for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
+        uint64_t z = 0;
+        for (int j = 0; j < d; ++j) z = z * dim[j] + col[j][s];
+        atomicAdd(&s_pcnt[part_of(z, lp)], 1);
+    }
+    __syncthreads();
+    if (tid < 32) {  // padded exclusive scan, eight partitions per lane at most
+        const int per = (P + 31) / 32;
+        int sum = 0;
+        for (int i = 0; i < per; ++i) {
+            const int p = tid * per + i;
+            if (p < P) sum += (s_pcnt[p] + 7) & ~7;
+        }
+        int incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (tid >= o) incl += t;
+        }
+        int run = incl - sum;
+        for (int i = 0; i < per; ++i) {
+            const int p = tid * per + i;
+            if (p < P) {
+                s_poff[p] = run;
+                s_pcur[p] = run;
+                run += (s_pcnt[p] + 7) & ~7;
+            }
+        }
+        if (tid == 31) s_poff[P] = incl;
+    }
+    __syncthreads();
+    for (int64_t v = tid; v < nvec; v += kThreads) {
+        uint64_t z[16];
+        zcodes16(z, col, dim, d, v);
+        const uint4 wx = __ldg(reinterpret_cast<const uint4 *>(colx) + v);
+        const uint4 wy = __ldg(reinterpret_cast<const uint4 *>(coly) + v);
+        const uint32_t xx[4] = {wx.x, wx.y, wx.z, wx.w}, yy[4] = {wy.x, wy.y, wy.z, wy.w};
+#pragma unroll
+        for (int b = 0; b < 16; ++b) {
+            const int pos = atomicAdd(&s_pcur[part_of(z[b], lp)], 1);
+            const int sh = 8 * (b & 3);
+            rec_z[pos] = (K)z[b];
+            rec_xy[pos] = (uint16_t)((((xx[b >> 2] >> sh) & 0xffu) << 8) | ((yy[b >> 2] >> sh) & 0xffu));
+        }
+    }
+    for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
+        uint64_t z = 0;
+        for (int j = 0; j < d; ++j) z = z * dim[j] + col[j][s];
+        const int pos = atomicAdd(&s_pcur[part_of(z, lp)], 1);
+        rec_z[pos] = (K)z;
+        rec_xy[pos] = (uint16_t)((colx[s] << 8) | coly[s]);
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void partial_add(Partial &a, const Partial &b) {
+    a.df += b.df;
+    a.g2 += b.g2;
+    a.err += b.err;
+    a.abs_g2 += b.abs_g2;
+    a.hash += b.hash;
+}
+
+// Counts and scores every partition in shared memory; returns this thread's share of the
+// statistic.  *s_over is set when a partition's codes overflow its table (first pass only:
+// the FP64 recheck probes without bound, so it cannot fail where the first pass did not).
+// Thread 0 adds the strata it saw to claims.
+template <bool kFp64, class K>
+__device__ __noinline__ Partial part_run(int lp, const K *rec_z, const uint16_t *rec_xy, const int *s_pcnt,
+                                         const int *s_poff, int dx, int dy, unsigned char *smem, uint16_t *gord,
+                                         int *gwt, uint64_t *gzk, bool want_hash, int *s_w, int *s_over,
+                                         int *s_nbig, int *s_nocc, int &claims, unsigned long long *dbg) {
+    using Plan = PartPlan<K>;
+    constexpr uint32_t cap = Plan::cap;
+    const int tid = threadIdx.x, warp = tid >> 5, P = 1 << lp;
+    K *keys = reinterpret_cast<K *>(smem);
+    int *A = reinterpret_cast<int *>(smem + Plan::a_off);
+    int *occ = reinterpret_cast<int *>(smem + Plan::occ_off);
+    int *E = reinterpret_cast<int *>(smem + Plan::e_off);
+    uint16_t *sord = reinterpret_cast<uint16_t *>(smem + Plan::ord_off);
+    const int dxy = dx * dy;
+    const bool wsmem = dxy + dx + dy <= Plan::wtab;
+    int *wt = wsmem ? reinterpret_cast<int *>(smem) + warp * Plan::wtab : gwt + (int64_t)warp * kGlobalWarpTab;
+    const int max_probe = kFp64 ? (int)cap : kPartProbe;
+    const int lim = Plan::lim;  // the same strata in both passes: the FP64 one cannot exceed it
+    Partial acc{0, 0.0, 0.0, 0.0, 0ull};
+    // sub-phase timers of thread 0 (FPGM_PHASE_TIMERS): dbg[16..21]
+    unsigned long long tp = (dbg && tid == 0) ? gtimer() : 0ull;
+    auto lap = [&](int i) {
+        if (dbg && tid == 0) {
+            const unsigned long long t = gtimer();
+            atomicAdd(&dbg[i], t - tp);
+            tp = t;
+        }
+    };
+    if (dbg && tid == 0) atomicAdd(&dbg[22], (unsigned long long)P);
+    for (int p = 0; p < P; ++p) {
+        const int n = s_pcnt[p];
+        bool over = false;
+        if (n > 0) {
+            const int base = s_poff[p];
+            for (uint32_t i = tid; i < cap; i += kThreads) {
+                keys[i] = (K)kEmptyKey;
+                A[i] = 0;
+            }
+            if (tid == 0) *s_nocc = 0;
+            __syncthreads();
+            lap(16);
+            // pass 1: first probes of eight codes at once; misses take the inserting path
+            const int ngroups = (n + 7) >> 3;
+            for (int g = tid; g < ngroups; g += kThreads) {
+                K z[8];
+                load8(z, rec_z + base + 8 * g);
+                const int m = n - 8 * g;
+                uint32_t h[8];
+                K k0[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    h[j] = part_slot(z[j], lp, Plan::lcap);
+                    k0[j] = j < m ? keys[h[j]] : z[j];
+                }
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    if (j >= m) break;
+                    int hj = (int)h[j];
+                    if (k0[j] != z[j]) hj = part_insert(keys, cap, h[j], z[j], max_probe, occ, s_nocc, lim);
+                    if (hj < 0) {
+                        *s_over = 1;
+                        break;
+                    }
+                    atomicAdd(&A[hj], 1);
+                }
+            }
+            __syncthreads();
+            lap(17);
+            over = *s_over != 0;
+            if (!over) {
+                const int n_occ = *s_nocc;
+                if (tid == 0) claims += n_occ;
+                // stratum index per slot, counts -> first sorted positions
+                for (int i = tid; i < n_occ; i += kThreads) {
+                    const int sl = occ[i];
+                    E[1 + i] = A[sl];
+                    A[sl] = i;
+                    if (want_hash) gzk[i] = (uint64_t)keys[sl];
+                }
+                if (tid == 0) E[0] = 0;
+                __syncthreads();
+                block_exclusive_scan(E + 1, n_occ, s_w);
+                lap(18);
+                uint16_t *ord = n <= Plan::ord_cap ? sord : gord + base;
+                for (int g = tid; g < ngroups; g += kThreads) {
+                    K z[8];
+                    load8(z, rec_z + base + 8 * g);
+                    const uint4 c = __ldcg(reinterpret_cast<const uint4 *>(rec_xy + base) + g);
+                    const uint32_t cw[4] = {c.x, c.y, c.z, c.w};
+                    const int m = n - 8 * g;
+                    uint32_t h[8];
+                    K k0[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        h[j] = part_slot(z[j], lp, Plan::lcap);
+                        k0[j] = j < m ? keys[h[j]] : z[j];
+                    }
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        if (j >= m) break;
+                        const int hj = k0[j] == z[j] ? (int)h[j] : part_find(keys, cap, h[j], z[j]);
+                        const int pos = atomicAdd(&E[1 + A[hj]], 1);
+                        ord[pos] = (uint16_t)(cw[j >> 1] >> (16 * (j & 1)));
+                    }
+                }
+                __syncthreads();
+                lap(19);
+                if (wsmem)  // keys and A are dead: per-warp x,y tables
+                    for (int i = tid; i < Plan::occ_off / 4; i += kThreads) reinterpret_cast<int *>(smem)[i] = 0;
+                if (tid == 0) *s_nbig = 0;
+                __syncthreads();
+                // the larger strata are listed over occ[] (dead since the index step)
+                Partial q = score_small_strata<kFp64>(E, ord, n_occ, dx, dy, occ, s_nbig, gzk, want_hash, true);
+                __syncthreads();
+                lap(20);
+                const int n_big = *s_nbig;
+                q = score_big_strata<kFp64>(q, E, ord, occ, n_big, dx, dy, wt, gzk, want_hash);
+                partial_add(acc, q);
+            }
+            __syncthreads();  // before the next partition reuses shared memory
+            lap(21);
+        }
+        if (over) break;
+    }
+    return acc;
+}
+
+// FP32 statistic r (block-summed) -> decision: band tables, Wilson-Hilferty beyond them;
+// inside the band the FP64 statistic (recheck() returns each thread's share) decides.
+// Called by every thread of the CTA; thread 0 records the verdict of a tier-2 test (path 2
+// compact strata, 3 partitioned strata).
+template <class Recheck>
+__device__ inline void decide_record(const WaveArgs &a, int item, const Partial &r, int64_t cells, int path,
+                                     int &s_flag, Partial *scratch, Recheck &&recheck) {
+    const int tid = threadIdx.x;
+    const double err = 2.0 * r.err + 1e-6 * r.abs_g2 + 1e-12;
+    int dec = band_decide(r.df, r.g2, err, a.bt);
+    if (dec < 0 && r.df > a.bt.dfmax) {
+        // beyond the tables: Wilson-Hilferty p of the FP32 statistic, widened by its own
+        // error and by the propagated G^2 error (chi-square density <= 0.3/sqrt(df) here)
+        if (tid == 0) {
+            const double pw = chisq_pvalue_wh(r.g2, (double)r.df);
+            const double dist = fabs(pw - a.alpha);
+            const double dpb = 2.0 * err * 0.3 / sqrt((double)r.df);
+            s_flag = (dist > kBand + kWhMargin && dist > dpb + kWhMargin) ? (pw > a.alpha) : -1;
+        }
+        __syncthreads();
+        dec = s_flag;
+    }
+    Verdict v{r.df, r.g2, 1.0, 1, 0, 0.0, r.hash};
+    if (dec < 0) {
+        const Partial r2 = block_sum(recheck(), scratch);
+        v.g2 = r2.g2;
+        v.rechecked = 1;
+        if (tid == 0) {
+            v.p = chisq_pvalue(r2.g2, r.df);
+            v.indep = v.p > a.alpha;
+            v.dp = fabs(v.p - chisq_pvalue(r.g2, r.df));
+        }
+    } else {
+        v.indep = dec;
+        if (tid == 0) v.p = (a.detail != nullptr && r.df > 0) ? chisq_pvalue(r.g2, r.df) : (dec ? 1.0 : 0.0);
+    }
+    if (tid == 0) {
+        atomicAdd(&a.stats[ST_LARGE], 1ull);
+        record(a, item, v, cells, 0, path);
+    }
+}
+
 // Tier 2: joint tables too large for shared memory, counted in O(samples):
 //  1. the observed Z strata are hashed, each new one taking the next id (shared-memory
 //     hash of kZCap32 32-bit or kZCap64 64-bit codes; a global one beyond that);
@@ -763,6 +1122,7 @@ __device__ __forceinline__ unsigned long long gtimer() {
 //     table and reads each touched cell back with atomicExch(.., 0), so every distinct
 //     cell contributes once and the table is left zeroed.  FP32 terms first; the FP64
 //     pass runs only when the decision falls inside the recheck band.
+template <bool kRetry>
 __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t *hkeys = reinterpret_cast<uint64_t *>(smem_raw);
@@ -788,7 +1148,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     int *gwt = reinterpret_cast<int *>(slot + L.wt);
     uint16_t *gord = reinterpret_cast<uint16_t *>(slot + L.ord);
     int *gtab = reinterpret_cast<int *>(slot + L.tab);
-    const int n2 = a.counters[C_TIER2];
+    const int n2 = a.counters[kRetry ? C_RETRY : C_TIER2];
     const int d = a.d, ncols = d + 2;
     uint64_t *zk = a.want_hash ? gzk : nullptr;
     unsigned long long t_prev = 0;
@@ -801,12 +1161,12 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         }                                                               \
     } while (0)
     for (;;) {
-        if (tid == 0) s_idx = atomicAdd(&a.counters[C_WORK2], 1);
+        if (tid == 0) s_idx = atomicAdd(&a.counters[kRetry ? C_WORKR : C_WORK2], 1);
         __syncthreads();
         const int idx = s_idx;
         if (idx >= n2) break;
         FPGM_PHASE(-1);
-        const int item = a.lists[2 * a.list_cap + idx];
+        const int item = a.lists[(kRetry ? 5 : 2) * a.list_cap + idx];
         const int64_t S = a.var_S[a.item_vars[(int64_t)item * ncols + d]];  // <= the slots' layout size
         const int64_t nvec = S >> 4;
         if (tid < ncols) {
@@ -827,15 +1187,25 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         const int zlimit = code32 ? kZStrata : kZCap64 / 2;
         uint32_t cap = code32 ? (uint32_t)kZCap32 : (uint32_t)kZCap64;
         uint32_t *hkeys32 = reinterpret_cast<uint32_t *>(hkeys);
-        for (int attempt = 0; attempt < 3; ++attempt) {
+        bool deferred = false;  // handed to the partitioned kernel
+        for (int attempt = kRetry ? 2 : 0; attempt < 3; ++attempt) {
             global = attempt >= 1;
             const bool k32 = !global && code32;
             if (attempt == 1) {
                 const double est = (double)zlimit * (double)(nvec > 1 ? nvec : 1) / (double)(seen > 1 ? seen : 1);
+                if (S >= kPartMinSamples) {
+                    if (tid == 0) {
+                        const int q = atomicAdd(&a.counters[C_PART], 1);
+                        a.lists[3 * a.list_cap + q] = item;
+                        a.lists[4 * a.list_cap + q] = __float_as_int((float)est);
+                    }
+                    deferred = true;
+                    break;
+                }
                 cap = 16384u < gcap ? 16384u : gcap;
                 while ((double)cap < 2.0 * est && cap < gcap) cap <<= 1;
             } else if (attempt == 2) {
-                if (cap == gcap) break;  // attempt 1 had the full size already
+                if (cap == gcap && !kRetry) break;  // attempt 1 had the full size already
                 cap = gcap;
             }
             uint64_t *keys = global ? gkeys : hkeys;
@@ -908,8 +1278,8 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             if (!s_over) break;
             __syncthreads();
         }
-        if (s_over) {  // cannot happen with cap >= 2 S; flag instead of guessing
-            if (tid == 0) {
+        if (s_over) {  // deferred, or (cannot happen with cap >= 2 S) flagged instead of guessed
+            if (tid == 0 && !deferred) {
                 a.flag[item] = 2;
                 atomicAdd(&a.stats[ST_UNSUPPORTED], 1ull);
             }
@@ -1037,22 +1407,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             FPGM_PHASE(5);
         }
         const Partial r = block_sum(acc, scratch);
-        const double err = 2.0 * r.err + 1e-6 * r.abs_g2 + 1e-12;
-        int dec = band_decide(r.df, r.g2, err, a.bt);
-        if (dec < 0 && r.df > a.bt.dfmax) {
-            // beyond the tables: Wilson-Hilferty p of the FP32 statistic, widened by its own
-            // error and by the propagated G^2 error (chi-square density <= 0.3/sqrt(df) here)
-            if (tid == 0) {
-                const double pw = chisq_pvalue_wh(r.g2, (double)r.df);
-                const double dist = fabs(pw - a.alpha);
-                const double dpb = 2.0 * err * 0.3 / sqrt((double)r.df);
-                s_flag = (dist > kBand + kWhMargin && dist > dpb + kWhMargin) ? (pw > a.alpha) : -1;
-            }
-            __syncthreads();
-            dec = s_flag;
-        }
-        Verdict v{r.df, r.g2, 1.0, 1, 0, 0.0, r.hash};
-        if (dec < 0) {
+        decide_record(a, item, r, (int64_t)n_obs * dxy, 2, s_flag, scratch, [&]() {
             Partial q;
             if (dense) {
                 q = score_dense_groups<true>(gtab, n_obs, dx, dy, nullptr, false);
@@ -1060,22 +1415,8 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
                 q = score_small_strata<true>(cnt, gord, n_obs, dx, dy, big, nullptr, nullptr, false, false);
                 q = score_big_strata<true>(q, cnt, gord, big, n_big, dx, dy, wt, nullptr, false);
             }
-            const Partial r2 = block_sum(q, scratch);
-            v.g2 = r2.g2;
-            v.rechecked = 1;
-            if (tid == 0) {
-                v.p = chisq_pvalue(r2.g2, r.df);
-                v.indep = v.p > a.alpha;
-                v.dp = fabs(v.p - chisq_pvalue(r.g2, r.df));
-            }
-        } else {
-            v.indep = dec;
-            if (tid == 0) v.p = (a.detail != nullptr && r.df > 0) ? chisq_pvalue(r.g2, r.df) : (dec ? 1.0 : 0.0);
-        }
-        if (tid == 0) {
-            atomicAdd(&a.stats[ST_LARGE], 1ull);
-            record(a, item, v, (int64_t)n_obs * dxy, 0, 2);
-        }
+            return q;
+        });
         if (dense) {  // leave the table zeroed for the next test
             __syncthreads();
             const int64_t ncell = (int64_t)n_obs * dxy;
@@ -1084,6 +1425,121 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             for (int64_t i = (ncell & ~(int64_t)3) + tid; i < ncell; i += kThreads) gtab[i] = 0;
         }
         FPGM_PHASE(6);
+        __syncthreads();
+    }
+#undef FPGM_PHASE
+}
+
+// Tier 2, partitioned: the tests ci_compact_kernel handed over (strata beyond its shared
+// hash, at least kPartMinSamples samples), one CTA per test, in the CTA's own slot.  A test
+// whose partitions overflow is split again with twice the partitions; past
+// 2^part_max_log partitions it goes back to the compact kernel's global hash (retry list,
+// ci_compact_kernel<true>).
+__global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ const uint8_t *s_col[kMaxCols];
+    __shared__ uint32_t s_dim[kMaxCols];
+    __shared__ int s_idx, s_over, s_distinct, s_flag, s_nbig, s_nocc;
+    __shared__ int s_w[kWarps];
+    __shared__ Partial scratch[kWarps];
+    __shared__ int s_pcnt[kPartMax], s_poff[kPartMax + 1], s_pcur[kPartMax];
+    const int tid = threadIdx.x;
+    char *slot = a.slot_mem + (int64_t)blockIdx.x * a.slot_bytes;
+    const SlotLayout L = slot_layout(a.slot_S, (uint32_t)a.hash_cap_global);
+    char *rz = slot + L.keys;  // record codes (u32 or u64), S + padding
+    uint16_t *rxy = reinterpret_cast<uint16_t *>(slot + L.ids);  // record (x << 8) | y
+    uint64_t *gzk = reinterpret_cast<uint64_t *>(slot + L.zk);
+    int *gwt = reinterpret_cast<int *>(slot + L.wt);
+    uint16_t *gord = reinterpret_cast<uint16_t *>(slot + L.ord);
+    uint64_t *zk = a.want_hash ? gzk : nullptr;
+    const int np = a.counters[C_PART];
+    const int d = a.d, ncols = d + 2;
+    unsigned long long t_prev = 0;
+#define FPGM_PHASE(i)                                                   \
+    do {                                                                \
+        if (a.dbg && tid == 0) {                                        \
+            const unsigned long long t_ = gtimer();                     \
+            if ((i) >= 0) atomicAdd(&a.dbg[(i)], t_ - t_prev);          \
+            t_prev = t_;                                                \
+        }                                                               \
+    } while (0)
+    for (;;) {
+        if (tid == 0) s_idx = atomicAdd(&a.counters[C_WORKP], 1);
+        __syncthreads();
+        const int idx = s_idx;
+        if (idx >= np) break;
+        FPGM_PHASE(-1);
+        const int item = a.lists[3 * a.list_cap + idx];
+        const double est = (double)__int_as_float(a.lists[4 * a.list_cap + idx]);
+        const int64_t S = a.var_S[a.item_vars[(int64_t)item * ncols + d]];
+        if (tid < ncols) {
+            const int var = a.item_vars[(int64_t)item * ncols + tid];
+            s_dim[tid] = a.card[var];
+            s_col[tid] = a.cols + a.var_off[var];
+        }
+        __syncthreads();
+        uint64_t dz = 1;
+        for (int j = 0; j < d; ++j) dz *= s_dim[j];
+        const bool code32 = dz <= 0xFFFFFFFFull;
+        const int dx = s_dim[d], dy = s_dim[d + 1];
+        // partitions: about 30% of a partition table's slots (strata are estimated high) and
+        // half the shared sorted array expected per partition
+        const double capmax = code32 ? PartPlan<uint32_t>::cap : PartPlan<uint64_t>::cap;
+        const double ordcap = code32 ? PartPlan<uint32_t>::ord_cap : PartPlan<uint64_t>::ord_cap;
+        int lp = 1;
+        const int maxlog = a.part_max_log;
+        while ((double)(1 << lp) < fmax(est / (0.3 * capmax), (double)S / (0.5 * ordcap)) && lp < maxlog) ++lp;
+        Partial acc;
+        bool over;
+        for (;;) {
+            if (tid == 0) {
+                s_over = 0;
+                s_distinct = 0;
+            }  // visible after part_scatter's first barrier
+            int claims = 0;
+            if (code32) {
+                part_scatter(s_col, s_dim, d, S, lp, reinterpret_cast<uint32_t *>(rz), rxy, s_pcnt, s_poff, s_pcur);
+                FPGM_PHASE(14);
+                acc = part_run<false>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, s_pcnt, s_poff, dx, dy,
+                                      smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
+                                      claims, a.dbg);
+            } else {
+                part_scatter(s_col, s_dim, d, S, lp, reinterpret_cast<uint64_t *>(rz), rxy, s_pcnt, s_poff, s_pcur);
+                FPGM_PHASE(14);
+                acc = part_run<false>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, s_pcnt, s_poff, dx, dy,
+                                      smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
+                                      claims, a.dbg);
+            }
+            atomicAdd(&s_distinct, claims);
+            __syncthreads();
+            over = s_over != 0;
+            __syncthreads();  // every thread has read s_over before it is reset
+            if (!over || lp >= maxlog) break;
+            ++lp;
+        }
+        if (over) {  // the compact kernel's global hash takes it
+            if (tid == 0) {
+                const int q = atomicAdd(&a.counters[C_RETRY], 1);
+                a.lists[5 * a.list_cap + q] = item;
+            }
+        } else {
+            const int n_obs = s_distinct;
+            if (a.dbg && tid == 0) {
+                atomicAdd(&a.dbg[9], (unsigned long long)n_obs);
+                atomicAdd(&a.dbg[13], 1ull);
+            }
+            const Partial r = block_sum(acc, scratch);
+            decide_record(a, item, r, (int64_t)n_obs * dx * dy, 3, s_flag, scratch, [&]() {
+                int claims = 0;
+                return code32 ? part_run<true>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, s_pcnt, s_poff, dx,
+                                               dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over,
+                                               &s_nbig, &s_nocc, claims, nullptr)
+                              : part_run<true>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, s_pcnt, s_poff, dx,
+                                               dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over,
+                                               &s_nbig, &s_nocc, claims, nullptr);
+            });
+        }
+        FPGM_PHASE(15);
         __syncthreads();
     }
 #undef FPGM_PHASE

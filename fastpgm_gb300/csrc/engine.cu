@@ -130,6 +130,7 @@ struct fpgm_engine {
     DevBuf mle_counts, mle_pot, mle_meta;  // parameter learning: counts, potentials, per-node tables
     double band_alpha = -1.0;
     int n_slots = 0, hash_cap_global = 0;
+    int part_max_log = kPartMaxLog;  // FPGM_PART_MAX_LOG (tests): fewer partitions before the global hash
     int64_t slot_bytes = 0, slot_S = 0;  // slot_S: the sample count the slots' layout was made for
     bool wave_log = false;               // FPGM_WAVE_LOG: one stderr line per wave (tier sizes, kernel times)
     // result
@@ -432,7 +433,9 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     CK(cudaEventCreate(&e->ev2));
     CK(cudaFuncSetAttribute(ci_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     CK(cudaFuncSetAttribute(ci_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-    CK(cudaFuncSetAttribute(ci_compact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    CK(cudaFuncSetAttribute(ci_compact_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    CK(cudaFuncSetAttribute(ci_compact_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    CK(cudaFuncSetAttribute(ci_part_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     CK(cudaFuncSetAttribute(ci_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     int occ = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ci_warp_kernel, kThreads, kSmemBytes));
@@ -453,9 +456,10 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     RET(e->counters.ensure(64));
     RET(e->stats.ensure(ST_COUNT * 8));
     e->wave_log = getenv("FPGM_WAVE_LOG") != nullptr;
+    if (const char *pm = getenv("FPGM_PART_MAX_LOG")) e->part_max_log = std::min(kPartMaxLog, std::max(1, atoi(pm)));
     if (getenv("FPGM_PHASE_TIMERS")) {
-        RET(e->phase_timers.ensure(16 * 8));
-        CK(cudaMemset(e->phase_timers.p, 0, 16 * 8));
+        RET(e->phase_timers.ensure(32 * 8));
+        CK(cudaMemset(e->phase_timers.p, 0, 32 * 8));
     }
     *out = e;
     return FPGM_OK;
@@ -645,7 +649,7 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t ite
     a.bt.hi = a.bt.lo + kBandDfMax + 1;
     a.bt.dfmax = kBandDfMax;
     RET(e->item_vars.ensure((size_t)std::max<int64_t>(items, 1) * (2 + d) * 2 + 16));
-    RET(e->lists.ensure((size_t)3 * std::max<int64_t>(items, 1) * 4 + 16));
+    RET(e->lists.ensure((size_t)6 * std::max<int64_t>(items, 1) * 4 + 16));
     RET(e->flag.ensure((size_t)std::max<int64_t>(items, 1) + 16));
     a.item_vars = e->item_vars.as<uint16_t>();
     a.lists = e->lists.as<int32_t>();
@@ -658,7 +662,18 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t ite
         a.slot_S = e->slot_S;
         a.hash_cap_global = e->hash_cap_global;
     }
+    a.part_max_log = e->part_max_log;
     return FPGM_OK;
+}
+
+// Tier 2 on the current stream: the compact kernel, the partitioned kernel for the tests it
+// hands over, and the compact kernel again for any the partitioned one hands back (each a
+// persistent loop over its list; an empty list ends at once).  Returns launches issued.
+int launch_compact(fpgm_engine *e, const WaveArgs &a, int grid) {
+    ci_compact_kernel<false><<<grid, kThreads, kSmemBytes, e->stream>>>(a);
+    ci_part_kernel<<<grid, kThreads, kSmemBytes, e->stream>>>(a);
+    ci_compact_kernel<true><<<grid, kThreads, kSmemBytes, e->stream>>>(a);
+    return 3;
 }
 
 // Classify + the three tiers on the current stream.  Returns launches issued.
@@ -668,10 +683,7 @@ int launch_tiers(fpgm_engine *e, const WaveArgs &a) {
     ci_warp_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
     ci_cta_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
     int n = 3;
-    if (a.slot_mem) {
-        ci_compact_kernel<<<e->n_slots, kThreads, kSmemBytes, e->stream>>>(a);
-        ++n;
-    }
+    if (a.slot_mem) n += launch_compact(e, a, e->n_slots);
     return n;
 }
 
@@ -722,16 +734,22 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
         st->kernel_launches += 5;  // plan, classify, warp tier, CTA tier, reduce
         a.dbg = e->phase_timers.as<unsigned long long>();
         if (a.slot_mem) {
-            ci_compact_kernel<<<e->n_slots, kThreads, kSmemBytes, e->stream>>>(a);
+            st->kernel_launches += launch_compact(e, a, e->n_slots);
             CK(cudaGetLastError());
-            st->kernel_launches += 1;
         }
         if (a.dbg) {  // FPGM_PHASE_TIMERS: per-wave breakdown of the compact tier on stderr
-            unsigned long long h[16];
+            unsigned long long h[32];
             CK(cudaMemcpyAsync(h, a.dbg, sizeof h, cudaMemcpyDeviceToHost, e->stream));
 
             CK(cudaMemsetAsync(a.dbg, 0, sizeof h, e->stream));
             CK(cudaStreamSynchronize(e->stream));
+            if (h[13])
+                fprintf(stderr,
+                        "partitioned d=%d tests=%llu strata/test=%.0f partitions/test=%.1f us/test: records=%.1f "
+                        "counted+scored=%.1f [clear=%.1f insert=%.1f scan=%.1f place=%.1f small=%.1f big=%.1f]\n",
+                        d, h[13], (double)h[9] / h[13], (double)h[22] / h[13], h[14] / 1e3 / h[13],
+                        h[15] / 1e3 / h[13], h[16] / 1e3 / h[13], h[17] / 1e3 / h[13], h[18] / 1e3 / h[13],
+                        h[19] / 1e3 / h[13], h[20] / 1e3 / h[13], h[21] / 1e3 / h[13]);
             if (h[11])
                 fprintf(stderr,
                         "compact d=%d tests=%llu strata/test=%.0f us/test: shared-hash=%.1f global-hash=%.1f "
@@ -1014,13 +1032,15 @@ int plain_test(fpgm_engine *e, int x, int y, const int *z, int d, double alpha, 
         for (int k = 0; k < d; ++k) iv[k] = (uint16_t)z[k];
         iv[d] = (uint16_t)x;
         iv[d + 1] = (uint16_t)y;
-        int32_t ctr[C_COUNT] = {0, 0, 1, 0, 0, 0};
+        int32_t ctr[C_COUNT] = {};
+        ctr[C_TIER2] = 1;
         int32_t zero = 0;
         CK(cudaMemcpyAsync(a.item_vars, iv, (d + 2) * 2, cudaMemcpyHostToDevice, e->stream));
         CK(cudaMemcpyAsync(a.lists + 2 * a.list_cap, &zero, 4, cudaMemcpyHostToDevice, e->stream));
         CK(cudaMemcpyAsync(a.counters, ctr, sizeof ctr, cudaMemcpyHostToDevice, e->stream));
-        ci_compact_kernel<<<1, kThreads, kSmemBytes, e->stream>>>(a);
+        const int n = launch_compact(e, a, 1);
         CK(cudaGetLastError());
+        if (st) st->kernel_launches += n - 1;
     }
     if (st) st->kernel_launches += 1;
     CK(cudaMemcpyAsync(out, e->detail_buf.p, sizeof(fpgm_ci_result), cudaMemcpyDeviceToHost, e->stream));

@@ -68,7 +68,8 @@ typedef struct {
     double g2;             /* G^2 the decision used: FP64 when rechecked, else the FP32 compensated sum */
     double p_value;        /* 1 - P(df/2, G^2/2) */
     int32_t rechecked;     /* 1 when G^2 was computed with FP64 terms (recheck band or compact path) */
-    int32_t path;          /* 0 warp tier, 1 CTA tier or plain kernel, 2 compact strata */
+    int32_t path;          /* 0 warp tier, 1 CTA tier or plain kernel, 2 compact strata,
+                              3 partitioned strata */
 } fpgm_ci_result;
 
 typedef struct {

@@ -175,13 +175,14 @@ def test_256_state_column_is_rejected_at_upload(eng):
     assert list(card) == [255, 3, 5]
 
 
-@pytest.mark.parametrize("card,d", [((2, 5), 5), ((6, 9), 3), ((6, 9), 4)])
+@pytest.mark.parametrize("card,d", [((2, 5), 5), ((6, 9), 3), ((6, 9), 4), ((6, 9), 5)])
 def test_compact_tier_across_dataset_sizes(eng, card, d):
     """Compact-tier tests after datasets of other sample counts: the per-CTA slots are laid
     out once for the largest dataset seen and reused; their zeroed tables must stay zeroed.
     Cards 2-5 at |Z| = 5 take the dense strata table (at most 32 cells per stratum), cards
-    6-9 the counting-sort path, at |Z| = 4 also through the global strata hash."""
-    for S in (20000, 6000, 30000, 6000):
+    6-9 the counting-sort path, at |Z| = 4 also through the global strata hash and at |Z| = 5
+    (beyond 8,192 strata) on 70,000 samples through the partitioned kernel."""
+    for S in (20000, 6000, 70000, 6000):
         raw, _, _ = F.generate(n_nodes=10, n_samples=S, seed=S + d, n_edges=12, max_indegree=3, card=card)
         cols, cd = O.relabel(raw)
         eng.upload(raw)
@@ -212,9 +213,53 @@ def test_compact_tier_at_c4_scale(eng, c4_data, d):
     rng = np.random.default_rng(11 + d)
     tests = random_tests(rng, n, d, 300)
     got = eng.ci_test_batch(tests, d, want_hash=True)
-    idx = [i for i, g in enumerate(got) if g.path == 2][:10]
-    assert len(idx) == 10
+    idx = [i for i, g in enumerate(got) if g.path == 2][:6] + [i for i, g in enumerate(got) if g.path == 3][:6]
+    assert len(idx) >= 6
+    if d >= 6:
+        assert sum(g.path == 3 for g in got) >= 6, "partitioned kernel not used"
     exp = O.ci_tests(cols, cd, tests[idx], d, threads=8)
     for i, o in zip(idx, exp):
         check(got[i], o, exact_p=got[i].rechecked == 1)
     assert all(np.isfinite(g.g2) and np.isfinite(g.p_value) for g in got)
+
+
+def test_partitioned_strata_with_64_bit_codes(eng):
+    """|Z| = 8 over 16-state variables (2^32 strata codes: 64-bit keys) on 70,000 samples:
+    nearly every sample is its own stratum, far beyond the shared hash, so the partitioned
+    kernel counts them in 64+ shared-memory partitions."""
+    rng = np.random.default_rng(23)
+    S = 70000
+    raw = rng.integers(0, 16, size=(12, S)).astype(np.uint8)
+    raw[1] = (raw[0] + (rng.random(S) < 0.5) * rng.integers(0, 16, S)) % 16
+    cols, card = O.relabel(raw)
+    eng.upload(raw)
+    tests = np.array([[0, 1, 2, 3, 4, 5, 6, 7, 8, 9], [2, 3, 4, 5, 6, 7, 8, 9, 10, 11],
+                      [0, 11, 1, 2, 3, 4, 5, 6, 7, 8]], dtype=np.int32)
+    got = eng.ci_test_batch(tests, 8, want_hash=True)
+    exp = O.ci_tests(cols, card, tests, 8, threads=3)
+    for g, o in zip(got, exp):
+        assert g.path == 3
+        check(g, o, exact_p=g.rechecked == 1)  # FP32 G^2 on 70,000 samples: p within 1e-3 unless rechecked
+
+
+def test_partition_overflow_falls_back_to_global_hash(monkeypatch):
+    """With at most 2 partitions (FPGM_PART_MAX_LOG=1) a test with ~60,000 strata overflows
+    every partition table, and the compact kernel's global hash takes it (retry list): same
+    counts and decisions."""
+    monkeypatch.setenv("FPGM_PART_MAX_LOG", "1")
+    e = F.Engine(0)
+    try:
+        rng = np.random.default_rng(29)
+        S = 70000
+        raw = rng.integers(0, 9, size=(10, S)).astype(np.uint8)
+        raw[1] = (raw[0] + (rng.random(S) < 0.4) * rng.integers(0, 9, S)) % 9
+        cols, card = O.relabel(raw)
+        e.upload(raw)
+        tests = np.array([[0, 1, 2, 3, 4, 5, 6, 7], [2, 3, 4, 5, 6, 7, 8, 9]], dtype=np.int32)
+        got = e.ci_test_batch(tests, 6, want_hash=True)
+        exp = O.ci_tests(cols, card, tests, 6, threads=2)
+        for g, o in zip(got, exp):
+            assert g.path == 2 and g.cells > 8192 * 81
+            check(g, o, exact_p=g.rechecked == 1)
+    finally:
+        e.close()
