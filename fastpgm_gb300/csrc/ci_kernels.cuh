@@ -418,8 +418,10 @@ __device__ inline int zinsert(K *keys, Id *ids, uint32_t cap, uint64_t zz, int *
 }
 
 // Stratum codes of 16 consecutive samples (vector v) from the d Z columns, four column
-// loads in flight at a time.
-__device__ __forceinline__ void zcodes16(uint64_t (&z)[16], const uint8_t *const *col, const uint32_t *dim, int d,
+// loads in flight at a time.  K = uint32_t when every code is below 2^32 (so is every
+// prefix of the mixed-radix code).
+template <class K>
+__device__ __forceinline__ void zcodes16(K (&z)[16], const uint8_t *const *col, const uint32_t *dim, int d,
                                          int64_t v) {
 #pragma unroll
     for (int b = 0; b < 16; ++b) z[b] = 0;
@@ -432,7 +434,7 @@ __device__ __forceinline__ void zcodes16(uint64_t (&z)[16], const uint8_t *const
         for (int t = 0; t < 4; ++t) {
             if (j0 + t >= d) break;
             const uint32_t ww[4] = {w[t].x, w[t].y, w[t].z, w[t].w};
-            const uint64_t dm = dim[j0 + t];
+            const K dm = dim[j0 + t];
 #pragma unroll
             for (int b = 0; b < 16; ++b) z[b] = z[b] * dm + ((ww[b >> 2] >> (8 * (b & 3))) & 0xffu);
         }
@@ -764,9 +766,11 @@ __device__ __forceinline__ unsigned long long gtimer() {
 //   pass 1  the partition's codes are hashed to slots (next bits of the mixed code); a new
 //           code appends its slot to occ[] (stratum i = occ[i]) and every slot counts its
 //           samples in A[slot];
-//   index   A[occ[i]] becomes i, and E[1 + i] its count, scanned to its first sorted position;
+//   index   strata are ranked by size (1, 2, ..., 8 samples, then larger), so a warp's lanes
+//           score strata of one size; A[slot] becomes the rank r and E[1 + r] the count,
+//           scanned to the stratum's first sorted position;
 //   pass 2  every record is found again and its (x << 8) | y code placed at its stratum's
-//           cursor E[1 + i], so afterwards stratum i's samples are ord[E[i] .. E[i + 1]);
+//           cursor E[1 + r], so afterwards stratum r's samples are ord[E[r] .. E[r + 1]);
 //   score   score_small_strata / score_big_strata over the strata.
 // No global hash, no per-sample id array and no global scatter of the sorted codes (unless a
 // partition holds more samples than the shared sorted array).
@@ -868,14 +872,14 @@ __device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint3
     for (int i = tid; i < P; i += kThreads) s_pcnt[i] = 0;
     __syncthreads();
     for (int64_t v = tid; v < nvec; v += kThreads) {
-        uint64_t z[16];
+        K z[16];
         zcodes16(z, col, dim, d, v);
 #pragma unroll
         for (int b = 0; b < 16; ++b) atomicAdd(&s_pcnt[part_of(z[b], lp)], 1);
     }
     for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
-        uint64_t z = 0;
-        for (int j = 0; j < d; ++j) z = z * dim[j] + col[j][s];
+        K z = 0;
+        for (int j = 0; j < d; ++j) z = z * (K)dim[j] + col[j][s];
         atomicAdd(&s_pcnt[part_of(z, lp)], 1);
     }
     __syncthreads();
@@ -905,7 +909,7 @@ __device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint3
     }
     __syncthreads();
     for (int64_t v = tid; v < nvec; v += kThreads) {
-        uint64_t z[16];
+        K z[16];
         zcodes16(z, col, dim, d, v);
         const uint4 wx = __ldg(reinterpret_cast<const uint4 *>(colx) + v);
         const uint4 wy = __ldg(reinterpret_cast<const uint4 *>(coly) + v);
@@ -914,15 +918,15 @@ __device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint3
         for (int b = 0; b < 16; ++b) {
             const int pos = atomicAdd(&s_pcur[part_of(z[b], lp)], 1);
             const int sh = 8 * (b & 3);
-            rec_z[pos] = (K)z[b];
+            rec_z[pos] = z[b];
             rec_xy[pos] = (uint16_t)((((xx[b >> 2] >> sh) & 0xffu) << 8) | ((yy[b >> 2] >> sh) & 0xffu));
         }
     }
     for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
-        uint64_t z = 0;
-        for (int j = 0; j < d; ++j) z = z * dim[j] + col[j][s];
+        K z = 0;
+        for (int j = 0; j < d; ++j) z = z * (K)dim[j] + col[j][s];
         const int pos = atomicAdd(&s_pcur[part_of(z, lp)], 1);
-        rec_z[pos] = (K)z;
+        rec_z[pos] = z;
         rec_xy[pos] = (uint16_t)((colx[s] << 8) | coly[s]);
     }
     __syncthreads();
@@ -944,7 +948,8 @@ template <bool kFp64, class K>
 __device__ __noinline__ Partial part_run(int lp, const K *rec_z, const uint16_t *rec_xy, const int *s_pcnt,
                                          const int *s_poff, int dx, int dy, unsigned char *smem, uint16_t *gord,
                                          int *gwt, uint64_t *gzk, bool want_hash, int *s_w, int *s_over,
-                                         int *s_nbig, int *s_nocc, int &claims, unsigned long long *dbg) {
+                                         int *s_nbig, int *s_nocc, int *s_bin, int &claims,
+                                         unsigned long long *dbg) {
     using Plan = PartPlan<K>;
     constexpr uint32_t cap = Plan::cap;
     const int tid = threadIdx.x, warp = tid >> 5, P = 1 << lp;
@@ -979,6 +984,7 @@ __device__ __noinline__ Partial part_run(int lp, const K *rec_z, const uint16_t 
                 A[i] = 0;
             }
             if (tid == 0) *s_nocc = 0;
+            if (tid < 10) s_bin[tid] = 0;
             __syncthreads();
             lap(16);
             // pass 1: first probes of eight codes at once; misses take the inserting path
@@ -1012,14 +1018,26 @@ __device__ __noinline__ Partial part_run(int lp, const K *rec_z, const uint16_t 
             if (!over) {
                 const int n_occ = *s_nocc;
                 if (tid == 0) claims += n_occ;
-                // stratum index per slot, counts -> first sorted positions
-                for (int i = tid; i < n_occ; i += kThreads) {
-                    const int sl = occ[i];
-                    E[1 + i] = A[sl];
-                    A[sl] = i;
-                    if (want_hash) gzk[i] = (uint64_t)keys[sl];
+                // strata ranked by size: bins 1..8 samples, 9 for larger ones
+                for (int i = tid; i < n_occ; i += kThreads) atomicAdd(&s_bin[min(A[occ[i]], 9)], 1);
+                __syncthreads();
+                if (tid == 0) {
+                    int run = 0;
+                    for (int b = 1; b < 10; ++b) {
+                        const int c = s_bin[b];
+                        s_bin[b] = run;
+                        run += c;
+                    }
+                    E[0] = 0;
                 }
-                if (tid == 0) E[0] = 0;
+                __syncthreads();
+                for (int i = tid; i < n_occ; i += kThreads) {
+                    const int sl = occ[i], m = A[sl];
+                    const int r = atomicAdd(&s_bin[min(m, 9)], 1);
+                    E[1 + r] = m;
+                    A[sl] = r;
+                    if (want_hash) gzk[r] = (uint64_t)keys[sl];
+                }
                 __syncthreads();
                 block_exclusive_scan(E + 1, n_occ, s_w);
                 lap(18);
@@ -1440,6 +1458,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
     __shared__ const uint8_t *s_col[kMaxCols];
     __shared__ uint32_t s_dim[kMaxCols];
     __shared__ int s_idx, s_over, s_distinct, s_flag, s_nbig, s_nocc;
+    __shared__ int s_bin[16];
     __shared__ int s_w[kWarps];
     __shared__ Partial scratch[kWarps];
     __shared__ int s_pcnt[kPartMax], s_poff[kPartMax + 1], s_pcur[kPartMax];
@@ -1502,13 +1521,13 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
                 FPGM_PHASE(14);
                 acc = part_run<false>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, s_pcnt, s_poff, dx, dy,
                                       smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
-                                      claims, a.dbg);
+                                      s_bin, claims, a.dbg);
             } else {
                 part_scatter(s_col, s_dim, d, S, lp, reinterpret_cast<uint64_t *>(rz), rxy, s_pcnt, s_poff, s_pcur);
                 FPGM_PHASE(14);
                 acc = part_run<false>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, s_pcnt, s_poff, dx, dy,
                                       smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
-                                      claims, a.dbg);
+                                      s_bin, claims, a.dbg);
             }
             atomicAdd(&s_distinct, claims);
             __syncthreads();
@@ -1533,10 +1552,10 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
                 int claims = 0;
                 return code32 ? part_run<true>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, s_pcnt, s_poff, dx,
                                                dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over,
-                                               &s_nbig, &s_nocc, claims, nullptr)
+                                               &s_nbig, &s_nocc, s_bin, claims, nullptr)
                               : part_run<true>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, s_pcnt, s_poff, dx,
                                                dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over,
-                                               &s_nbig, &s_nocc, claims, nullptr);
+                                               &s_nbig, &s_nocc, s_bin, claims, nullptr);
             });
         }
         FPGM_PHASE(15);
