@@ -782,10 +782,10 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
         st->count_launches += 1;
         if (e->wave_log)
             fprintf(stderr,
-                    "wave level=%d tests=%d tier0=%d tier1=%d tier2=%d compact_launched=%d count_ms=%.4f "
-                    "compact_ms=%.4f count_bytes=%.0f compact_bytes=%.0f\n",
-                    d, T, tiers[C_TIER0], tiers[C_TIER1], tiers[C_TIER2], a.slot_mem != nullptr, ms, ms2,
-                    (double)hs[ST_BYTES_SHARED], (double)hs[ST_BYTES_LARGE]);
+                    "wave level=%d tests=%d tier0=%d tier1=%d tier2=%d (partitioned=%d retried=%d) "
+                    "compact_launched=%d count_ms=%.4f compact_ms=%.4f count_bytes=%.0f compact_bytes=%.0f\n",
+                    d, T, tiers[C_TIER0], tiers[C_TIER1], tiers[C_TIER2], tiers[C_PART], tiers[C_RETRY],
+                    a.slot_mem != nullptr, ms, ms2, (double)hs[ST_BYTES_SHARED], (double)hs[ST_BYTES_LARGE]);
         if (hs[ST_UNSUPPORTED])
             return set_error(FPGM_ERR_UNSUPPORTED,
                              "level %d: %llu CI test(s) are outside the engine's limits (joint table beyond 2^62 "
