@@ -1,6 +1,7 @@
 """GPU PC-stable skeleton parity: batched engine and plain path against the reference's
 golden sepsets/CPDAGs and the oracle's per-level deterministic test counts."""
 import os
+import re
 import subprocess
 
 import numpy as np
@@ -135,6 +136,34 @@ def test_several_datasets_match_each_oracle(eng):
         assert np.array_equal(adj, ref["adj"])
         assert seps == ref["sepsets"]
         assert ref["stats"]["n_levels"] <= st["n_levels"]
+        for lv, t in enumerate(ref["stats"]["tests"]):
+            levels[lv] += t
+    assert st["tests"] == levels
+
+
+def test_partitioned_strata_in_a_skeleton(monkeypatch, capfd):
+    """A 70,000-sample dataset with 6-9 states per variable whose levels 5 and 6 test 8,000 to
+    22,000 strata (beyond the shared hash: partitioned kernel), learned next to a small
+    dataset in one skeleton call: each skeleton, sepset and test count equals the oracle's,
+    and the wave log shows partitioned tests."""
+    monkeypatch.setenv("FPGM_WAVE_LOG", "1")
+    big, _, _ = F.generate(n_nodes=12, n_samples=70000, seed=72, n_edges=30, max_indegree=5, card=(6, 10))
+    small, _, _ = F.generate(n_nodes=10, n_samples=5000, seed=73, n_edges=14, max_indegree=3, card=(2, 4))
+    data = [big, small]
+    with F.Engine(0) as e:
+        e.upload_jobs(data)
+        st = e.pc_skeleton().to_dict()
+        res = e.result()
+        offsets = e.job_offsets
+    log = capfd.readouterr().err
+    parts = [int(t) for t in re.findall(r"partitioned=(\d+)", log)]
+    assert sum(parts) > 0, "no test reached the partitioned kernel"
+    levels = [0] * st["n_levels"]
+    for raw, (adj, seps) in zip(data, F.split_jobs(res, offsets)):
+        cols, card = O.relabel(raw)
+        ref = O.pc_skeleton(cols, card, threads=16)
+        assert np.array_equal(adj, ref["adj"])
+        assert seps == ref["sepsets"]
         for lv, t in enumerate(ref["stats"]["tests"]):
             levels[lv] += t
     assert st["tests"] == levels
