@@ -66,3 +66,15 @@ def test_reference_arm_prints_one_line_under_torchrun():
     assert j["impl"] == "reference" and j["n_gpus"] == 2
     assert j["cpu_baseline"]["kind"] == "port" and j["value"] > 0
     assert j["e2e"]["h2d_bytes_per_step"] == 0 and j["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_roofline_traffic_comes_from_the_committed_profiles():
+    """bench.py's roofline `traffic` is read from the ncu summaries under profiles/: the DRAM
+    bytes and algorithmic bytes of one captured launch, and which kernel was captured."""
+    sys.path.insert(0, ROOT)
+    import bench
+    dram, alg, kernel = bench.profiled_traffic(("ci_part_kernel", "ci_compact_kernel"), "c4")
+    assert kernel == "ci_part_kernel" and dram > 0 and alg > 0
+    dram, alg, kernel = bench.profiled_traffic(("ci_warp_kernel",), "c2")
+    assert kernel == "ci_warp_kernel" and 0 < dram < alg  # the c2 dataset stays in L2
+    assert bench.profiled_traffic(("ci_warp_kernel",), "c3") is None
