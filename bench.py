@@ -197,6 +197,18 @@ def profiled_traffic(kernels, config):
     return got.get("dram_bytes_per_launch"), got.get("algorithmic_bytes_per_launch"), got["kernel"]
 
 
+def counting_phase(groups, peak):
+    """The whole counting phase (every counting kernel group): summed algorithmic bytes over
+    summed event time, against the HBM peak.  groups: [(kernel_ms, algorithmic_bytes)]."""
+    ms = sum(g[0] for g in groups)
+    nbytes = sum(g[1] for g in groups)
+    if ms <= 0:
+        return None
+    ach = nbytes / (ms / 1e3) / 1e9
+    return {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "kernel_ms": ms,
+            "algorithmic_bytes": nbytes}
+
+
 def cpu_port(data, depth, alpha, threads):
     """The oracle port over the datasets one after another: (tests, seconds)."""
     from oracle import oracle as O
@@ -333,6 +345,7 @@ def run_ours(a, d):
     kernels.sort(key=lambda k: -k["kernel_ms"])
     roofline = dict(kernels[0])
     roofline["others"] = kernels[1:]
+    roofline["counting_phase"] = counting_phase([(k["kernel_ms"], k["algorithmic_bytes"]) for k in kernels], peak)
     cpu = None
     if d.rank == 0 and d.world == 1 and not a.no_cpu:
         threads = os.cpu_count() or 1

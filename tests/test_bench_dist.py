@@ -78,3 +78,13 @@ def test_roofline_traffic_comes_from_the_committed_profiles():
     dram, alg, kernel = bench.profiled_traffic(("ci_warp_kernel",), "c2")
     assert kernel == "ci_warp_kernel" and 0 < dram < alg  # the c2 dataset stays in L2
     assert bench.profiled_traffic(("ci_warp_kernel",), "c3") is None
+
+
+def test_counting_phase_fraction_sums_both_kernel_groups():
+    """The counting-phase roofline figure is total algorithmic bytes over total event time of
+    both kernel groups (e.g. 4 GB in 1 s and 1 GB in 4 s: 1 GB/s)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    r = bench.counting_phase([(1000.0, 4e9), (4000.0, 1e9)], 10.0)
+    assert abs(r["achieved"] - 1.0) < 1e-12 and abs(r["frac"] - 0.1) < 1e-12 and r["kernel_ms"] == 5000.0
+    assert bench.counting_phase([], 10.0) is None
