@@ -9,7 +9,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, read_tests
+from conftest import GOLDEN, read_tests, tiny_table_cases
 from oracle import oracle as O
 import fastpgm_gb300 as F
 
@@ -263,3 +263,20 @@ def test_partition_overflow_falls_back_to_global_hash(monkeypatch):
             check(g, o, exact_p=g.rechecked == 1)
     finally:
         e.close()
+
+
+@pytest.mark.parametrize("case", tiny_table_cases(), ids=lambda c: c[0])
+def test_known_answers_on_tiny_tables(eng, case):
+    """Hand-built tables of 8 to 18 samples (every sample in the kernels' ragged tails), G^2
+    and p in closed form: batched and plain paths give the exact df and decision, G^2 within
+    the FP32 bound (exact to 1e-10 when rechecked in FP64)."""
+    name, raw, d, g2, df, p = case
+    eng.upload(raw)
+    test = list(range(2 + d))
+    got = [eng.ci_test_batch(np.array([test], dtype=np.int32), d)[0], eng.ci_test(0, 1, tuple(test[2:]))]
+    for g in got:
+        assert g.df == df and g.independent == (p > 0.05), (name, g.df, g.independent)
+        if g.rechecked:
+            assert abs(g.g2 - g2) < 1e-10 and abs(g.p_value - p) < 1e-10
+        else:
+            assert abs(g.g2 - g2) <= max(G2_ATOL, G2_RTOL * g2) and abs(g.p_value - p) <= P_ATOL

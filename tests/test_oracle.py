@@ -11,7 +11,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, read_sepsets, read_tests
+from conftest import GOLDEN, read_sepsets, read_tests, tiny_table_cases
 from oracle import oracle as O
 import fastpgm_gb300 as F
 
@@ -165,3 +165,12 @@ def test_mle_oracle_matches_reference_parameter_learning(tmp_path, alpha):
         rel, pots = ref[v]
         assert rel[0] == v and rel[1:] == sorted(int(p) for p in par[v] if p >= 0)
         assert np.array_equal(got[v], pots), v
+
+
+@pytest.mark.parametrize("case", tiny_table_cases(), ids=lambda c: c[0])
+def test_oracle_known_answers_on_tiny_tables(case):
+    name, raw, d, g2, df, p = case
+    cols, card = O.relabel(raw)
+    r = O.ci_tests(cols, card, np.array([list(range(2 + d))], dtype=np.int32), d, threads=1)[0]
+    assert r.df == df and abs(r.g2 - g2) < 1e-12 and abs(r.p_value - p) < 1e-12
+    assert r.independent == (p > 0.05)
