@@ -158,7 +158,8 @@ int fpgm_mle_cpts(fpgm_engine *eng, const int32_t *parent_off, const int32_t *pa
 int fpgm_dataset_download(fpgm_engine *eng, uint8_t *columns);
 
 /* ---- single / batched CI tests (G^2) ----
- * fpgm_ci_test: one test, one kernel launch ("plain" path).
+ * fpgm_ci_test: one test, one kernel launch ("plain" path; a joint table beyond the
+ * shared-memory tiers runs the three tier-2 launches on one CTA instead).
  * fpgm_ci_test_batch: tests[t*(2+d) + 0,1,2..] = x, y, z1..zd; all tests run in one
  * persistent launch.  want_hash != 0 fills table_hash (slower). */
 int fpgm_ci_test(fpgm_engine *eng, int32_t x, int32_t y, const int32_t *z, int32_t nz, double alpha,
@@ -195,7 +196,7 @@ int fpgm_ci_test_noalloc(const uint8_t *columns, int64_t pitch, int32_t n_vars, 
 /* ---- PC-stable skeleton ----
  * depth follows PCStable(Network*, alpha, depth=1000): levels d = 0 .. depth-1.
  * mode: FPGM_MODE_BATCHED (device-resident level engine) or FPGM_MODE_PLAIN
- * (the reference's control flow on the host, one kernel launch per CI test).
+ * (the reference's control flow on the host, one fpgm_ci_test per CI test).
  * The result stays in the engine until the next call; fetch it below. */
 int fpgm_pc_skeleton(fpgm_engine *eng, double alpha, int32_t depth, int32_t mode, fpgm_pc_stats *stats);
 int fpgm_pc_result_sizes(fpgm_engine *eng, int32_t *n_nodes, int32_t *n_removed, int64_t *n_sep_vars);
