@@ -52,13 +52,21 @@ def cpu_sample(data):
                                                                              CPU_SAMPLE_MAX_S)
 
 
-def load_workload(name):
-    """(list of raw uint8 [n, S] datasets, depth): one dataset, or c5's 64."""
-    import fastpgm_gb300 as F
+def load_workload(name, generate=None):
+    """(list of raw uint8 [n, S] datasets, depth): one dataset, or c5's 64.  generate: the
+    seeded sampler (default the engine library's; the CPU arms pass the oracle's copy so that
+    they never load the engine)."""
+    from fastpgm_gb300 import configs as C
     if name == "c5":
-        return F.make_jobs(F.c5_jobs())
-    raw, depth, _ = F.make_config(name)
+        return C.make_jobs(C.c5_jobs(), generate=generate)
+    raw, depth, _ = C.make_config(name, generate=generate)
     return [raw], depth
+
+
+def bench_config(a, depth):
+    """The `config` object, identical in both arms."""
+    return {"workload": WORKLOADS[a.config], "alpha": a.alpha, "depth": depth,
+            "parallelism": "replicas" if a.gpus > 1 else "single GPU"}
 
 
 def upload(eng, data):
@@ -79,6 +87,8 @@ def parse():
     ap.add_argument("--alpha", type=float, default=0.05)
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-kernel comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline run")
+    ap.add_argument("--no-north-star", action="store_true", help="skip the c4 (north-star workload) object")
+    ap.add_argument("--no-wall", action="store_true", help="skip the BNSL_PCStable wall-time object")
     ap.add_argument("--profile-one", action="store_true",
                     help="run exactly one skeleton (no warm-up, flush, e2e or baselines) for profilers; "
                          "prints its statistics, not a benchmark line")
@@ -223,10 +233,12 @@ def cpu_port(data, depth, alpha, threads):
 
 
 def run_reference(a, d):
-    import fastpgm_gb300 as F
+    """The reference algorithm's CPU path (the oracle port, all host threads).  Loads only
+    oracle/_build/*.so: the inputs come from the oracle's copy of the seeded sampler."""
+    from oracle import oracle as O
     if d.rank != 0:
         return
-    data, depth = load_workload(a.config)
+    data, depth = load_workload(a.config, generate=O.generate)
     sample, what = cpu_sample(data)
     what = (what + " per step") if what else "full %s skeleton per step" % a.config
     threads = os.cpu_count() or 1
@@ -241,8 +253,8 @@ def run_reference(a, d):
     line = {"impl": "reference", "metric": "CI tests/s (PC-stable skeleton, deterministic test count)", "value": v,
             "unit": "CI tests/s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": secs / a.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "u8 data, int32 counts, fp64 G2", "data": "synthetic (seeded random DAG + Dirichlet CPTs)",
-            "config": {"workload": WORKLOADS[a.config], "alpha": a.alpha, "tests_per_step": tests // a.steps},
+            "dtype": "u8 data, int32 counts, fp64 G2", "data": "synthetic (seeded random DAG + Dirichlet CPTs, forward sampled)",
+            "config": bench_config(a, depth), "tests_per_step": tests // a.steps,
             "cpu_baseline": {"value": v, "unit": "CI tests/s", "cores": threads, "kind": "port",
                              "sample": what},
             "e2e": {"value": v, "unit": "CI tests/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -255,6 +267,203 @@ def flush_l2(buf):
     torch.cuda.synchronize()
 
 
+def skeleton_run(eng, a, depth, steps, l2buf, clocks=None, d=None):
+    """`steps` timed skeletons on a resident dataset, L2 flushed before each; the sums of the
+    engine's per-call statistics (device span and the counting kernels' event times)."""
+    import torch
+    tot = {"tests": 0, "span_ms": 0.0, "count_ms": 0.0, "count_bytes": 0.0, "count_launches": 0, "large_ms": 0.0,
+           "large_bytes": 0.0, "kernel_launches": 0, "gram_ms": 0.0, "gram_flops": 0.0, "gram_tests": 0}
+    if clocks:
+        clocks.start()
+    if d:
+        d.barrier()
+    torch.cuda.synchronize()
+    last = None
+    for _ in range(steps):
+        flush_l2(l2buf)
+        st = eng.pc_skeleton(alpha=a.alpha, depth=depth).to_dict()
+        tot["tests"] += sum(st["tests"])
+        for k in ("span_ms", "count_ms", "count_bytes", "count_launches", "large_ms", "large_bytes",
+                  "kernel_launches", "gram_ms", "gram_flops", "gram_tests"):
+            tot[k] += st[k]
+        last = st
+    torch.cuda.synchronize()
+    if d:
+        d.barrier()
+    tot["clocks"] = clocks.stop() if clocks else None
+    tot["last"] = last
+    return tot
+
+
+def e2e_run(eng, a, data, depth, steps, l2buf):
+    """End to end through the C ABI: samples from pinned host memory (upload + relabel),
+    the skeleton, the adjacency and separating sets back to the host.  (tests, seconds, d2h bytes)."""
+    import torch
+    pinned = [torch.from_numpy(raw).pin_memory().numpy() for raw in data]
+    secs, tests, res = 0.0, 0, None
+    for _ in range(steps):
+        flush_l2(l2buf)
+        t0 = time.perf_counter()
+        upload(eng, pinned)
+        st = eng.pc_skeleton(alpha=a.alpha, depth=depth).to_dict()
+        res = eng.result_arrays()
+        secs += time.perf_counter() - t0
+        tests += sum(st["tests"])
+    n = sum(r.shape[0] for r in data)
+    W = (n + 31) // 32
+    d2h = n * W * 4 + len(res["removed"]) * 16 + len(res["sep_vars"]) * 4
+    return tests, secs, d2h
+
+
+def kernel_groups(tot, config, peak, peak_kind):
+    """Roofline objects of the two counting-kernel groups (event-timed on the engine's stream),
+    the larger share first."""
+    kernels = []
+    for name, desc, members, ms, nbytes in (
+            ("ci_warp_kernel", "classify + warp-per-test + CTA-per-test kernels, shared-memory tables",
+             ("ci_warp_kernel",), tot["count_ms"], tot["count_bytes"]),
+            ("ci_compact_kernel+ci_part_kernel",
+             "tier 2, joint tables beyond shared memory: hashed strata (compact kernel) and partitioned "
+             "strata (partition kernels)", ("ci_part_kernel", "ci_compact_kernel"), tot["large_ms"],
+             tot["large_bytes"])):
+        if ms <= 0:
+            continue
+        ach = nbytes / (ms / 1e3) / 1e9
+        tr = profiled_traffic(members, config)
+        kernels.append({"kernel": name, "what": desc, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                        "frac": ach / peak, "peak_kind": peak_kind, "kernel_ms": ms, "algorithmic_bytes": nbytes,
+                        "launches": tot["count_launches"] if name == "ci_warp_kernel" else None,
+                        "traffic": tr[0] if tr else None,
+                        "traffic_source": ("profiles/%s_%s.txt (one ncu capture; not measured in this run)"
+                                           % (tr[2], config)) if tr else None,
+                        "traffic_launch_algorithmic_bytes": tr[1] if tr else None})
+    kernels.sort(key=lambda k: -k["kernel_ms"])
+    return kernels
+
+
+def tensor_peak():
+    """Dense FP8 tensor rate: twice the measured bf16 GEMM burst (FP8 runs at twice the bf16
+    rate on this part; no FP8 figure is measured), else twice the fallback."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return 2.0 * float(json.load(open(p))["bf16_tflops"]), "fp8 dense = 2 x measured bf16 burst"
+    return 2.0 * 1900.0, "fp8 dense = 2 x fallback bf16 burst"
+
+
+def gram_roofline(tot):
+    """Level 0 on the tensor cores: Gram GEMM flops over the event time of the whole level-0
+    wave (one-hot build + GEMM + pair scoring), against the dense FP8 tensor rate."""
+    if tot["gram_ms"] <= 0:
+        return None
+    peak, kind = tensor_peak()
+    ach = tot["gram_flops"] / (tot["gram_ms"] / 1e3) / 1e12
+    return {"kernel": "gram_kernel", "what": "level 0: E4M3 one-hot Gram GEMM on tcgen05 (TMA-staged, FP32 in TMEM) + "
+                                            "one-hot build + pair scoring", "bound": "tensor", "achieved": ach,
+            "peak": peak, "unit": "TFLOP/s", "frac": ach / peak, "peak_kind": kind, "kernel_ms": tot["gram_ms"],
+            "flops": tot["gram_flops"], "tests": tot["gram_tests"]}
+
+
+def level_record(st):
+    return {"levels": st["n_levels"], "tests_per_level": st["tests"], "tests_executed_per_level": st["tests_executed"],
+            "edges_after": st["edges_after"], "waves": st["waves"], "level_ms": [round(x, 3) for x in st["ms"]],
+            "large_table_ms": st["large_ms"]}
+
+
+def recorded(name):
+    """A measurement kept under profiles/ as 'key: value' lines (see the file for its command)."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    out = {}
+    for line in open(p):
+        if ":" in line and not line.startswith((" ", "#", "|")):
+            k, v = line.split(":", 1)
+            out[k.strip()] = v.strip()
+    return out
+
+
+def north_star_c4(a, l2buf, peak, peak_kind):
+    """The spec workload (c4: 1,041 nodes, 100,000 samples) on the same engine build:
+    device and end-to-end CI tests/s, the counting phase against the HBM roofline, and the
+    plain one-launch-per-test kernel's rate from its recorded full run."""
+    import fastpgm_gb300 as F
+    sub = argparse.Namespace(**vars(a))
+    sub.config = "c4"
+    data, depth = load_workload("c4")
+    with F.Engine(0) as eng:
+        upload(eng, data)
+        eng.pc_skeleton(alpha=a.alpha, depth=depth)
+        tot = skeleton_run(eng, sub, depth, 2, l2buf, clocks=Clocks(0))
+        tests, secs, d2h = e2e_run(eng, sub, data, depth, 1, l2buf)
+    value = tot["tests"] / (tot["span_ms"] / 1e3)
+    kernels = kernel_groups(tot, "c4", peak, peak_kind)
+    plain = recorded("plain_kernel_c4.md")
+    out = {"workload": WORKLOADS["c4"], "steps": 2, "value": value, "unit": "CI tests/s",
+           "ms_per_step": tot["span_ms"] / 2, "tests_per_step": tot["tests"] // 2,
+           "e2e": {"value": tests / secs, "unit": "CI tests/s", "h2d_bytes_per_step": int(sum(r.nbytes for r in data)),
+                   "d2h_bytes_per_step": d2h},
+           "counting_phase": counting_phase([(k["kernel_ms"], k["algorithmic_bytes"]) for k in kernels], peak),
+           "kernel_groups": [{k: g[k] for k in ("kernel", "frac", "kernel_ms", "algorithmic_bytes")} for g in kernels],
+           "tensor": gram_roofline(tot),
+           "gpu_launches_per_step": tot["kernel_launches"] // 2, "clocks": tot["clocks"]}
+    out.update(level_record(tot["last"]))
+    if plain and "value" in plain:
+        pv = float(plain["value"])
+        out["plain"] = {"value": pv, "unit": "CI tests/s", "measured": plain.get("date"),
+                        "source": "profiles/plain_kernel_c4.md (full plain skeleton, recorded run; too long to "
+                                  "repeat in every bench run)"}
+        out["speedup_vs_plain"] = value / pv
+    return out
+
+
+def wall_bnsl(configs, verbose=1):
+    """Full BNSL_PCStable seconds through the C ABI (fpgm_bnsl_pcstable): CSV load, skeleton,
+    orientation and the _struct file, the reference's whole learning job (fastpgm_api.cpp:18-44).
+    The CSV is written beforehand (untimed); one untimed call first so the shared engine exists.
+    The job's own report ("pc-stable step 1" = skeleton, "pc-stable" = skeleton + orientation)
+    is read from its standard output."""
+    import ctypes
+    import fastpgm_gb300 as F
+    libc = ctypes.CDLL(None)
+    out = {}
+    tmp = tempfile.mkdtemp(prefix="fpgm_wall_")
+    try:
+        for name in configs:
+            data, depth = load_workload(name)
+            csv = os.path.join(tmp, name + ".csv")
+            F.write_csv(csv, data[0])
+            rec = None
+            for rep in range(2):
+                log = os.path.join(tmp, "stdout.txt")
+                sys.stdout.flush()
+                saved = os.dup(1)
+                fd = os.open(log, os.O_WRONLY | os.O_CREAT | os.O_TRUNC)
+                os.dup2(fd, 1)
+                try:
+                    t0 = time.perf_counter()
+                    F.bnsl_pcstable(verbose, os.cpu_count() or 1, 1, 0.05, "", csv, True)
+                    secs = time.perf_counter() - t0
+                finally:
+                    libc.fflush(None)  # the job writes through C stdio: flush before fd 1 goes back
+                    os.dup2(saved, 1)
+                    os.close(saved)
+                    os.close(fd)
+                text = open(log).read()
+                step1 = [l for l in text.splitlines() if l.startswith("pc-stable step 1:")]
+                full = [l for l in text.splitlines() if l.startswith("pc-stable:")]
+                rec = {"seconds": secs, "csv_mb": os.path.getsize(csv) / 1e6,
+                       "skeleton_s": float(step1[-1].split(":")[1].split()[0]) if step1 else None,
+                       "pc_stable_s": float(full[-1].split(":")[1].split()[0]) if full else None}
+            if rec["pc_stable_s"] is not None:
+                rec["orientation_s"] = rec["pc_stable_s"] - (rec["skeleton_s"] or 0.0)
+                rec["load_and_write_s"] = rec["seconds"] - rec["pc_stable_s"]
+            out[name] = rec
+    finally:
+        import shutil
+        shutil.rmtree(tmp, ignore_errors=True)
+    return out
+
+
 def run_ours(a, d):
     import torch
     import fastpgm_gb300 as F
@@ -265,55 +474,12 @@ def run_ours(a, d):
     l2buf = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda:%d" % d.local)
     for _ in range(max(3, a.warmup)):
         eng.pc_skeleton(alpha=a.alpha, depth=depth)
-    clocks = Clocks(d.local)
-    clocks.start()
-    d.barrier()
-    torch.cuda.synchronize()
-    tests = 0
-    span_ms = 0.0
-    count_ms = 0.0
-    count_bytes = 0.0
-    count_launches = 0
-    large_ms = 0.0
-    large_bytes = 0.0
-    launches = 0
-    last = None
-    for _ in range(a.steps):
-        flush_l2(l2buf)
-        st = eng.pc_skeleton(alpha=a.alpha, depth=depth).to_dict()
-        tests += sum(st["tests"])
-        span_ms += st["span_ms"]
-        count_ms += st["count_ms"]
-        count_bytes += st["count_bytes"]
-        count_launches += st["count_launches"]
-        large_ms += st["large_ms"]
-        large_bytes += st["large_bytes"]
-        launches += st["kernel_launches"]
-        last = st
-    torch.cuda.synchronize()
-    d.barrier()
-    clk = clocks.stop()
-    t_max = d.max(span_ms / 1e3)
-    tests_all = d.sum(tests)
+    tot = skeleton_run(eng, a, depth, a.steps, l2buf, clocks=Clocks(d.local), d=d)
+    t_max = d.max(tot["span_ms"] / 1e3)
+    tests_all = d.sum(tot["tests"])
     value = tests_all / t_max
-    # end to end through the C ABI with host buffers: samples from pinned host memory
-    # (upload + relabel), the skeleton, and the adjacency + sepset arrays back to the host
-    pinned = [torch.from_numpy(raw).pin_memory().numpy() for raw in data]
-    e2e_secs = 0.0
-    e2e_tests = 0
-    res = None
-    for _ in range(a.steps):
-        flush_l2(l2buf)
-        t0 = time.perf_counter()
-        upload(eng, pinned)
-        st = eng.pc_skeleton(alpha=a.alpha, depth=depth).to_dict()
-        res = eng.result_arrays()
-        e2e_secs += time.perf_counter() - t0
-        e2e_tests += sum(st["tests"])
+    e2e_tests, e2e_secs, d2h = e2e_run(eng, a, data, depth, a.steps, l2buf)
     e2e = d.sum(e2e_tests) / d.max(e2e_secs)
-    n = sum(r.shape[0] for r in data)
-    W = (n + 31) // 32
-    d2h = n * W * 4 + len(res["removed"]) * 16 + len(res["sep_vars"]) * 4
     # plain one-launch-per-test kernel
     plain = None
     if not a.no_plain:
@@ -322,31 +488,12 @@ def run_ours(a, d):
         plain = {"value": pt / (st["span_ms"] / 1e3), "unit": "CI tests/s", "ms": st["span_ms"],
                  "kernel_launches": st["kernel_launches"]}
     peak, peak_kind = peaks()
-    # the two counting kernels, timed with CUDA events on the engine's stream; the roofline
-    # object describes the one with the larger share of device time
-    kernels = []
-    for name, desc, members, ms, nbytes in (
-            ("ci_warp_kernel", "classify + warp-per-test + CTA-per-test kernels, shared-memory tables",
-             ("ci_warp_kernel",), count_ms, count_bytes),
-            ("ci_compact_kernel+ci_part_kernel",
-             "tier 2, joint tables beyond shared memory: hashed strata (compact kernel) and, for tests of "
-             "65,536+ samples whose strata overflow its shared hash, partitioned strata (partition kernel)",
-             ("ci_part_kernel", "ci_compact_kernel"), large_ms, large_bytes)):
-        if ms <= 0:
-            continue
-        ach = nbytes / (ms / 1e3) / 1e9
-        tr = profiled_traffic(members, a.config)
-        kernels.append({"kernel": name, "what": desc, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                        "frac": ach / peak, "peak_kind": peak_kind, "kernel_ms": ms, "algorithmic_bytes": nbytes,
-                        "launches": count_launches if name == "ci_warp_kernel" else None,
-                        "traffic": tr[0] if tr else None,
-                        "traffic_launch_algorithmic_bytes": tr[1] if tr else None,
-                        "traffic_kernel": tr[2] if tr else None})
-    kernels.sort(key=lambda k: -k["kernel_ms"])
-    roofline = dict(kernels[0])
+    kernels = kernel_groups(tot, a.config, peak, peak_kind)
+    roofline = dict(kernels[0]) if kernels else {"kernel": None}
     roofline["others"] = kernels[1:]
     roofline["counting_phase"] = counting_phase([(k["kernel_ms"], k["algorithmic_bytes"]) for k in kernels], peak)
-    cpu = None
+    roofline["tensor"] = gram_roofline(tot)
+    cpu, sample_gpu = None, None
     if d.rank == 0 and d.world == 1 and not a.no_cpu:
         threads = os.cpu_count() or 1
         sample, what = cpu_sample(data)
@@ -354,7 +501,19 @@ def run_ours(a, d):
         what = what or "one full %s skeleton" % a.config
         cpu = {"value": t / s, "unit": "CI tests/s", "cores": threads, "kind": "port",
                "sample": "%s (%d tests, %.1f s)" % (what, t, s)}
+        if len(sample) < len(data):  # the GPU on the very datasets the CPU timed
+            with F.Engine(d.local) as e2:
+                upload(e2, sample)
+                e2.pc_skeleton(alpha=a.alpha, depth=depth)
+                ts = skeleton_run(e2, a, depth, 2, l2buf)
+            sample_gpu = {"value": ts["tests"] / (ts["span_ms"] / 1e3), "unit": "CI tests/s",
+                          "tests_per_step": ts["tests"] // 2, "sample": what}
     eng.close()
+    ns, wall = None, None
+    if d.rank == 0 and d.world == 1 and not a.no_north_star and a.config != "c4":
+        ns = north_star_c4(a, l2buf, peak, peak_kind)
+    if d.rank == 0 and d.world == 1 and not a.no_wall:
+        wall = wall_bnsl(["c2", "c4"])
     if d.rank != 0:
         return
     line = {
@@ -363,22 +522,24 @@ def run_ours(a, d):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u8 data, int32 counts, fp32 G2 (fp64 p-value and band recheck)",
         "data": "synthetic (seeded random DAG + Dirichlet CPTs, forward sampled)",
-        "config": {"workload": WORKLOADS[a.config], "alpha": a.alpha, "tests_per_step": tests // a.steps,
-                   "levels": last["n_levels"], "tests_per_level": last["tests"],
-                   "tests_executed_per_level": last["tests_executed"], "edges_after": last["edges_after"],
-                   "waves": last["waves"], "level_ms": [round(x, 3) for x in last["ms"]],
-                   "large_table_ms": last["large_ms"], "l2": "flushed before each timed step (512 MB write)",
-                   "parallelism": "replicas" if a.gpus > 1 else "single GPU"},
+        "config": bench_config(a, depth),
+        "tests_per_step": tot["tests"] // a.steps,
+        "l2": "flushed before each timed step (512 MB write)",
+        "levels": level_record(tot["last"]),
         "e2e": {"value": e2e, "unit": "CI tests/s", "h2d_bytes_per_step": int(sum(r.nbytes for r in data)),
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": launches,
+        "gpu_launches": tot["kernel_launches"],
         "roofline": roofline,
         "plain": plain,
         "speedup_vs_plain": (value / plain["value"]) if plain else None,
-        "precision": {"fp64_rechecks": last["rechecks"], "near_ties": last["near_ties"],
-                      "max_abs_dp_fp32_vs_fp64": last["max_abs_dp"], "large_tests": last["large_tests"]},
+        "precision": {"fp64_rechecks": tot["last"]["rechecks"], "near_ties": tot["last"]["near_ties"],
+                      "max_abs_dp_fp32_vs_fp64": tot["last"]["max_abs_dp"],
+                      "large_tests": tot["last"]["large_tests"]},
         "cpu_baseline": cpu,
-        "clocks": clk,
+        "gpu_on_cpu_sample": sample_gpu,
+        "north_star": ns,
+        "wall": wall,
+        "clocks": tot["clocks"],
     }
     print(json.dumps(line))
 

@@ -42,7 +42,8 @@ class PCStats(ctypes.Structure):
                 ("near_ties", ctypes.c_int64), ("large_tests", ctypes.c_int64), ("max_abs_dp", ctypes.c_double),
                 ("count_ms", ctypes.c_double), ("count_bytes", ctypes.c_double), ("large_ms", ctypes.c_double),
                 ("count_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("span_ms", ctypes.c_double),
-                ("total_ms", ctypes.c_double), ("large_bytes", ctypes.c_double)]
+                ("total_ms", ctypes.c_double), ("large_bytes", ctypes.c_double), ("gram_ms", ctypes.c_double),
+                ("gram_flops", ctypes.c_double), ("gram_tests", ctypes.c_int64)]
 
     def to_dict(self):
         L = self.n_levels
@@ -56,7 +57,8 @@ class PCStats(ctypes.Structure):
                 "large_ms": float(self.large_ms),
                 "count_launches": int(self.count_launches), "kernel_launches": int(self.kernel_launches),
                 "span_ms": float(self.span_ms), "total_ms": float(self.total_ms),
-                "large_bytes": float(self.large_bytes)}
+                "large_bytes": float(self.large_bytes), "gram_ms": float(self.gram_ms),
+                "gram_flops": float(self.gram_flops), "gram_tests": int(self.gram_tests)}
 
 
 class GenSpec(ctypes.Structure):

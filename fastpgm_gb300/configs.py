@@ -38,10 +38,12 @@ def c5_jobs(seed=5, n_jobs=64):
     return jobs
 
 
-def make_jobs(jobs):
+def make_jobs(jobs, generate=None):
     """Generate the datasets of a list of job parameter dicts (c5_jobs()).  Returns
-    (list of raw uint8 [n_j, S_j], depth)."""
-    from . import generate
+    (list of raw uint8 [n_j, S_j], depth).  generate: the sampler to call (default the
+    engine library's; any function with fastpgm_gb300.generate's signature and output)."""
+    if generate is None:
+        from . import generate
     out, depth = [], 1000
     for spec in jobs:
         spec = dict(spec)
@@ -64,9 +66,11 @@ def split_jobs(result, offsets):
     return out
 
 
-def make_config(name, n_samples=None, n_nodes=None):
-    """Generate a config's data.  Returns (columns raw uint8 [n,S], depth, spec dict)."""
-    from . import generate
+def make_config(name, n_samples=None, n_nodes=None, generate=None):
+    """Generate a config's data.  Returns (columns raw uint8 [n,S], depth, spec dict).
+    generate: the sampler to call (default the engine library's)."""
+    if generate is None:
+        from . import generate
     spec = dict(CONFIGS[name])
     if n_samples is not None:
         spec["n_samples"] = n_samples

@@ -14,8 +14,10 @@
 //
 // Tiers 0/1 count with 128-bit column loads folded into packed 16-bit Horner
 // codes (two samples per 32-bit multiply-add) and shared-memory atomics into R
-// replicas of the table laid out with an odd stride, so lanes of a warp that
-// hit the same cell land in different banks.
+// replicas of the table interleaved cell by cell (cell c of replica r at c*R + r):
+// lane l adds into replica l mod R, so with R = 32 each lane owns one bank and a
+// warp's increments never conflict, whichever cells they hit; the replicas are
+// then summed into the dense table.
 #pragma once
 #include "ci_device.cuh"
 
@@ -24,12 +26,33 @@ namespace fpgm {
 // counters[] slots (int32)
 // C_PART / C_RETRY: tier-2 tests handed to the partitioned kernel, and from it back to the
 // compact kernel's global hash (lists 3-4 and 5 of WaveArgs::lists)
-enum { C_TIER0 = 0, C_TIER1, C_TIER2, C_WORK0, C_WORK1, C_WORK2, C_PART, C_WORKP, C_RETRY, C_WORKR, C_COUNT };
+// C_WIDET / C_WIDEQ / C_WIDEW: tests published for partition-parallel scoring, the
+// (test, partition) items queued for it, and the items taken
+enum { C_TIER0 = 0, C_TIER1, C_TIER2, C_WORK0, C_WORK1, C_WORK2, C_PART, C_WORKP, C_RETRY, C_WORKR, C_WIDET, C_WIDEQ,
+       C_WIDEW, C_COUNT };
+static_assert(C_COUNT <= 16, "counters are cleared as 64 bytes");
 // stats[] slots (unsigned long long)
+// ST_TIMEOUT: a bounded device wait gave up (the tensor-core level-0 kernel)
 enum { ST_RECHECK = 0, ST_NEARTIE, ST_LARGE, ST_MAXDP, ST_UNSUPPORTED, ST_DET, ST_EXEC, ST_UNRESOLVED,
-       ST_REMOVED, ST_MAXDEG, ST_TIER0, ST_TIER1, ST_TIER2, ST_BYTES_SHARED, ST_BYTES_LARGE, ST_COUNT };
+       ST_REMOVED, ST_MAXDEG, ST_TIER0, ST_TIER1, ST_TIER2, ST_BYTES_SHARED, ST_BYTES_LARGE, ST_TIMEOUT, ST_COUNT };
 
 enum { SRC_WAVE = 0, SRC_EXPLICIT = 1 };
+
+constexpr int kPartMaxLog = 8;  // at most 256 partitions per partitioned test
+constexpr int kPartMax = 1 << kPartMaxLog;
+
+// A partitioned test published for partition-parallel scoring: its records stay in the
+// owner CTA's slot, every (test, partition) pair is a queue item that any CTA may take, the
+// partial statistics are summed here, and the CTA that finishes the last partition decides.
+struct WideTest {
+    int32_t item, owner, lp, code32, dx, dy, n_items;
+    int32_t done, over, n_obs;  // partitions finished; a partition overflowed; strata seen
+    unsigned long long df;
+    double g2, err, abs_g2;
+    unsigned long long hash;
+    int32_t pcnt[kPartMax];      // records per partition
+    int32_t poff[kPartMax + 1];  // first record of each partition (runs padded to 8 records)
+};
 
 struct WaveArgs {
     const uint8_t *cols;
@@ -69,6 +92,14 @@ struct WaveArgs {
     int32_t hash_cap_global;  // power of two >= 2 * slot_S
     unsigned long long *dbg;  // compact-tier phase timers (FPGM_PHASE_TIMERS), else null
     int32_t part_max_log;     // partitioned kernel: at most 2^part_max_log partitions (<= kPartMaxLog)
+    // partition-parallel scoring (null: every partitioned test stays on its own CTA)
+    WideTest *wide;           // one per CTA of the partition kernel
+    int32_t *wide_items;      // (test << 8) | partition, kPartMax per test
+    int32_t wide_small_n2;    // tests of fewer than kPartMinSamples samples are partitioned too when
+                              // the wave has at most this many tier-2 tests (0: never)
+    int32_t wide_min_log;     // least partitions (log2) of a published test
+    int32_t wide_part_min;    // published tests are split no finer than this many samples per partition
+    int32_t wide_direct;      // in such a wave, hand every tier-2 test over before any hashing
 };
 
 __device__ inline int upper_bound_i32(const int32_t *a, int n, int v) {
@@ -234,42 +265,45 @@ __global__ void __launch_bounds__(kThreads, 2) ci_warp_kernel(WaveArgs a) {
         const int dz = (int)cells / (dx * dy);
         __syncwarp();
         const int marg = dz * (dx + dy + 1);
-        const int stride = (int)cells | 1;
-        int R = 1;
-        for (int r = 32; r >= 2; r >>= 1)
-            if (stride * r + marg <= kWarpInts) { R = r; break; }
-        int *tab = wreg;
-        int *ni = wreg + stride * R, *nj = ni + dz * dx, *nk = nj + dz * dy;
-        for (int i = lane; i < stride * R; i += 32) tab[i] = 0;
+        int lgR = 0;  // replicas: 2^lgR interleaved copies of the table, then the reduced table
+        for (int l = 5; l >= 1; --l)
+            if (((int)cells << l) + (int)cells + marg <= kWarpInts) { lgR = l; break; }
+        const int R = 1 << lgR;
+        int *rep = wreg;                                  // cell c of replica r at rep[c * R + r]
+        int *tab = R > 1 ? wreg + ((int)cells << lgR) : wreg;  // dense table in reference cell order
+        int *ni = tab + cells, *nj = ni + dz * dx, *nk = nj + dz * dy;
+        for (int i = lane; i < ((int)cells << lgR); i += 32) rep[i] = 0;
         __syncwarp();
-        int *mytab = tab + (lane & (R - 1)) * stride;
+        // lane l counts into replica l mod R: with 32 replicas every lane owns one bank, so a
+        // warp's 32 increments never conflict whatever cells they hit
+        int *myrep = rep + (lane & (R - 1));
         for (int64_t v = lane; v < nvec; v += 64) {
             const bool two = v + 32 < nvec;
             uint32_t ca[8], cb[8];
             horner_pair(ca, cb, s_col[warp], s_dim[warp], ncols, v, v + 32, two);
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                atomicAdd(&mytab[ca[q] & 0xffffu], 1);
-                atomicAdd(&mytab[ca[q] >> 16], 1);
+                atomicAdd(&myrep[(ca[q] & 0xffffu) << lgR], 1);
+                atomicAdd(&myrep[(ca[q] >> 16) << lgR], 1);
             }
             if (two) {
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
-                    atomicAdd(&mytab[cb[q] & 0xffffu], 1);
-                    atomicAdd(&mytab[cb[q] >> 16], 1);
+                    atomicAdd(&myrep[(cb[q] & 0xffffu) << lgR], 1);
+                    atomicAdd(&myrep[(cb[q] >> 16) << lgR], 1);
                 }
             }
         }
         for (int64_t s = (S & ~(int64_t)15) + lane; s < S; s += 32) {
             uint32_t c = 0;
             for (int j = 0; j < ncols; ++j) c = c * s_dim[warp][j] + s_col[warp][j][s];
-            atomicAdd(&mytab[c], 1);
+            atomicAdd(&myrep[c << lgR], 1);
         }
         __syncwarp();
         if (R > 1) {
             for (int c = lane; c < (int)cells; c += 32) {
                 int s = 0;
-                for (int r = 0; r < R; ++r) s += tab[r * stride + c];
+                for (int r = 0; r < R; ++r) s += rep[(c << lgR) + r];
                 tab[c] = s;
             }
             __syncwarp();
@@ -311,42 +345,43 @@ __global__ void __launch_bounds__(kThreads, 2) ci_cta_kernel(WaveArgs a) {
         const int dx = s_dim[d], dy = s_dim[d + 1];
         const int dz = cells / (dx * dy);
         const int marg = dz * (dx + dy + 1);
-        const int stride = cells | 1;
-        int R = 1;
-        for (int r = 32; r >= 2; r >>= 1)
-            if (stride * r + marg <= kCtaInts) { R = r; break; }
-        int *tab = smem;
-        int *ni = smem + stride * R, *nj = ni + dz * dx, *nk = nj + dz * dy;
-        for (int i = tid; i < stride * R; i += kThreads) tab[i] = 0;
+        int lgR = 0;  // replicas interleaved cell by cell, as in the warp tier
+        for (int l = 5; l >= 1; --l)
+            if ((cells << l) + cells + marg <= kCtaInts) { lgR = l; break; }
+        const int R = 1 << lgR;
+        int *rep = smem;
+        int *tab = R > 1 ? smem + (cells << lgR) : smem;
+        int *ni = tab + cells, *nj = ni + dz * dx, *nk = nj + dz * dy;
+        for (int i = tid; i < (cells << lgR); i += kThreads) rep[i] = 0;
         __syncthreads();
-        int *mytab = tab + (lane & (R - 1)) * stride;
+        int *myrep = rep + (lane & (R - 1));
         for (int64_t v = tid; v < nvec; v += 2 * kThreads) {
             const bool two = v + kThreads < nvec;
             uint32_t ca[8], cb[8];
             horner_pair(ca, cb, s_col, s_dim, ncols, v, v + kThreads, two);
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                atomicAdd(&mytab[ca[q] & 0xffffu], 1);
-                atomicAdd(&mytab[ca[q] >> 16], 1);
+                atomicAdd(&myrep[(ca[q] & 0xffffu) << lgR], 1);
+                atomicAdd(&myrep[(ca[q] >> 16) << lgR], 1);
             }
             if (two) {
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
-                    atomicAdd(&mytab[cb[q] & 0xffffu], 1);
-                    atomicAdd(&mytab[cb[q] >> 16], 1);
+                    atomicAdd(&myrep[(cb[q] & 0xffffu) << lgR], 1);
+                    atomicAdd(&myrep[(cb[q] >> 16) << lgR], 1);
                 }
             }
         }
         for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
             uint32_t c = 0;
             for (int j = 0; j < ncols; ++j) c = c * s_dim[j] + s_col[j][s];
-            atomicAdd(&mytab[c], 1);
+            atomicAdd(&myrep[c << lgR], 1);
         }
         __syncthreads();
         if (R > 1) {
             for (int c = tid; c < cells; c += kThreads) {
                 int s = 0;
-                for (int r = 0; r < R; ++r) s += tab[r * stride + c];
+                for (int r = 0; r < R; ++r) s += rep[(c << lgR) + r];
                 tab[c] = s;
             }
             __syncthreads();
@@ -776,8 +811,6 @@ __device__ __forceinline__ unsigned long long gtimer() {
 // partition holds more samples than the shared sorted array).
 // Shared-memory plan (kSmemBytes, PartPlan<K>): keys K[cap] at 0 and A int[cap] after them
 // (per-warp x,y tables once pass 2 is done), occ int[lim], E int[lim + 1], sorted codes u16[].
-constexpr int kPartMaxLog = 8;                     // at most 256 partitions
-constexpr int kPartMax = 1 << kPartMaxLog;
 constexpr int kPartProbe = 256;                   // probe bound of the first pass
 // Tests of fewer samples keep the compact kernel's global hash: measured on GB300, the
 // partitioned path wins at 100,000 samples (1,041 nodes, cards 2-21: 3.85 vs 3.40 M tests/s)
@@ -932,27 +965,19 @@ __device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint3
     __syncthreads();
 }
 
-__device__ __forceinline__ void partial_add(Partial &a, const Partial &b) {
-    a.df += b.df;
-    a.g2 += b.g2;
-    a.err += b.err;
-    a.abs_g2 += b.abs_g2;
-    a.hash += b.hash;
-}
-
-// Counts and scores every partition in shared memory; returns this thread's share of the
-// statistic.  *s_over is set when a partition's codes overflow its table (first pass only:
-// the FP64 recheck probes without bound, so it cannot fail where the first pass did not).
-// Thread 0 adds the strata it saw to claims.
+// Counts and scores one partition (n records from rec_z/rec_xy + base) in shared memory;
+// returns this thread's share of the statistic.  *s_over is set when the partition's codes
+// overflow its table (first pass only: the FP64 recheck probes without bound, so it cannot
+// fail where the first pass did not).  Thread 0 adds the strata it saw to claims.  Every
+// thread of the CTA calls it; it ends on a barrier, so shared memory is free afterwards.
 template <bool kFp64, class K>
-__device__ __noinline__ Partial part_run(int lp, const K *rec_z, const uint16_t *rec_xy, const int *s_pcnt,
-                                         const int *s_poff, int dx, int dy, unsigned char *smem, uint16_t *gord,
-                                         int *gwt, uint64_t *gzk, bool want_hash, int *s_w, int *s_over,
-                                         int *s_nbig, int *s_nocc, int *s_bin, int &claims,
-                                         unsigned long long *dbg) {
+__device__ __noinline__ Partial part_partition(int lp, const K *rec_z, const uint16_t *rec_xy, int n, int base,
+                                               int dx, int dy, unsigned char *smem, uint16_t *gord, int *gwt,
+                                               uint64_t *gzk, bool want_hash, int *s_w, int *s_over, int *s_nbig,
+                                               int *s_nocc, int *s_bin, int &claims, unsigned long long *dbg) {
     using Plan = PartPlan<K>;
     constexpr uint32_t cap = Plan::cap;
-    const int tid = threadIdx.x, warp = tid >> 5, P = 1 << lp;
+    const int tid = threadIdx.x, warp = tid >> 5;
     K *keys = reinterpret_cast<K *>(smem);
     int *A = reinterpret_cast<int *>(smem + Plan::a_off);
     int *occ = reinterpret_cast<int *>(smem + Plan::occ_off);
@@ -973,114 +998,134 @@ __device__ __noinline__ Partial part_run(int lp, const K *rec_z, const uint16_t 
             tp = t;
         }
     };
-    if (dbg && tid == 0) atomicAdd(&dbg[22], (unsigned long long)P);
+    for (uint32_t i = tid; i < cap; i += kThreads) {
+        keys[i] = (K)kEmptyKey;
+        A[i] = 0;
+    }
+    if (tid == 0) *s_nocc = 0;
+    if (tid < 10) s_bin[tid] = 0;
+    __syncthreads();
+    lap(16);
+    // pass 1: first probes of eight codes at once; misses take the inserting path
+    const int ngroups = (n + 7) >> 3;
+    for (int g = tid; g < ngroups; g += kThreads) {
+        K z[8];
+        load8(z, rec_z + base + 8 * g);
+        const int m = n - 8 * g;
+        uint32_t h[8];
+        K k0[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            h[j] = part_slot(z[j], lp, Plan::lcap);
+            k0[j] = j < m ? keys[h[j]] : z[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (j >= m) break;
+            int hj = (int)h[j];
+            if (k0[j] != z[j]) hj = part_insert(keys, cap, h[j], z[j], max_probe, occ, s_nocc, lim);
+            if (hj < 0) {
+                *s_over = 1;
+                break;
+            }
+            atomicAdd(&A[hj], 1);
+        }
+    }
+    __syncthreads();
+    lap(17);
+    if (*s_over == 0) {
+        const int n_occ = *s_nocc;
+        if (tid == 0) claims += n_occ;
+        // strata ranked by size: bins 1..8 samples, 9 for larger ones
+        for (int i = tid; i < n_occ; i += kThreads) atomicAdd(&s_bin[min(A[occ[i]], 9)], 1);
+        __syncthreads();
+        if (tid == 0) {
+            int run = 0;
+            for (int b = 1; b < 10; ++b) {
+                const int c = s_bin[b];
+                s_bin[b] = run;
+                run += c;
+            }
+            E[0] = 0;
+        }
+        __syncthreads();
+        for (int i = tid; i < n_occ; i += kThreads) {
+            const int sl = occ[i], m = A[sl];
+            const int r = atomicAdd(&s_bin[min(m, 9)], 1);
+            E[1 + r] = m;
+            A[sl] = r;
+            if (want_hash) gzk[r] = (uint64_t)keys[sl];
+        }
+        __syncthreads();
+        block_exclusive_scan(E + 1, n_occ, s_w);
+        lap(18);
+        uint16_t *ord = n <= Plan::ord_cap ? sord : gord + base;
+        for (int g = tid; g < ngroups; g += kThreads) {
+            K z[8];
+            load8(z, rec_z + base + 8 * g);
+            const uint4 c = __ldcg(reinterpret_cast<const uint4 *>(rec_xy + base) + g);
+            const uint32_t cw[4] = {c.x, c.y, c.z, c.w};
+            const int m = n - 8 * g;
+            uint32_t h[8];
+            K k0[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                h[j] = part_slot(z[j], lp, Plan::lcap);
+                k0[j] = j < m ? keys[h[j]] : z[j];
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                if (j >= m) break;
+                const int hj = k0[j] == z[j] ? (int)h[j] : part_find(keys, cap, h[j], z[j]);
+                const int pos = atomicAdd(&E[1 + A[hj]], 1);
+                ord[pos] = (uint16_t)(cw[j >> 1] >> (16 * (j & 1)));
+            }
+        }
+        __syncthreads();
+        lap(19);
+        if (wsmem)  // keys and A are dead: per-warp x,y tables
+            for (int i = tid; i < Plan::occ_off / 4; i += kThreads) reinterpret_cast<int *>(smem)[i] = 0;
+        if (tid == 0) *s_nbig = 0;
+        __syncthreads();
+        // the larger strata are listed over occ[] (dead since the index step)
+        Partial q = score_small_strata<kFp64>(E, ord, n_occ, dx, dy, occ, s_nbig, gzk, want_hash, true);
+        __syncthreads();
+        lap(20);
+        const int n_big = *s_nbig;
+        acc = score_big_strata<kFp64>(q, E, ord, occ, n_big, dx, dy, wt, gzk, want_hash);
+    }
+    __syncthreads();  // before the next partition reuses shared memory
+    lap(21);
+    return acc;
+}
+
+__device__ __forceinline__ void partial_add(Partial &a, const Partial &b) {
+    a.df += b.df;
+    a.g2 += b.g2;
+    a.err += b.err;
+    a.abs_g2 += b.abs_g2;
+    a.hash += b.hash;
+}
+
+// Counts and scores every partition of a test in shared memory, one after another; returns
+// this thread's share of the statistic (see part_partition; stops at the first overflow).
+// s_pcnt / s_poff: records per partition and each partition's first record.
+template <bool kFp64, class K>
+__device__ __noinline__ Partial part_run(int lp, const K *rec_z, const uint16_t *rec_xy, const int *s_pcnt,
+                                         const int *s_poff, int dx, int dy, unsigned char *smem, uint16_t *gord,
+                                         int *gwt, uint64_t *gzk, bool want_hash, int *s_w, int *s_over,
+                                         int *s_nbig, int *s_nocc, int *s_bin, int &claims,
+                                         unsigned long long *dbg) {
+    const int P = 1 << lp;
+    Partial acc{0, 0.0, 0.0, 0.0, 0ull};
+    if (dbg && threadIdx.x == 0) atomicAdd(&dbg[22], (unsigned long long)P);
     for (int p = 0; p < P; ++p) {
         const int n = s_pcnt[p];
-        bool over = false;
-        if (n > 0) {
-            const int base = s_poff[p];
-            for (uint32_t i = tid; i < cap; i += kThreads) {
-                keys[i] = (K)kEmptyKey;
-                A[i] = 0;
-            }
-            if (tid == 0) *s_nocc = 0;
-            if (tid < 10) s_bin[tid] = 0;
-            __syncthreads();
-            lap(16);
-            // pass 1: first probes of eight codes at once; misses take the inserting path
-            const int ngroups = (n + 7) >> 3;
-            for (int g = tid; g < ngroups; g += kThreads) {
-                K z[8];
-                load8(z, rec_z + base + 8 * g);
-                const int m = n - 8 * g;
-                uint32_t h[8];
-                K k0[8];
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    h[j] = part_slot(z[j], lp, Plan::lcap);
-                    k0[j] = j < m ? keys[h[j]] : z[j];
-                }
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    if (j >= m) break;
-                    int hj = (int)h[j];
-                    if (k0[j] != z[j]) hj = part_insert(keys, cap, h[j], z[j], max_probe, occ, s_nocc, lim);
-                    if (hj < 0) {
-                        *s_over = 1;
-                        break;
-                    }
-                    atomicAdd(&A[hj], 1);
-                }
-            }
-            __syncthreads();
-            lap(17);
-            over = *s_over != 0;
-            if (!over) {
-                const int n_occ = *s_nocc;
-                if (tid == 0) claims += n_occ;
-                // strata ranked by size: bins 1..8 samples, 9 for larger ones
-                for (int i = tid; i < n_occ; i += kThreads) atomicAdd(&s_bin[min(A[occ[i]], 9)], 1);
-                __syncthreads();
-                if (tid == 0) {
-                    int run = 0;
-                    for (int b = 1; b < 10; ++b) {
-                        const int c = s_bin[b];
-                        s_bin[b] = run;
-                        run += c;
-                    }
-                    E[0] = 0;
-                }
-                __syncthreads();
-                for (int i = tid; i < n_occ; i += kThreads) {
-                    const int sl = occ[i], m = A[sl];
-                    const int r = atomicAdd(&s_bin[min(m, 9)], 1);
-                    E[1 + r] = m;
-                    A[sl] = r;
-                    if (want_hash) gzk[r] = (uint64_t)keys[sl];
-                }
-                __syncthreads();
-                block_exclusive_scan(E + 1, n_occ, s_w);
-                lap(18);
-                uint16_t *ord = n <= Plan::ord_cap ? sord : gord + base;
-                for (int g = tid; g < ngroups; g += kThreads) {
-                    K z[8];
-                    load8(z, rec_z + base + 8 * g);
-                    const uint4 c = __ldcg(reinterpret_cast<const uint4 *>(rec_xy + base) + g);
-                    const uint32_t cw[4] = {c.x, c.y, c.z, c.w};
-                    const int m = n - 8 * g;
-                    uint32_t h[8];
-                    K k0[8];
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        h[j] = part_slot(z[j], lp, Plan::lcap);
-                        k0[j] = j < m ? keys[h[j]] : z[j];
-                    }
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        if (j >= m) break;
-                        const int hj = k0[j] == z[j] ? (int)h[j] : part_find(keys, cap, h[j], z[j]);
-                        const int pos = atomicAdd(&E[1 + A[hj]], 1);
-                        ord[pos] = (uint16_t)(cw[j >> 1] >> (16 * (j & 1)));
-                    }
-                }
-                __syncthreads();
-                lap(19);
-                if (wsmem)  // keys and A are dead: per-warp x,y tables
-                    for (int i = tid; i < Plan::occ_off / 4; i += kThreads) reinterpret_cast<int *>(smem)[i] = 0;
-                if (tid == 0) *s_nbig = 0;
-                __syncthreads();
-                // the larger strata are listed over occ[] (dead since the index step)
-                Partial q = score_small_strata<kFp64>(E, ord, n_occ, dx, dy, occ, s_nbig, gzk, want_hash, true);
-                __syncthreads();
-                lap(20);
-                const int n_big = *s_nbig;
-                q = score_big_strata<kFp64>(q, E, ord, occ, n_big, dx, dy, wt, gzk, want_hash);
-                partial_add(acc, q);
-            }
-            __syncthreads();  // before the next partition reuses shared memory
-            lap(21);
-        }
-        if (over) break;
+        if (n == 0) continue;
+        const Partial q = part_partition<kFp64, K>(lp, rec_z, rec_xy, n, s_poff[p], dx, dy, smem, gord, gwt, gzk,
+                                                   want_hash, s_w, s_over, s_nbig, s_nocc, s_bin, claims, dbg);
+        if (*s_over) break;  // read after part_partition's closing barrier, same in every thread
+        partial_add(acc, q);
     }
     return acc;
 }
@@ -1206,12 +1251,25 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         uint32_t cap = code32 ? (uint32_t)kZCap32 : (uint32_t)kZCap64;
         uint32_t *hkeys32 = reinterpret_cast<uint32_t *>(hkeys);
         bool deferred = false;  // handed to the partitioned kernel
+        if (!kRetry && a.wide != nullptr && a.wide_direct && n2 <= a.wide_small_n2) {
+            // A wave of few tier-2 tests: every one goes straight to the partition-parallel
+            // path, with min(dz, samples) as its strata bound, so no CTA spends the wave on
+            // one test's hash or strata scoring alone.
+            if (tid == 0) {
+                const double est = fmin((double)dz, (double)S);
+                const int q = atomicAdd(&a.counters[C_PART], 1);
+                a.lists[3 * a.list_cap + q] = item;
+                a.lists[4 * a.list_cap + q] = __float_as_int((float)est);
+            }
+            __syncthreads();
+            continue;
+        }
         for (int attempt = kRetry ? 2 : 0; attempt < 3; ++attempt) {
             global = attempt >= 1;
             const bool k32 = !global && code32;
             if (attempt == 1) {
                 const double est = (double)zlimit * (double)(nvec > 1 ? nvec : 1) / (double)(seen > 1 ? seen : 1);
-                if (S >= kPartMinSamples) {
+                if (S >= kPartMinSamples || (a.wide != nullptr && n2 <= a.wide_small_n2)) {
                     if (tid == 0) {
                         const int q = atomicAdd(&a.counters[C_PART], 1);
                         a.lists[3 * a.list_cap + q] = item;
@@ -1508,6 +1566,55 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
         int lp = 1;
         const int maxlog = a.part_max_log;
         while ((double)(1 << lp) < fmax(est / (0.3 * capmax), (double)S / (0.5 * ordcap)) && lp < maxlog) ++lp;
+        if (a.wide != nullptr && idx >= np - (int)gridDim.x) {
+            // One of the list's last tests (all of them when there are no more tests than
+            // CTAs): its records are written here, then its partitions are queued for
+            // ci_part_wide_kernel, which scores them on whichever CTAs are free.  This CTA
+            // takes no further test, so its slot keeps the records.
+            const int nw = np < (int)gridDim.x ? np : (int)gridDim.x;
+            int lw = lp > a.wide_min_log ? lp : a.wide_min_log;
+            if (lw > maxlog) lw = maxlog;
+            while ((1 << lw) * nw < 2 * (int)gridDim.x && lw < maxlog && (S >> (lw + 1)) >= a.wide_part_min) ++lw;
+            if (code32)
+                part_scatter(s_col, s_dim, d, S, lw, reinterpret_cast<uint32_t *>(rz), rxy, s_pcnt, s_poff, s_pcur);
+            else
+                part_scatter(s_col, s_dim, d, S, lw, reinterpret_cast<uint64_t *>(rz), rxy, s_pcnt, s_poff, s_pcur);
+            FPGM_PHASE(14);
+            if (tid == 0) s_idx = atomicAdd(&a.counters[C_WIDET], 1);
+            __syncthreads();
+            WideTest *w = a.wide + s_idx;
+            const int P = 1 << lw;
+            for (int i = tid; i < P; i += kThreads) {
+                w->pcnt[i] = s_pcnt[i];
+                w->poff[i] = s_poff[i];
+            }
+            if (tid == 0) {
+                w->poff[P] = s_poff[P];
+                int nne = 0;
+                for (int i = 0; i < P; ++i) nne += s_pcnt[i] > 0;
+                w->item = item;
+                w->owner = blockIdx.x;
+                w->lp = lw;
+                w->code32 = code32;
+                w->dx = dx;
+                w->dy = dy;
+                w->n_items = nne;
+                w->done = 0;
+                w->over = 0;
+                w->n_obs = 0;
+                w->df = 0ull;
+                w->g2 = 0.0;
+                w->err = 0.0;
+                w->abs_g2 = 0.0;
+                w->hash = 0ull;
+                const int q0 = atomicAdd(&a.counters[C_WIDEQ], nne);
+                for (int i = 0, q = q0; i < P; ++i)
+                    if (s_pcnt[i] > 0) a.wide_items[q++] = (s_idx << 8) | i;
+                if (a.dbg) atomicAdd(&a.dbg[23], 1ull);
+            }
+            __syncthreads();
+            break;
+        }
         Partial acc;
         bool over;
         for (;;) {
@@ -1562,6 +1669,102 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
         __syncthreads();
     }
 #undef FPGM_PHASE
+}
+
+// Partition-parallel scoring of the tests ci_part_kernel published (WideTest): every CTA
+// takes (test, partition) items from the queue, counts and scores that partition in shared
+// memory from the owner CTA's records, and adds its share to the test's sums.  The CTA that
+// finishes a test's last partition decides it -- FP64 recheck over all partitions when the
+// statistic falls inside the band -- or, if any partition overflowed its table, hands the
+// test to the compact kernel's global hash (retry list, ci_compact_kernel<true>).
+__global__ void __launch_bounds__(kThreads, 2) ci_part_wide_kernel(WaveArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_idx, s_over, s_flag, s_nbig, s_nocc, s_last;
+    __shared__ int s_bin[16];
+    __shared__ int s_w[kWarps];
+    __shared__ Partial scratch[kWarps];
+    if (a.wide == nullptr) return;
+    const int tid = threadIdx.x;
+    char *slot = a.slot_mem + (int64_t)blockIdx.x * a.slot_bytes;
+    const SlotLayout L = slot_layout(a.slot_S, (uint32_t)a.hash_cap_global);
+    uint64_t *gzk = reinterpret_cast<uint64_t *>(slot + L.zk);
+    int *gwt = reinterpret_cast<int *>(slot + L.wt);
+    uint16_t *gord = reinterpret_cast<uint16_t *>(slot + L.ord);
+    uint64_t *zk = a.want_hash ? gzk : nullptr;
+    const int nq = a.counters[C_WIDEQ];
+    for (;;) {
+        if (tid == 0) s_idx = atomicAdd(&a.counters[C_WIDEW], 1);
+        __syncthreads();
+        const int idx = s_idx;
+        if (idx >= nq) break;
+        const int code = a.wide_items[idx];
+        WideTest *w = a.wide + (code >> 8);
+        const int p = code & 0xff;
+        const char *own = a.slot_mem + (int64_t)w->owner * a.slot_bytes;
+        const char *rz = own + L.keys;
+        const uint16_t *rxy = reinterpret_cast<const uint16_t *>(own + L.ids);
+        const int lp = w->lp, dx = w->dx, dy = w->dy;
+        const bool code32 = w->code32 != 0;
+        if (tid == 0) s_over = 0;
+        __syncthreads();
+        int claims = 0;
+        const Partial q =
+            code32 ? part_partition<false, uint32_t>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, w->pcnt[p],
+                                                     w->poff[p], dx, dy, smem_raw, gord, gwt, zk, a.want_hash != 0, s_w,
+                                                     &s_over, &s_nbig, &s_nocc, s_bin, claims, nullptr)
+                   : part_partition<false, uint64_t>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, w->pcnt[p],
+                                                     w->poff[p], dx, dy, smem_raw, gord, gwt, zk, a.want_hash != 0, s_w,
+                                                     &s_over, &s_nbig, &s_nocc, s_bin, claims, nullptr);
+        const bool over = s_over != 0;  // read after part_partition's closing barrier
+        const Partial r = block_sum(q, scratch);
+        if (tid == 0) {
+            if (over) {
+                atomicExch(&w->over, 1);
+            } else {
+                atomicAdd(&w->df, r.df);
+                atomicAdd(&w->g2, r.g2);
+                atomicAdd(&w->err, r.err);
+                atomicAdd(&w->abs_g2, r.abs_g2);
+                atomicAdd(&w->hash, r.hash);
+                atomicAdd(&w->n_obs, claims);
+            }
+            __threadfence();  // the sums are visible before the partition counts as done
+            s_last = atomicAdd(&w->done, 1) == w->n_items - 1;
+        }
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            const int item = w->item;
+            if (__ldcg(&w->over)) {
+                if (tid == 0) {
+                    const int qr = atomicAdd(&a.counters[C_RETRY], 1);
+                    a.lists[5 * a.list_cap + qr] = item;
+                }
+            } else {
+                Partial R;
+                R.df = (long long)__ldcg(&w->df);
+                R.g2 = __ldcg(&w->g2);
+                R.err = __ldcg(&w->err);
+                R.abs_g2 = __ldcg(&w->abs_g2);
+                R.hash = __ldcg(&w->hash);
+                const int n_obs = __ldcg(&w->n_obs);
+                if (a.dbg && tid == 0) {
+                    atomicAdd(&a.dbg[9], (unsigned long long)n_obs);
+                    atomicAdd(&a.dbg[13], 1ull);
+                }
+                decide_record(a, item, R, (int64_t)n_obs * dx * dy, 4, s_flag, scratch, [&]() {
+                    int cl = 0;
+                    return code32 ? part_run<true>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, w->pcnt, w->poff,
+                                                   dx, dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over, &s_nbig,
+                                                   &s_nocc, s_bin, cl, nullptr)
+                                  : part_run<true>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, w->pcnt, w->poff,
+                                                   dx, dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over, &s_nbig,
+                                                   &s_nocc, s_bin, cl, nullptr);
+                });
+            }
+        }
+        __syncthreads();
+    }
 }
 
 // ---------------------------------------------------------------- band tables

@@ -127,12 +127,22 @@ struct fpgm_engine {
     DevBuf bits, deg, adjl, edges_x, edges_y, pxy, pyx, cntx, total, next, status, seprank, g, off, flag,
         counters, stats, scan_tmp, log_pair, log_vars, log_meta, node_cnt, node_off;
     DevBuf slots, plain_ws, tests_buf, detail_buf, item_vars, lists, band, phase_timers;
+    DevBuf wide, wide_items;  // partition-parallel scoring: one WideTest per slot, kPartMax items each
     DevBuf mle_counts, mle_pot, mle_meta;  // parameter learning: counts, potentials, per-node tables
     double band_alpha = -1.0;
     int n_slots = 0, hash_cap_global = 0;
     int part_max_log = kPartMaxLog;  // FPGM_PART_MAX_LOG (tests): fewer partitions before the global hash
     int64_t slot_bytes = 0, slot_S = 0;  // slot_S: the sample count the slots' layout was made for
     bool wave_log = false;               // FPGM_WAVE_LOG: one stderr line per wave (tier sizes, kernel times)
+    // level 0 on the tensor cores (FPGM_GRAM=0 keeps it on the counting kernels)
+    GramLevel0 *gram = nullptr;
+    bool gram_on = true, gram_planned = false, gram_ok = false;
+    // partition-parallel scoring of the last partitioned tests of a wave (FPGM_WIDE=0 turns it off)
+    bool wide_on = true;
+    int wide_small_n2 = -1;    // tier-2 tests per wave at most for tests under 65,536 samples (-1: one per slot)
+    int wide_min_log = 1;      // least partitions (log2) of a published test
+    int wide_part_min = 1024;  // samples per partition at least when splitting for parallelism
+    bool wide_direct = true;   // hand a small wave's tier-2 tests over before the compact kernel hashes them
     // result
     bool has_result = false;
     std::vector<uint8_t> res_adj;
@@ -411,6 +421,34 @@ __global__ void degree_kernel(const uint32_t *bits, int n, int W, unsigned long 
 
 inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
+// Level 0 from the tensor-core Gram matrix (gram.cu): one warp per pair x < y (at level 0
+// item e is edge e, one test each).  The pair's dx x dy block of G -- rows of x's states,
+// columns of y's -- goes into the warp's shared slice, then the same scoring and decision
+// as the counting tiers (score_dense, CellTable.cpp:430-455 / IndependenceTest.cpp:295-364).
+__global__ void __launch_bounds__(kThreads, 2) level0_gram_score_kernel(WaveArgs a, const int32_t *G, int ld,
+                                                                        const int32_t *row_off, int n_items) {
+    extern __shared__ int smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int *tab = smem + warp * kWarpInts;
+    const WarpGroup g{lane};
+    for (int item = blockIdx.x * kWarps + warp; item < n_items; item += gridDim.x * kWarps) {
+        const int x = a.ex[item], y = a.ey[item];
+        const int dx = a.card[x], dy = a.card[y];
+        const int cells = dx * dy;
+        int *ni = tab + cells, *nj = ni + dx, *nk = nj + dy;
+        const int32_t *src = G + (int64_t)row_off[x] * ld + row_off[y];
+        for (int c = lane; c < cells; c += 32) {
+            const int i = c / dy, j = c - i * dy;
+            tab[c] = src[(int64_t)i * ld + j];
+        }
+        __syncwarp();
+        const Verdict v = score_dense(g, tab, ni, nj, nk, dx, dy, 1, a.alpha, a.bt, a.detail != nullptr,
+                                      a.want_hash != 0, nullptr);
+        if (lane == 0) record(a, item, v, cells, a.want_hash ? table_hash(tab, cells) : 0, 0);
+        __syncwarp();
+    }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ engine setup
@@ -436,6 +474,8 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     CK(cudaFuncSetAttribute(ci_compact_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     CK(cudaFuncSetAttribute(ci_compact_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     CK(cudaFuncSetAttribute(ci_part_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    CK(cudaFuncSetAttribute(ci_part_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    CK(cudaFuncSetAttribute(level0_gram_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     CK(cudaFuncSetAttribute(ci_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     int occ = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ci_warp_kernel, kThreads, kSmemBytes));
@@ -457,6 +497,13 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     RET(e->stats.ensure(ST_COUNT * 8));
     e->wave_log = getenv("FPGM_WAVE_LOG") != nullptr;
     if (const char *pm = getenv("FPGM_PART_MAX_LOG")) e->part_max_log = std::min(kPartMaxLog, std::max(1, atoi(pm)));
+    if (const char *w = getenv("FPGM_WIDE")) e->wide_on = atoi(w) != 0;
+    if (const char *w = getenv("FPGM_GRAM")) e->gram_on = atoi(w) != 0;
+    e->gram = gram_create();
+    if (const char *w = getenv("FPGM_WIDE_N2")) e->wide_small_n2 = atoi(w);
+    if (const char *w = getenv("FPGM_WIDE_MIN_LOG")) e->wide_min_log = std::min(kPartMaxLog, std::max(0, atoi(w)));
+    if (const char *w = getenv("FPGM_WIDE_PART_MIN")) e->wide_part_min = std::max(64, atoi(w));
+    if (const char *w = getenv("FPGM_WIDE_DIRECT")) e->wide_direct = atoi(w) != 0;
     if (getenv("FPGM_PHASE_TIMERS")) {
         RET(e->phase_timers.ensure(32 * 8));
         CK(cudaMemset(e->phase_timers.p, 0, 32 * 8));
@@ -474,8 +521,9 @@ extern "C" int fpgm_engine_destroy(fpgm_engine *e) {
                       &e->log_vars, &e->log_meta, &e->node_cnt, &e->node_off, &e->slots, &e->plain_ws,
                       &e->tests_buf, &e->detail_buf, &e->item_vars, &e->lists, &e->band,
                       &e->phase_timers, &e->var_off, &e->var_S, &e->var_lo, &e->var_hi, &e->mle_counts,
-                      &e->mle_pot, &e->mle_meta};
+                      &e->mle_pot, &e->mle_meta, &e->wide, &e->wide_items};
     for (DevBuf *b : bufs) b->release();
+    gram_destroy(e->gram);
     if (e->ev0) cudaEventDestroy(e->ev0);
     if (e->ev1) cudaEventDestroy(e->ev1);
     if (e->ev2) cudaEventDestroy(e->ev2);
@@ -505,6 +553,7 @@ int load_datasets(fpgm_engine *e, int32_t n_jobs, const int32_t *job_vars, const
     CK(cudaSetDevice(e->device));
     e->n = 0;
     e->has_result = false;
+    e->gram_planned = false;  // the one-hot layout follows the dataset
     e->n_jobs = n_jobs;
     e->S = smax;
     e->S_pad = (smax + 63) & ~(int64_t)63;
@@ -630,6 +679,8 @@ int ensure_slots(fpgm_engine *e) {
     e->slot_bytes = slot_layout(e->slot_S, cap).total;
     RET(e->slots.ensure((size_t)e->slot_bytes * e->n_slots));
     CK(cudaMemsetAsync(e->slots.p, 0, (size_t)e->slot_bytes * e->n_slots, e->stream));  // zeroed tables
+    RET(e->wide.ensure((size_t)e->n_slots * sizeof(WideTest)));
+    RET(e->wide_items.ensure((size_t)e->n_slots * kPartMax * 4));
     return FPGM_OK;
 }
 
@@ -661,6 +712,14 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t ite
         a.slot_bytes = e->slot_bytes;
         a.slot_S = e->slot_S;
         a.hash_cap_global = e->hash_cap_global;
+        if (e->wide_on) {
+            a.wide = e->wide.as<WideTest>();
+            a.wide_items = e->wide_items.as<int32_t>();
+            a.wide_small_n2 = e->wide_small_n2 >= 0 ? e->wide_small_n2 : e->n_slots;
+            a.wide_min_log = e->wide_min_log;
+            a.wide_part_min = e->wide_part_min;
+            a.wide_direct = e->wide_direct;
+        }
     }
     a.part_max_log = e->part_max_log;
     return FPGM_OK;
@@ -672,8 +731,13 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t ite
 int launch_compact(fpgm_engine *e, const WaveArgs &a, int grid) {
     ci_compact_kernel<false><<<grid, kThreads, kSmemBytes, e->stream>>>(a);
     ci_part_kernel<<<grid, kThreads, kSmemBytes, e->stream>>>(a);
+    int n = 3;
+    if (a.wide) {
+        ci_part_wide_kernel<<<grid, kThreads, kSmemBytes, e->stream>>>(a);
+        ++n;
+    }
     ci_compact_kernel<true><<<grid, kThreads, kSmemBytes, e->stream>>>(a);
-    return 3;
+    return n;
 }
 
 // Classify + the three tiers on the current stream.  Returns launches issued.
@@ -688,7 +752,7 @@ int launch_tiers(fpgm_engine *e, const WaveArgs &a) {
 }
 
 int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, fpgm_pc_stats *st, int level_idx,
-                        const WaveArgs &proto) {
+                        const WaveArgs &proto, bool gram = false) {
     unsigned long long *dstat = e->stats.as<unsigned long long>();
     int wave = 0;
     int64_t unresolved = n_active;
@@ -726,14 +790,23 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
         a.off = e->off.as<int32_t>();
         a.n_edges = (int32_t)n_active;
         CK(cudaEventRecord(e->ev0, e->stream));
-        classify_kernel<SRC_WAVE><<<e->ci_blocks, kThreads, 0, e->stream>>>(a);
-        ci_warp_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
-        ci_cta_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
-        CK(cudaGetLastError());
+        if (gram) {  // level 0: every pair's table from the tensor-core Gram matrix (one wave, one test per edge)
+            int nl = 0;
+            RET(gram_run(e->gram, e->stream, dstat + ST_TIMEOUT, &nl));
+            level0_gram_score_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(
+                a, gram_counts(e->gram), gram_ld(e->gram), gram_row_off(e->gram), (int)n_active);
+            CK(cudaGetLastError());
+            st->kernel_launches += nl + 3;  // plan, one-hot + GEMM, scoring, reduce
+        } else {
+            classify_kernel<SRC_WAVE><<<e->ci_blocks, kThreads, 0, e->stream>>>(a);
+            ci_warp_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+            ci_cta_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+            CK(cudaGetLastError());
+            st->kernel_launches += 5;  // plan, classify, warp tier, CTA tier, reduce
+        }
         CK(cudaEventRecord(e->ev1, e->stream));
-        st->kernel_launches += 5;  // plan, classify, warp tier, CTA tier, reduce
         a.dbg = e->phase_timers.as<unsigned long long>();
-        if (a.slot_mem) {
+        if (a.slot_mem && !gram) {
             st->kernel_launches += launch_compact(e, a, e->n_slots);
             CK(cudaGetLastError());
         }
@@ -743,6 +816,7 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
 
             CK(cudaMemsetAsync(a.dbg, 0, sizeof h, e->stream));
             CK(cudaStreamSynchronize(e->stream));
+            if (h[23]) fprintf(stderr, "partition-parallel d=%d tests=%llu\n", d, h[23]);
             if (h[13])
                 fprintf(stderr,
                         "partitioned d=%d tests=%llu strata/test=%.0f partitions/test=%.1f us/test: records=%.1f "
@@ -774,17 +848,25 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
         float ms = 0.f, ms2 = 0.f;
         CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
         CK(cudaEventElapsedTime(&ms2, e->ev1, e->ev2));
-        st->count_ms += ms;
+        if (gram) {
+            st->gram_ms += ms;
+            st->gram_flops += gram_flops(e->gram);
+            st->gram_tests += n_active;
+        } else {
+            st->count_ms += ms;
+        }
         st->large_ms += ms2;
         // algorithmic bytes: (2 + d) columns of the test's samples per test, split by kernel
         st->count_bytes += (double)hs[ST_BYTES_SHARED];
         st->large_bytes += (double)hs[ST_BYTES_LARGE];
-        st->count_launches += 1;
+        if (!gram) st->count_launches += 1;
+        if (hs[ST_TIMEOUT])
+            return set_error(FPGM_ERR_TIMEOUT, "level %d: a bounded wait of the tensor-core level-0 kernel gave up", d);
         if (e->wave_log)
             fprintf(stderr,
-                    "wave level=%d tests=%d tier0=%d tier1=%d tier2=%d (partitioned=%d retried=%d) "
+                    "wave level=%d tests=%d tier0=%d tier1=%d tier2=%d (partitioned=%d parallel=%d retried=%d) "
                     "compact_launched=%d count_ms=%.4f compact_ms=%.4f count_bytes=%.0f compact_bytes=%.0f\n",
-                    d, T, tiers[C_TIER0], tiers[C_TIER1], tiers[C_TIER2], tiers[C_PART], tiers[C_RETRY],
+                    d, T, tiers[C_TIER0], tiers[C_TIER1], tiers[C_TIER2], tiers[C_PART], tiers[C_WIDET], tiers[C_RETRY],
                     a.slot_mem != nullptr, ms, ms2, (double)hs[ST_BYTES_SHARED], (double)hs[ST_BYTES_LARGE]);
         if (hs[ST_UNSUPPORTED])
             return set_error(FPGM_ERR_UNSUPPORTED,
@@ -896,7 +978,16 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
             a.pyx = e->pyx.as<int32_t>();
             a.cntx = e->cntx.as<uint64_t>();
             a.next = e->next.as<uint64_t>();
-            RET(run_waves_and_count(e, alpha, d, n_active, st, st->n_levels, a));
+            bool gram = false;
+            if (d == 0 && e->n_jobs == 1 && e->gram_on) {
+                if (!e->gram_planned) {
+                    RET(gram_plan(e->gram, n, e->h_card.data(), e->S, e->cols.as<uint8_t>(), e->var_off.as<int64_t>(),
+                                  e->card.as<uint8_t>(), e->num_sms, e->stream, &e->gram_ok));
+                    e->gram_planned = true;
+                }
+                gram = e->gram_ok;
+            }
+            RET(run_waves_and_count(e, alpha, d, n_active, st, st->n_levels, a, gram));
         }
         // finalize: removals into the bitset and the removal log
         RET(e->log_vars.ensure((size_t)(var_count + std::max<int64_t>(n_active, 1) * std::max(d, 1)) * 4 + 16, true,
@@ -1026,6 +1117,7 @@ int plain_test(fpgm_engine *e, int x, int y, const int *z, int d, double alpha, 
         a.slot_bytes = e->slot_bytes;
         a.slot_S = e->slot_S;
         a.hash_cap_global = e->hash_cap_global;
+        a.wide = nullptr;  // the single test stays on its one CTA
         a.detail = e->detail_buf.as<fpgm_ci_result>();
         a.want_hash = want_hash;
         uint16_t iv[kMaxCols];
@@ -1490,6 +1582,9 @@ extern "C" int fpgm_ci_test_noalloc(const uint8_t *columns, int64_t pitch, int32
                                     int32_t x, int32_t y, const int32_t *z, int32_t nz, double alpha,
                                     int32_t want_hash, fpgm_ci_result *result, void *stream) {
     if (!columns || !result || (nz > 0 && !z)) return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_noalloc: NULL argument");
+    if (reinterpret_cast<uintptr_t>(result) % alignof(fpgm_ci_result) != 0)
+        return set_error(FPGM_ERR_INVALID, "fpgm_ci_test_noalloc: result must be %zu-byte aligned",
+                         alignof(fpgm_ci_result));
     if (!(alpha >= 0.0 && alpha <= 1.0))
         return set_error(FPGM_ERR_INVALID, "Error with incorrect significance level alpha!");
     if (n_vars < 2 || n_vars > kNoAllocMaxVars || n_samples < 1 || n_samples > ((int64_t)1 << 31) - 16)

@@ -69,7 +69,7 @@ typedef struct {
     double p_value;        /* 1 - P(df/2, G^2/2) */
     int32_t rechecked;     /* 1 when G^2 was computed with FP64 terms (recheck band or compact path) */
     int32_t path;          /* 0 warp tier, 1 CTA tier or plain kernel, 2 compact strata,
-                              3 partitioned strata */
+                              3 partitioned strata, 4 partitioned strata scored by several CTAs */
 } fpgm_ci_result;
 
 typedef struct {
@@ -91,6 +91,10 @@ typedef struct {
     double span_ms;              /* CUDA-event span of the whole call on the engine's stream */
     double total_ms;             /* host wall time of the whole skeleton call */
     double large_bytes;          /* algorithmic bytes of the global-memory kernel's tests */
+    double gram_ms;              /* device time of level 0 on the tensor cores (one-hot build, Gram GEMM,
+                                    pair scoring; 0 when level 0 ran on the counting kernels) */
+    double gram_flops;           /* tensor-core flops of that Gram GEMM */
+    int64_t gram_tests;          /* level-0 tests decided from the Gram matrix */
 } fpgm_pc_stats;
 
 typedef struct {
@@ -179,14 +183,15 @@ int fpgm_ci_test_batch(fpgm_engine *eng, const int32_t *tests, int32_t n_tests, 
  *   columns  device pointer; variable v at columns + v*pitch, ids already dense
  *            (0 .. states-1, e.g. first-appearance relabelled as fpgm_dataset_upload does);
  *            16-byte aligned, pitch a multiple of 16 and >= n_samples
- *   result   device pointer to one fpgm_ci_result (written when the stream reaches it)
+ *   result   device pointer to one fpgm_ci_result, 8-byte aligned (written when the stream reaches it)
  *   stream   cudaStream_t to run on (NULL: the legacy default stream); the call waits on
  *            it once, to read the tested columns' state counts for the size check
  * Limits: joint table plus marginals of at most 2^20 ints (else FPGM_ERR_UNSUPPORTED),
  * at most 65,536 variables and 255 states per variable.
  * The first call on a device resolves the scratch array's device address
  * (cudaGetSymbolAddress) with that device current: make that first call before any
- * stream capture.  All calls share the one scratch array, which keeps the previous
+ * stream capture.  The address is kept for the life of the process, so the entry point
+ * must not be used on a device after cudaDeviceReset of that device.  All calls share the one scratch array, which keeps the previous
  * call's contents (each call clears what it uses): calls that overlap on the GPU, from
  * other streams or threads, race and must be serialised by the caller. */
 int fpgm_ci_test_noalloc(const uint8_t *columns, int64_t pitch, int32_t n_vars, int64_t n_samples, int32_t x,

@@ -14,8 +14,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+DATAGEN_PATH = os.path.join(HERE, "_build", "libdatagen.so")
 REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
-REFERENCE_TREE = "/root/reference"
+# The FastPGM source tree the reference-built driver compiles from (only where it exists).
+REFERENCE_TREE = os.environ.get("FASTPGM_REFERENCE", "/root/reference")
 
 
 class CIResult(ctypes.Structure):
@@ -62,6 +64,41 @@ def lib():
         L.oracle_mle_cpts.restype = ctypes.c_int
         _lib = L
     return _lib
+
+
+_gen = None
+
+
+class GenSpec(ctypes.Structure):
+    """fpgm_gen_spec of the engine's C header (same field order and types)."""
+    _fields_ = [("n_nodes", ctypes.c_int32), ("n_edges", ctypes.c_int32), ("avg_indegree", ctypes.c_double),
+                ("max_indegree", ctypes.c_int32), ("card_min", ctypes.c_int32), ("card_max", ctypes.c_int32),
+                ("tail_frac", ctypes.c_double), ("tail_min", ctypes.c_int32), ("tail_max", ctypes.c_int32),
+                ("dirichlet_alpha", ctypes.c_double), ("n_samples", ctypes.c_int64), ("seed", ctypes.c_uint64)]
+
+
+def generate(n_nodes, n_samples, seed, n_edges=0, avg_indegree=2.0, max_indegree=4, card=(2, 4),
+             tail=(0.0, 2, 2), dirichlet=1.0):
+    """The seeded network sampler built on its own (_build/libdatagen.so), for the CPU arms:
+    same arguments and bytes as fastpgm_gb300.generate, without loading the engine library.
+    Returns (columns uint8 [n, S] raw ids, card, parents)."""
+    global _gen
+    if _gen is None:
+        if not os.path.exists(DATAGEN_PATH):
+            build()
+        _gen = ctypes.CDLL(DATAGEN_PATH)
+        _gen.fpgm_generate_network.argtypes = [ctypes.POINTER(GenSpec), ctypes.POINTER(ctypes.c_uint8),
+                                               ctypes.POINTER(ctypes.c_uint8), ctypes.POINTER(ctypes.c_int32)]
+        _gen.fpgm_generate_network.restype = ctypes.c_int
+    spec = GenSpec(n_nodes, n_edges, avg_indegree, max_indegree, card[0], card[1], tail[0], tail[1], tail[2],
+                   dirichlet, n_samples, seed)
+    cols = np.empty((n_nodes, n_samples), dtype=np.uint8)
+    c = np.empty(n_nodes, dtype=np.uint8)
+    par = np.full((n_nodes, max(1, max_indegree)), -1, dtype=np.int32)
+    rc = _gen.fpgm_generate_network(ctypes.byref(spec), _u8(cols), _u8(c), _i32(par))
+    if rc != 0:
+        raise RuntimeError("fpgm_generate_network failed: %d" % rc)
+    return cols, c, par
 
 
 def _u8(a):
@@ -119,6 +156,23 @@ def pc_skeleton(cols, card, alpha=0.05, depth=1000, threads=8, max_z=32):
              "edges_after": [int(st.edges_after[i]) for i in range(st.n_levels)],
              "seconds": [float(st.seconds[i]) for i in range(st.n_levels)]}
     return {"adj": adj, "sepsets": seps, "stats": stats}
+
+
+def sha256(a):
+    """sha256 hex digest of an array's bytes (C order)."""
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def skeleton_digest(adj, sepsets):
+    """Compact, order-free fingerprint of a skeleton result: sha256 of the upper triangle
+    of the 0/1 adjacency (row-major) and of the sorted separating-set lines "a b:z1 z2 ..."."""
+    import hashlib
+    adj = np.asarray(adj, dtype=np.uint8)
+    iu = np.triu_indices(adj.shape[0], 1)
+    lines = "".join("%d %d:%s\n" % (a, b, " ".join(map(str, z))) for (a, b), z in sorted(sepsets.items()))
+    return {"adj_sha256": sha256((adj[iu] != 0).astype(np.uint8)),
+            "sep_sha256": hashlib.sha256(lines.encode()).hexdigest(), "n_removed": len(sepsets)}
 
 
 def read_csv_columns(path):

@@ -1,0 +1,74 @@
+"""Full-size skeleton fixtures for the c3, c4 and c5 workloads, from the CPU oracle.
+
+The reference's own code cannot run these sizes here: its dense per-test tables
+(Counts3D, dz*dx*dy cells) at c4's deep levels need more memory than any host has, and
+single-threaded (the only race-free setting for its separating sets) c3 or c5 would take
+hours.  The fixtures therefore come from the plain-C restatement (oracle/pc_oracle.c),
+which the other fixtures pin to the reference on alarm, c1 and c2 (sepsets, CPDAGs,
+per-level test counts, 800 per-test vectors).
+
+Writes tests/golden/full_<cfg>.json with, per dataset (c5: per job):
+  sha256        of the raw generated columns (the sampler's bytes must match on the test host)
+  tests         deterministic CI tests per level (sequential group-size-1 count)
+  edges_after   skeleton edges left after each level
+  adj_sha256    of the upper triangle of the 0/1 adjacency, row-major
+  sep_sha256    of the sorted separating-set lines "a b:z1 z2 ...\\n" (a < b)
+  n_removed     removed edges (one separating set each)
+and, for c5, the level totals over all jobs (what a multi-dataset skeleton reports).
+
+Run:  python tests/golden/make_full.py [c3] [c4] [c5]   (default: all three; c5 takes longest)
+"""
+import json
+import os
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from fastpgm_gb300 import configs as C  # noqa: E402  (pure Python: parameters only)
+from oracle import oracle as O  # noqa: E402
+
+
+def dataset_digest(raw, depth, threads):
+    cols, card = O.relabel(raw)
+    t0 = time.perf_counter()
+    r = O.pc_skeleton(cols, card, depth=depth, threads=threads)
+    dt = time.perf_counter() - t0
+    d = O.skeleton_digest(r["adj"], r["sepsets"])
+    d.update({"sha256": O.sha256(raw), "shape": list(raw.shape), "tests": r["stats"]["tests"],
+              "edges_after": r["stats"]["edges_after"]})
+    return d, dt
+
+
+def main():
+    names = [a for a in sys.argv[1:] if a in ("c3", "c4", "c5")] or ["c3", "c4", "c5"]
+    threads = os.cpu_count() or 1
+    O.build()
+    for name in names:
+        t0 = time.perf_counter()
+        if name == "c5":
+            data, depth = C.make_jobs(C.c5_jobs(), generate=O.generate)
+            jobs = []
+            for j, raw in enumerate(data):
+                d, dt = dataset_digest(raw, depth, threads)
+                jobs.append(d)
+                print("c5 job %d: %d x %d, %d tests, %.1f s" % (j, raw.shape[0], raw.shape[1], sum(d["tests"]), dt),
+                      flush=True)
+            L = max(len(d["tests"]) for d in jobs)
+            out = {"config": name, "depth": depth, "jobs": jobs,
+                   "level_tests": [sum(d["tests"][i] for d in jobs if i < len(d["tests"])) for i in range(L)]}
+        else:
+            raw, depth, spec = C.make_config(name, generate=O.generate)
+            d, dt = dataset_digest(raw, depth, threads)
+            out = {"config": name, "depth": depth, "spec": spec, "jobs": [d]}
+        out["oracle_seconds"] = round(time.perf_counter() - t0, 1)
+        out["oracle_threads"] = threads
+        with open(os.path.join(HERE, "full_%s.json" % name), "w") as f:
+            json.dump(out, f, indent=1, sort_keys=True)
+        print("%s: %.1f s" % (name, out["oracle_seconds"]), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,6 +1,6 @@
 """Regenerates the committed golden fixtures from the reference's own PC-stable code.
 
-Needs the reference tree (FastPGM) at /root/reference and the reference-built
+Needs the reference tree (FastPGM; $FASTPGM_REFERENCE, default /root/reference) and the reference-built
 driver (oracle/Makefile `ref` target).  Writes, under tests/golden/:
 
   alarm_s5000.npz        the reference's shipped alarm_s5000 dataset, as the reference
@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 import fastpgm_gb300 as F  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-REF = "/root/reference"
+REF = O.REFERENCE_TREE
 
 
 def sample_tests(n, card, rng, count, dmax):

@@ -88,3 +88,43 @@ def test_counting_phase_fraction_sums_both_kernel_groups():
     r = bench.counting_phase([(1000.0, 4e9), (4000.0, 1e9)], 10.0)
     assert abs(r["achieved"] - 1.0) < 1e-12 and abs(r["frac"] - 0.1) < 1e-12 and r["kernel_ms"] == 5000.0
     assert bench.counting_phase([], 10.0) is None
+
+
+_REF_ARM = r"""
+import argparse, sys
+sys.path.insert(0, sys.argv[1])
+import bench
+a = argparse.Namespace(gpus=1, steps=1, warmup=0, impl="reference", config="c1", alpha=0.05)
+bench.run_reference(a, bench.Dist())
+maps = open("/proc/self/maps").read()
+print("ENGINE_LOADED" if "libfastpgm_gb300" in maps else "ENGINE_NOT_LOADED")
+print("ORACLE_LOADED" if "liboracle" in maps else "ORACLE_NOT_LOADED")
+"""
+
+
+def test_reference_arm_never_loads_the_engine_library():
+    """The reference arm times the reference algorithm's CPU port and generates its inputs
+    with the oracle's copy of the seeded sampler: the engine's own library stays unloaded, and
+    its config object is the one the GPU arm prints."""
+    r = subprocess.run([sys.executable, "-c", _REF_ARM, ROOT], capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "ENGINE_NOT_LOADED" in r.stdout and "ORACLE_LOADED" in r.stdout, r.stdout
+    line = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][0])
+    sys.path.insert(0, ROOT)
+    import argparse
+    import bench
+    a = argparse.Namespace(gpus=1, config="c1", alpha=0.05)
+    assert line["config"] == bench.bench_config(a, 1000)
+
+
+def test_oracle_sampler_is_the_engine_sampler():
+    """The oracle's separately built sampler gives the engine's bytes (both compile the same
+    source with the same floating-point flags)."""
+    import numpy as np
+    import fastpgm_gb300 as F
+    from oracle import oracle as O
+    kw = dict(n_nodes=40, n_samples=3000, seed=9, avg_indegree=1.5, max_indegree=3, card=(2, 9), tail=(0.2, 10, 21),
+              dirichlet=0.3)
+    a, ca, pa = F.generate(**kw)
+    b, cb, pb = O.generate(**kw)
+    assert np.array_equal(a, b) and np.array_equal(ca, cb) and np.array_equal(pa, pb)

@@ -213,10 +213,10 @@ def test_compact_tier_at_c4_scale(eng, c4_data, d):
     rng = np.random.default_rng(11 + d)
     tests = random_tests(rng, n, d, 300)
     got = eng.ci_test_batch(tests, d, want_hash=True)
-    idx = [i for i, g in enumerate(got) if g.path == 2][:6] + [i for i, g in enumerate(got) if g.path == 3][:6]
+    idx = [i for i, g in enumerate(got) if g.path == 2][:6] + [i for i, g in enumerate(got) if g.path in (3, 4)][:6]
     assert len(idx) >= 6
     if d >= 6:
-        assert sum(g.path == 3 for g in got) >= 6, "partitioned kernel not used"
+        assert sum(g.path in (3, 4) for g in got) >= 6, "partitioned kernels not used"
     exp = O.ci_tests(cols, cd, tests[idx], d, threads=8)
     for i, o in zip(idx, exp):
         check(got[i], o, exact_p=got[i].rechecked == 1)
@@ -238,15 +238,18 @@ def test_partitioned_strata_with_64_bit_codes(eng):
     got = eng.ci_test_batch(tests, 8, want_hash=True)
     exp = O.ci_tests(cols, card, tests, 8, threads=3)
     for g, o in zip(got, exp):
-        assert g.path == 3
+        assert g.path in (3, 4)
         check(g, o, exact_p=g.rechecked == 1)  # FP32 G^2 on 70,000 samples: p within 1e-3 unless rechecked
 
 
-def test_partition_overflow_falls_back_to_global_hash(monkeypatch):
+@pytest.mark.parametrize("wide", ["0", "1"])
+def test_partition_overflow_falls_back_to_global_hash(monkeypatch, wide):
     """With at most 2 partitions (FPGM_PART_MAX_LOG=1) a test with ~60,000 strata overflows
     every partition table, and the compact kernel's global hash takes it (retry list): same
-    counts and decisions."""
+    counts and decisions -- from the per-CTA partition kernel (FPGM_WIDE=0) and from the
+    partition-parallel one, whose overflowing partition is found by another CTA."""
     monkeypatch.setenv("FPGM_PART_MAX_LOG", "1")
+    monkeypatch.setenv("FPGM_WIDE", wide)
     e = F.Engine(0)
     try:
         rng = np.random.default_rng(29)
@@ -263,6 +266,67 @@ def test_partition_overflow_falls_back_to_global_hash(monkeypatch):
             check(g, o, exact_p=g.rechecked == 1)
     finally:
         e.close()
+
+
+def _engine_with(monkeypatch, **env):
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    e = F.Engine(0)
+    for k in env:
+        monkeypatch.delenv(k)
+    return e
+
+
+@pytest.mark.parametrize("d", [6, 8])
+def test_partition_parallel_matches_per_cta_and_oracle(monkeypatch, c4_data, d):
+    """The same c4-scale batch through the per-CTA partition kernel (FPGM_WIDE=0: every
+    partition of a test on the CTA that wrote its records, path 3) and through the
+    partition-parallel path (the test's partitions spread over all CTAs and summed by
+    atomics, path 4): identical counts, df and decisions, G^2 within the FP32 tolerance, and
+    both equal to the oracle on a sample."""
+    raw, cols, cd = c4_data
+    rng = np.random.default_rng(101 + d)
+    tests = random_tests(rng, raw.shape[0], d, 120)
+    res = {}
+    for wide in ("0", "1"):
+        e = _engine_with(monkeypatch, FPGM_WIDE=wide)
+        try:
+            e.upload(raw)
+            res[wide] = e.ci_test_batch(tests, d, want_hash=True)
+        finally:
+            e.close()
+    per_cta, par = res["0"], res["1"]
+    assert sum(g.path == 3 for g in per_cta) >= 6 and sum(g.path == 4 for g in par) >= 6
+    for a, b in zip(per_cta, par):
+        assert a.cell_hash == b.cell_hash and a.df == b.df and a.independent == b.independent
+        assert abs(a.g2 - b.g2) <= max(G2_ATOL, G2_RTOL * abs(a.g2))
+    idx = [i for i, g in enumerate(par) if g.path == 4][:8]
+    exp = O.ci_tests(cols, cd, tests[idx], d, threads=8)
+    for i, o in zip(idx, exp):
+        check(par[i], o, exact_p=par[i].rechecked == 1)
+        check(per_cta[i], o, exact_p=per_cta[i].rechecked == 1)
+
+
+def test_small_dataset_tail_goes_partition_parallel(monkeypatch):
+    """Below 65,536 samples a wave with few tier-2 tests hands those whose strata overflow the
+    shared hash to the partition-parallel path (FPGM_WIDE_N2 = tests per wave at most):
+    50,000 samples, |Z| = 6 over 6-9 states; the same batch with the handover off keeps the
+    global hash (path 2).  Counts, df and decisions equal the oracle either way."""
+    raw, _, _ = F.generate(n_nodes=14, n_samples=50000, seed=61, n_edges=20, max_indegree=4, card=(6, 9))
+    cols, cd = O.relabel(raw)
+    rng = np.random.default_rng(62)
+    tests = random_tests(rng, 14, 6, 12)
+    exp = O.ci_tests(cols, cd, tests, 6, threads=8)
+    for n2, paths in (("304", (4,)), ("0", (2,))):
+        e = _engine_with(monkeypatch, FPGM_WIDE_N2=n2)
+        try:
+            e.upload(raw)
+            got = e.ci_test_batch(tests, 6, want_hash=True)
+        finally:
+            e.close()
+        assert any(g.path in paths for g in got), [g.path for g in got]
+        for g, o in zip(got, exp):
+            check(g, o, exact_p=g.rechecked == 1)
 
 
 @pytest.mark.parametrize("case", tiny_table_cases(), ids=lambda c: c[0])

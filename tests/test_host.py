@@ -194,7 +194,7 @@ def test_shd_matches_reference_comparison(tmp_path):
     """BNSL_PCStable's SHD report: the learned CPDAG against the reference network, equal to
     the reference's own CustomNetwork::LoadBIFFile + BNSLComparison::GetSHD -- on alarm
     (its shipped alarm.bif) and on c1 (its generating DAG written as BIF)."""
-    ref_root = "/root/reference/dataset/alarm/"
+    ref_root = os.path.join(O.REFERENCE_TREE, "dataset", "alarm") + os.sep
     cases = [(ref_root + "alarm_s5000", ref_root + "alarm.bif", None)]
     raw, card, par = F.generate(n_nodes=37, n_samples=5000, seed=1, n_edges=46, max_indegree=4, card=(2, 4))
     c1_csv, c1_bif = str(tmp_path / "c1.csv"), str(tmp_path / "c1.bif")

@@ -104,7 +104,7 @@ def test_relabel_first_appearance():
 
 @pytest.mark.skipif(not O.ref_available(), reason="reference-built driver needs the reference tree")
 def test_reference_driver_reproduces_shipped_golden(tmp_path):
-    O.ref_pc("/root/reference/dataset/alarm/alarm_s5000", str(tmp_path / "a"))
+    O.ref_pc(os.path.join(O.REFERENCE_TREE, "dataset", "alarm", "alarm_s5000"), str(tmp_path / "a"))
     got = open(tmp_path / "a_struct").read()
     assert got == open(os.path.join(GOLDEN, "alarm_s5000_struct")).read()
 
@@ -174,3 +174,22 @@ def test_oracle_known_answers_on_tiny_tables(case):
     r = O.ci_tests(cols, card, np.array([list(range(2 + d))], dtype=np.int32), d, threads=1)[0]
     assert r.df == df and abs(r.g2 - g2) < 1e-12 and abs(r.p_value - p) < 1e-12
     assert r.independent == (p > 0.05)
+
+
+@pytest.mark.parametrize("name", ["c3", "c4", "c5"])
+def test_full_size_fixtures_describe_this_hosts_data(name):
+    """The full-size fixtures (oracle digests at the c3/c4/c5 sizes, checked against the GPU
+    engine in test_gpu_fullsize.py) were made from the bytes the seeded sampler gives here."""
+    from fastpgm_gb300 import configs as C
+    with open(os.path.join(GOLDEN, "full_%s.json" % name)) as f:
+        fx = json.load(f)
+    if name == "c5":
+        data, depth = C.make_jobs(C.c5_jobs(), generate=O.generate)
+    else:
+        raw, depth, _ = C.make_config(name, generate=O.generate)
+        data = [raw]
+    assert depth == fx["depth"] and len(data) == len(fx["jobs"])
+    for raw, job in zip(data, fx["jobs"]):
+        assert O.sha256(raw) == job["sha256"]
+        assert list(raw.shape) == job["shape"]
+        assert len(job["tests"]) == len(job["edges_after"]) >= 1

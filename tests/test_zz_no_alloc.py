@@ -13,6 +13,7 @@ import ctypes
 import numpy as np
 import pytest
 
+from oracle import oracle as O
 import fastpgm_gb300 as F
 
 pytestmark = pytest.mark.gpu
@@ -60,6 +61,66 @@ def test_noalloc_matches_ci_test_on_two_calls():
                 assert abs(got.g2 - exp.g2) <= max(G2_ATOL, G2_RTOL * abs(exp.g2)), (call, t)
                 tol = 1e-10 if exp.rechecked else P_ATOL
                 assert abs(got.p_value - exp.p_value) <= tol, (call, t)
+                _check_oracle(got, cols, t)
+
+
+def _check_oracle(got, cols, t):
+    """The CPU oracle's counts (table hash), df, decision and FP64 G^2 / p for the same test."""
+    card = (cols.max(axis=1).astype(np.int32) + 1).astype(np.uint8)  # dense ids: card = max + 1
+    o = O.ci_tests(cols, card, np.array([t], dtype=np.int32), len(t) - 2, threads=1)[0]
+    assert got.table_hash == o.table_hash and got.cell_hash == o.cell_hash, t
+    assert got.df == o.df and got.independent == o.independent, t
+    assert abs(got.g2 - o.g2) <= max(G2_ATOL, G2_RTOL * abs(o.g2)), t
+    assert abs(got.p_value - o.p_value) <= (1e-10 if got.rechecked else P_ATOL), t
+
+
+def test_noalloc_large_table_on_a_stream():
+    """A joint table of 140,000+ cells (beyond the shared-memory table, so the kernel counts
+    into the library's fixed scratch array with global atomics), issued on a caller's
+    non-default stream: the same result as fpgm_ci_test and the oracle, on two calls in a row."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    lib = F.load()
+    raw, _, _ = F.generate(n_nodes=8, n_samples=30011, seed=31, n_edges=9, max_indegree=2, card=(18, 20))
+    with F.Engine(0) as eng:
+        eng.upload(raw)
+        cols = eng.download()
+        n, S = cols.shape
+        pitch = (S + 63) // 64 * 64
+        dcols = _device_copy(torch, cols, pitch)
+        dres = torch.zeros(ctypes.sizeof(F.CIResult), dtype=torch.uint8, device="cuda:0")
+        stream = torch.cuda.Stream()
+        tests = [(0, 1, 2, 3), (4, 5, 6, 7), (2, 6, 0, 5)]
+        for call in range(2):
+            for t in tests:
+                card = cols.max(axis=1).astype(np.int64) + 1
+                assert np.prod(card[list(t)]) > 24576  # beyond the shared-memory table
+                z = np.array(t[2:], dtype=np.int32)
+                rc = lib.fpgm_ci_test_noalloc(dcols.data_ptr(), pitch, n, S, t[0], t[1],
+                                              z.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), 2, 0.05, 1,
+                                              dres.data_ptr(), ctypes.c_void_p(stream.cuda_stream))
+                assert rc == 0, lib.fpgm_last_error()
+                stream.synchronize()
+                got = F.CIResult.from_buffer_copy(dres.cpu().numpy().tobytes())
+                exp = eng.ci_test(t[0], t[1], list(t[2:]), want_hash=True)
+                assert got.table_hash == exp.table_hash and got.df == exp.df, (call, t)
+                assert got.independent == exp.independent, (call, t)
+                assert abs(got.g2 - exp.g2) <= max(G2_ATOL, G2_RTOL * abs(exp.g2)), (call, t)
+                _check_oracle(got, cols, t)
+
+
+def test_noalloc_rejects_a_misaligned_result():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    lib = F.load()
+    cols = np.zeros((2, 64), dtype=np.uint8)
+    dcols = _device_copy(torch, cols, 64)
+    dres = torch.zeros(ctypes.sizeof(F.CIResult) + 16, dtype=torch.uint8, device="cuda:0")
+    rc = lib.fpgm_ci_test_noalloc(dcols.data_ptr(), 64, 2, 64, 0, 1, None, 0, 0.05, 0, dres.data_ptr() + 4, None)
+    assert rc == F.FPGM_ERR_INVALID
+    assert b"aligned" in lib.fpgm_last_error()
 
 
 def test_noalloc_rejects_tables_beyond_its_scratch():
