@@ -100,7 +100,27 @@ struct WaveArgs {
     int32_t wide_min_log;     // least partitions (log2) of a published test
     int32_t wide_part_min;    // published tests are split no finer than this many samples per partition
     int32_t wide_direct;      // in such a wave, hand every tier-2 test over before any hashing
+    // Tier-2 method for a test whose strata overflow the shared hash: partition kernel or the
+    // global strata hash.  tune (kTuneSB x kTuneDB x kTuneCB bytes, 1 = partitions) when the
+    // autotuner's table is loaded, else part_min_samples decides (samples >= it: partitions).
+    const int8_t *tune;
+    int64_t part_min_samples;
 };
+
+// Autotuner table keys: sample count, |Z| and joint cardinality (cells = dz dx dy) relative
+// to the sample count.
+constexpr int kTuneSB = 6;   // samples: < 12.5k, < 25k, < 50k, < 100k, < 200k, more
+constexpr int kTuneDB = 12;  // |Z| = 1 .. 11, 12 and more
+constexpr int kTuneCB = 6;   // cells / samples: < 4, < 16, < 64, < 256, < 1024, more
+__host__ __device__ inline int tune_index(int64_t S, int d, double cells) {
+    int sb = 0;
+    for (int64_t lim = 12500; sb < kTuneSB - 1 && S >= lim; lim *= 2) ++sb;
+    const int db = d < 1 ? 0 : (d > kTuneDB ? kTuneDB - 1 : d - 1);
+    const double r = cells / (double)(S > 0 ? S : 1);
+    int cb = 0;
+    for (double lim = 4.0; cb < kTuneCB - 1 && r >= lim; lim *= 4.0) ++cb;
+    return (sb * kTuneDB + db) * kTuneCB + cb;
+}
 
 __device__ inline int upper_bound_i32(const int32_t *a, int n, int v) {
     int lo = 0, hi = n;
@@ -1269,7 +1289,9 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             const bool k32 = !global && code32;
             if (attempt == 1) {
                 const double est = (double)zlimit * (double)(nvec > 1 ? nvec : 1) / (double)(seen > 1 ? seen : 1);
-                if (S >= kPartMinSamples || (a.wide != nullptr && n2 <= a.wide_small_n2)) {
+                const bool part =
+                    a.tune ? a.tune[tune_index(S, d, (double)dz * s_dim[d] * s_dim[d + 1])] != 0 : S >= a.part_min_samples;
+                if (part || (a.wide != nullptr && n2 <= a.wide_small_n2)) {
                     if (tid == 0) {
                         const int q = atomicAdd(&a.counters[C_PART], 1);
                         a.lists[3 * a.list_cap + q] = item;

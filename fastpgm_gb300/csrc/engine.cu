@@ -17,6 +17,7 @@
 // launch (whole GPU) per CI test; it is the comparison baseline.
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
+#include <dlfcn.h>
 
 #include <algorithm>
 #include <chrono>
@@ -128,6 +129,9 @@ struct fpgm_engine {
         counters, stats, scan_tmp, log_pair, log_vars, log_meta, node_cnt, node_off;
     DevBuf slots, plain_ws, tests_buf, detail_buf, item_vars, lists, band, phase_timers;
     DevBuf wide, wide_items;  // partition-parallel scoring: one WideTest per slot, kPartMax items each
+    DevBuf wave_ctl;          // device-driven wave loop: q, wave count, per-group device time
+    bool graph_on = true;     // FPGM_GRAPH=0: the host drives every wave (as FPGM_WAVE_LOG does)
+    double graph_build_ms = 0.0;  // host time spent capturing and instantiating level graphs
     DevBuf mle_counts, mle_pot, mle_meta;  // parameter learning: counts, potentials, per-node tables
     double band_alpha = -1.0;
     int n_slots = 0, hash_cap_global = 0;
@@ -143,6 +147,12 @@ struct fpgm_engine {
     int wide_min_log = 1;      // least partitions (log2) of a published test
     int wide_part_min = 1024;  // samples per partition at least when splitting for parallelism
     bool wide_direct = true;   // hand a small wave's tier-2 tests over before the compact kernel hashes them
+    // tier-2 method: the autotuner's table (fastpgm_gb300/tune_table.txt, FPGM_TUNE_TABLE) or a
+    // fixed sample-count cut-over (FPGM_PART_CUTOVER, default 65,536)
+    int64_t part_min_samples = kPartMinSamples;
+    DevBuf tune;
+    bool tune_loaded = false;
+    std::string tune_source;
     // result
     bool has_result = false;
     std::vector<uint8_t> res_adj;
@@ -421,6 +431,74 @@ __global__ void degree_kernel(const uint32_t *bits, int n, int W, unsigned long 
 
 inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
+// ---- device-driven wave loop (one CUDA graph per level: a WHILE conditional node whose body
+// is one wave; the wave's tail kernel decides whether another wave runs)
+struct WaveCtl {
+    long long wave, q, n_waves;
+    unsigned long long t_prev, count_ns, large_ns;
+};
+constexpr long long kMaxWaves = 1 << 20;  // bound on waves per level (each wave resolves >= 1 rank per edge)
+
+// Start of a wave: q = ranks per unresolved edge this wave (the host loop's rule: doubling from
+// 1, raised so the wave fills the GPU, capped by the item buffers), counters cleared.
+__global__ void wave_prep_kernel(WaveCtl *c, unsigned long long *stats, int32_t *counters, long long n_active,
+                                 long long ci_blocks, long long max_items) {
+    if (threadIdx.x < 16) counters[threadIdx.x] = 0;
+    if (threadIdx.x != 0) return;
+    const long long unresolved = (long long)stats[ST_UNRESOLVED];
+    stats[ST_UNRESOLVED] = 0;
+    long long q = 1ll << (c->wave < 12 ? c->wave : 12);
+    const long long target = ci_blocks * 64;
+    if (unresolved > 0 && q * unresolved < target) {
+        const long long r = (target + unresolved - 1) / unresolved;
+        q = r < 4096 ? r : 4096;
+    }
+    const long long qmax = max_items / (n_active > 1 ? n_active : 1);
+    q = q < qmax ? q : qmax;
+    c->q = q > 1 ? q : 1;
+}
+
+__global__ void wave_plan_dev_kernel(int n_edges, const uint8_t *status, const uint64_t *total, const uint64_t *next,
+                                     const WaveCtl *c, int32_t *g) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e > n_edges) return;
+    if (e == n_edges) {
+        g[e] = 0;
+        return;
+    }
+    int v = 0;
+    if (status[e] == kStatusActive) {
+        const uint64_t q = (uint64_t)c->q, rem = total[e] - next[e];
+        v = (int)(rem < q ? rem : q);
+    }
+    g[e] = v;
+}
+
+// Device clock between kernels of a wave: slot -1 marks the start of the counting kernels,
+// 0 adds the shared-memory tiers' span, 1 the tier-2 kernels' span.
+__global__ void wave_stamp_kernel(WaveCtl *c, int slot) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (slot == 0) c->count_ns += t - c->t_prev;
+    if (slot == 1) c->large_ns += t - c->t_prev;
+    c->t_prev = t;
+}
+
+__global__ void wave_tail_kernel(WaveCtl *c, const unsigned long long *stats, cudaGraphConditionalHandle h) {
+    c->wave += 1;
+    c->n_waves += 1;
+    const bool more = stats[ST_UNRESOLVED] > 0 && stats[ST_UNSUPPORTED] == 0 && c->wave < kMaxWaves;
+    cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+__global__ void wave_ctl_init_kernel(WaveCtl *c, unsigned long long *stats, long long n_active) {
+    c->wave = c->q = c->n_waves = 0;
+    c->t_prev = c->count_ns = c->large_ns = 0;
+    stats[ST_UNRESOLVED] = (unsigned long long)n_active;
+    stats[ST_BYTES_SHARED] = 0;
+    stats[ST_BYTES_LARGE] = 0;
+}
+
 // Level 0 from the tensor-core Gram matrix (gram.cu): one warp per pair x < y (at level 0
 // item e is edge e, one test each).  The pair's dx x dy block of G -- rows of x's states,
 // columns of y's -- goes into the warp's shared slice, then the same scoring and decision
@@ -452,6 +530,55 @@ __global__ void __launch_bounds__(kThreads, 2) level0_gram_score_kernel(WaveArgs
 }  // namespace
 
 // ------------------------------------------------------------------ engine setup
+namespace {
+// The autotuner's table (written by fastpgm_gb300/tune.py from timings on the GPU): lines
+// "sb db cb method" after a '#' header; any entry not listed keeps the fixed cut-over.  Looked
+// for at $FPGM_TUNE_TABLE, else next to the library (../tune_table.txt); FPGM_TUNE_TABLE=off
+// or FPGM_PART_CUTOVER set keeps the fixed rule.
+int load_tune_table(fpgm_engine *e) {
+    const char *env = getenv("FPGM_TUNE_TABLE");
+    if ((env && strcmp(env, "off") == 0) || getenv("FPGM_PART_CUTOVER")) return FPGM_OK;
+    std::string path;
+    if (env) {
+        path = env;
+    } else {
+        Dl_info info;
+        if (dladdr(reinterpret_cast<void *>(&load_tune_table), &info) && info.dli_fname) {
+            path = info.dli_fname;
+            const size_t k = path.rfind('/');
+            path = (k == std::string::npos ? std::string(".") : path.substr(0, k)) + "/../tune_table.txt";
+        }
+    }
+    FILE *f = path.empty() ? nullptr : fopen(path.c_str(), "r");
+    if (!f) return FPGM_OK;
+    std::vector<int8_t> t((size_t)kTuneSB * kTuneDB * kTuneCB);
+    for (int sb = 0; sb < kTuneSB; ++sb)
+        for (int db = 0; db < kTuneDB; ++db)
+            for (int cb = 0; cb < kTuneCB; ++cb) {
+                const int64_t S_lo = sb == 0 ? 1 : (int64_t)12500 << (sb - 1);
+                t[((size_t)sb * kTuneDB + db) * kTuneCB + cb] = S_lo >= e->part_min_samples ? 1 : 0;
+            }
+    char line[256];
+    int entries = 0;
+    while (fgets(line, sizeof line, f)) {
+        if (line[0] == '#' || line[0] == '\n') continue;
+        int sb, db, cb, m;
+        if (sscanf(line, "%d %d %d %d", &sb, &db, &cb, &m) == 4 && sb >= 0 && sb < kTuneSB && db >= 0 &&
+            db < kTuneDB && cb >= 0 && cb < kTuneCB && (m == 0 || m == 1)) {
+            t[((size_t)sb * kTuneDB + db) * kTuneCB + cb] = (int8_t)m;
+            ++entries;
+        }
+    }
+    fclose(f);
+    if (!entries) return FPGM_OK;
+    RET(e->tune.ensure(t.size()));
+    CK(cudaMemcpy(e->tune.p, t.data(), t.size(), cudaMemcpyHostToDevice));
+    e->tune_loaded = true;
+    e->tune_source = path;
+    return FPGM_OK;
+}
+}  // namespace
+
 extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     if (!out) return set_error(FPGM_ERR_INVALID, "fpgm_engine_create: out is NULL");
     *out = nullptr;
@@ -499,11 +626,14 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     if (const char *pm = getenv("FPGM_PART_MAX_LOG")) e->part_max_log = std::min(kPartMaxLog, std::max(1, atoi(pm)));
     if (const char *w = getenv("FPGM_WIDE")) e->wide_on = atoi(w) != 0;
     if (const char *w = getenv("FPGM_GRAM")) e->gram_on = atoi(w) != 0;
+    if (const char *w = getenv("FPGM_GRAPH")) e->graph_on = atoi(w) != 0;
     e->gram = gram_create();
     if (const char *w = getenv("FPGM_WIDE_N2")) e->wide_small_n2 = atoi(w);
     if (const char *w = getenv("FPGM_WIDE_MIN_LOG")) e->wide_min_log = std::min(kPartMaxLog, std::max(0, atoi(w)));
     if (const char *w = getenv("FPGM_WIDE_PART_MIN")) e->wide_part_min = std::max(64, atoi(w));
     if (const char *w = getenv("FPGM_WIDE_DIRECT")) e->wide_direct = atoi(w) != 0;
+    if (const char *w = getenv("FPGM_PART_CUTOVER")) e->part_min_samples = std::max<int64_t>(0, atoll(w));
+    RET(load_tune_table(e));
     if (getenv("FPGM_PHASE_TIMERS")) {
         RET(e->phase_timers.ensure(32 * 8));
         CK(cudaMemset(e->phase_timers.p, 0, 32 * 8));
@@ -521,7 +651,7 @@ extern "C" int fpgm_engine_destroy(fpgm_engine *e) {
                       &e->log_vars, &e->log_meta, &e->node_cnt, &e->node_off, &e->slots, &e->plain_ws,
                       &e->tests_buf, &e->detail_buf, &e->item_vars, &e->lists, &e->band,
                       &e->phase_timers, &e->var_off, &e->var_S, &e->var_lo, &e->var_hi, &e->mle_counts,
-                      &e->mle_pot, &e->mle_meta, &e->wide, &e->wide_items};
+                      &e->mle_pot, &e->mle_meta, &e->wide, &e->wide_items, &e->tune, &e->wave_ctl};
     for (DevBuf *b : bufs) b->release();
     gram_destroy(e->gram);
     if (e->ev0) cudaEventDestroy(e->ev0);
@@ -720,6 +850,8 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t ite
             a.wide_part_min = e->wide_part_min;
             a.wide_direct = e->wide_direct;
         }
+        a.tune = e->tune_loaded ? e->tune.as<int8_t>() : nullptr;
+        a.part_min_samples = e->part_min_samples;
     }
     a.part_max_log = e->part_max_log;
     return FPGM_OK;
@@ -751,8 +883,118 @@ int launch_tiers(fpgm_engine *e, const WaveArgs &a) {
     return n;
 }
 
+// One level's waves driven by the device: a CUDA graph whose WHILE conditional node runs the
+// wave body (prep, plan, scan, classify, the counting tiers, reduce) until the tail kernel
+// finds no unresolved edge.  The graph is captured and instantiated once per level (the
+// level's edge count, |Z| and buffers are its parameters) and the host waits once per level.
+int run_waves_graph(fpgm_engine *e, double alpha, int d, int64_t n_active, fpgm_pc_stats *st, int level_idx,
+                    const WaveArgs &proto) {
+    unsigned long long *dstat = e->stats.as<unsigned long long>();
+    const int64_t cap = std::max<int64_t>(n_active, kMaxItems);  // items of one wave at most
+    WaveArgs a = proto;
+    RET(wave_args_base(e, a, alpha, d, cap));
+    a.adjl = proto.adjl;
+    a.adj_stride = proto.adj_stride;
+    a.deg = proto.deg;
+    a.ex = proto.ex;
+    a.ey = proto.ey;
+    a.pxy = proto.pxy;
+    a.pyx = proto.pyx;
+    a.cntx = proto.cntx;
+    a.next = proto.next;
+    a.off = e->off.as<int32_t>();
+    a.n_edges = (int32_t)n_active;
+    a.dbg = nullptr;
+    size_t sb = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, sb, e->g.as<int32_t>(), e->off.as<int32_t>(), (int)(n_active + 1),
+                                  e->stream);
+    RET(e->scan_tmp.ensure(sb + 16));
+    sb = e->scan_tmp.bytes;
+    RET(e->wave_ctl.ensure(sizeof(WaveCtl)));
+    WaveCtl *ctl = e->wave_ctl.as<WaveCtl>();
+    wave_ctl_init_kernel<<<1, 1, 0, e->stream>>>(ctl, dstat, (long long)n_active);
+    CK(cudaGetLastError());
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int per_wave = 0;
+    auto build = [&]() -> int {
+        CK(cudaGraphCreate(&graph, 0));
+        cudaGraphConditionalHandle h;
+        CK(cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault));
+        alignas(cudaGraphNodeParams) unsigned char cp_raw[sizeof(cudaGraphNodeParams)] = {};
+        cudaGraphNodeParams &cp = *reinterpret_cast<cudaGraphNodeParams *>(cp_raw);
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cn;
+        CK(cudaGraphAddNode(&cn, graph, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        CK(cudaStreamBeginCaptureToGraph(e->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+        wave_prep_kernel<<<1, 32, 0, e->stream>>>(ctl, dstat, e->counters.as<int32_t>(), (long long)n_active,
+                                                  (long long)e->ci_blocks, (long long)kMaxItems);
+        wave_plan_dev_kernel<<<blocks_for(n_active + 1, 256), 256, 0, e->stream>>>(
+            (int)n_active, e->status.as<uint8_t>(), e->total.as<uint64_t>(), e->next.as<uint64_t>(), ctl,
+            e->g.as<int32_t>());
+        cub::DeviceScan::ExclusiveSum(e->scan_tmp.p, sb, e->g.as<int32_t>(), e->off.as<int32_t>(),
+                                      (int)(n_active + 1), e->stream);
+        wave_stamp_kernel<<<1, 1, 0, e->stream>>>(ctl, -1);
+        classify_kernel<SRC_WAVE><<<e->ci_blocks, kThreads, 0, e->stream>>>(a);
+        ci_warp_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+        ci_cta_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+        wave_stamp_kernel<<<1, 1, 0, e->stream>>>(ctl, 0);
+        per_wave = 9;  // prep, plan, 3 stamps, classify, warp tier, CTA tier, reduce, tail (+ tier 2)
+        if (a.slot_mem) per_wave += launch_compact(e, a, e->n_slots);
+        wave_stamp_kernel<<<1, 1, 0, e->stream>>>(ctl, 1);
+        wave_reduce_kernel<<<blocks_for(n_active, 256), 256, 0, e->stream>>>(
+            (int)n_active, e->off.as<int32_t>(), e->flag.as<uint8_t>(), e->status.as<uint8_t>(),
+            e->next.as<uint64_t>(), e->total.as<uint64_t>(), e->seprank.as<uint64_t>(), dstat);
+        wave_tail_kernel<<<1, 1, 0, e->stream>>>(ctl, dstat, h);
+        const cudaError_t le = cudaGetLastError();
+        const cudaError_t ce = cudaStreamEndCapture(e->stream, &body);
+        if (le != cudaSuccess) return set_error(FPGM_ERR_CUDA, "level %d graph capture: %s", d, cudaGetErrorString(le));
+        CK(ce);
+        CK(cudaGraphInstantiate(&exec, graph, 0));
+        return FPGM_OK;
+    };
+    int rc = build();
+    e->graph_build_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (rc == FPGM_OK) {
+        const cudaError_t le = cudaGraphLaunch(exec, e->stream);
+        if (le != cudaSuccess) rc = set_error(FPGM_ERR_CUDA, "cudaGraphLaunch: %s", cudaGetErrorString(le));
+    }
+    WaveCtl hc;
+    unsigned long long hs[ST_COUNT];
+    if (rc == FPGM_OK) {
+        cudaError_t ce = cudaMemcpyAsync(&hc, ctl, sizeof hc, cudaMemcpyDeviceToHost, e->stream);
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(hs, dstat, sizeof hs, cudaMemcpyDeviceToHost, e->stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+        if (ce != cudaSuccess) rc = set_error(FPGM_ERR_CUDA, "level %d graph: %s", d, cudaGetErrorString(ce));
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (rc != FPGM_OK) return rc;
+    if (hs[ST_UNSUPPORTED])
+        return set_error(FPGM_ERR_UNSUPPORTED,
+                         "level %d: %llu CI test(s) are outside the engine's limits (joint table beyond 2^62 "
+                         "cells or a node degree >= %d)",
+                         d, hs[ST_UNSUPPORTED], kBinomN);
+    if (hs[ST_UNRESOLVED]) return set_error(FPGM_ERR_STATE, "level %d: wave limit reached with edges unresolved", d);
+    st->waves[level_idx] = (int32_t)hc.n_waves;
+    st->count_ms += hc.count_ns / 1e6;
+    st->large_ms += hc.large_ns / 1e6;
+    st->count_bytes += (double)hs[ST_BYTES_SHARED];
+    st->large_bytes += (double)hs[ST_BYTES_LARGE];
+    st->count_launches += hc.n_waves;
+    st->kernel_launches += 1 + hc.n_waves * per_wave;  // + the control-block init
+    return FPGM_OK;
+}
+
 int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, fpgm_pc_stats *st, int level_idx,
                         const WaveArgs &proto, bool gram = false) {
+    if (d >= 1 && e->graph_on && !e->wave_log && !e->phase_timers.p)
+        return run_waves_graph(e, alpha, d, n_active, st, level_idx, proto);
     unsigned long long *dstat = e->stats.as<unsigned long long>();
     int wave = 0;
     int64_t unresolved = n_active;

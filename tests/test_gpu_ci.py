@@ -29,6 +29,22 @@ def eng():
     e.close()
 
 
+@pytest.fixture(scope="module")
+def eng_per_cta():
+    """An engine without partition-parallel scoring (FPGM_WIDE=0): small batches of tier-2
+    tests stay in the compact kernel (shared or global strata hash) and the per-CTA
+    partition kernel, as in the large waves of a skeleton."""
+    os.environ["FPGM_WIDE"] = "0"
+    os.environ["FPGM_TUNE_TABLE"] = "off"  # the fixed 65,536-sample cut-over decides the method
+    try:
+        e = F.Engine(0)
+    finally:
+        del os.environ["FPGM_WIDE"]
+        del os.environ["FPGM_TUNE_TABLE"]
+    yield e
+    e.close()
+
+
 def check(g, o, exact_p=False):
     assert g.cell_hash == o.cell_hash, "table differs"
     if g.table_hash and o.table_hash:
@@ -118,8 +134,12 @@ def test_many_random_tests_c2_shape(eng):
             check(g, o)
 
 
-def test_compact_strata_tables(eng):
-    """Joint tables beyond the shared-memory budget are counted over observed strata."""
+@pytest.mark.parametrize("mode", ["per_cta", "parallel"])
+def test_compact_strata_tables(eng, eng_per_cta, mode):
+    """Joint tables beyond the shared-memory budget are counted over observed strata: in the
+    compact kernel (path 2), or -- a batch this small is a tail wave -- all handed straight to
+    the partition-parallel path (path 4)."""
+    eng = eng_per_cta if mode == "per_cta" else eng
     raw, _, _ = F.generate(n_nodes=12, n_samples=6000, seed=77, n_edges=14, max_indegree=3, card=(6, 9))
     cols, card = O.relabel(raw)
     eng.upload(raw)
@@ -127,7 +147,7 @@ def test_compact_strata_tables(eng):
     tests = random_tests(rng, 12, 4, 24)   # >= 6^6 = 46,656 cells
     got = eng.ci_test_batch(tests, 4, want_hash=True)
     exp = O.ci_tests(cols, card, tests, 4, threads=8)
-    assert all(g.path == 2 for g in got)
+    assert all(g.path == (2 if mode == "per_cta" else 4) for g in got)
     for g, o in zip(got, exp):
         check(g, o, exact_p=True)
     # the plain path sends the same test through the compact kernel on one CTA
@@ -175,13 +195,16 @@ def test_256_state_column_is_rejected_at_upload(eng):
     assert list(card) == [255, 3, 5]
 
 
+@pytest.mark.parametrize("mode", ["per_cta", "parallel"])
 @pytest.mark.parametrize("card,d", [((2, 5), 5), ((6, 9), 3), ((6, 9), 4), ((6, 9), 5)])
-def test_compact_tier_across_dataset_sizes(eng, card, d):
+def test_compact_tier_across_dataset_sizes(eng, eng_per_cta, card, d, mode):
     """Compact-tier tests after datasets of other sample counts: the per-CTA slots are laid
     out once for the largest dataset seen and reused; their zeroed tables must stay zeroed.
     Cards 2-5 at |Z| = 5 take the dense strata table (at most 32 cells per stratum), cards
     6-9 the counting-sort path, at |Z| = 4 also through the global strata hash and at |Z| = 5
-    (beyond 8,192 strata) on 70,000 samples through the partitioned kernel."""
+    (beyond 8,192 strata) on 70,000 samples through the partitioned kernel -- with FPGM_WIDE=0;
+    by default a batch this small goes to the partition-parallel path."""
+    eng = eng_per_cta if mode == "per_cta" else eng
     for S in (20000, 6000, 70000, 6000):
         raw, _, _ = F.generate(n_nodes=10, n_samples=S, seed=S + d, n_edges=12, max_indegree=3, card=card)
         cols, cd = O.relabel(raw)
@@ -202,12 +225,13 @@ def c4_data():
 
 
 @pytest.mark.parametrize("d", [5, 6, 7, 8])
-def test_compact_tier_at_c4_scale(eng, c4_data, d):
+def test_compact_tier_at_c4_scale(eng_per_cta, c4_data, d):
     """1,041 nodes x 100,000 samples, cardinalities to 21: batches of 300 random tests keep
     every CTA busy with thousands to tens of thousands of strata per test (shared hash,
     global hash, dense table and counting-sort paths); a sample of them is checked bit for
     bit against the oracle."""
     raw, cols, cd = c4_data
+    eng = eng_per_cta
     eng.upload(raw)
     n = raw.shape[0]
     rng = np.random.default_rng(11 + d)
@@ -289,7 +313,7 @@ def test_partition_parallel_matches_per_cta_and_oracle(monkeypatch, c4_data, d):
     tests = random_tests(rng, raw.shape[0], d, 120)
     res = {}
     for wide in ("0", "1"):
-        e = _engine_with(monkeypatch, FPGM_WIDE=wide)
+        e = _engine_with(monkeypatch, FPGM_WIDE=wide, FPGM_TUNE_TABLE="off")
         try:
             e.upload(raw)
             res[wide] = e.ci_test_batch(tests, d, want_hash=True)
@@ -318,7 +342,7 @@ def test_small_dataset_tail_goes_partition_parallel(monkeypatch):
     tests = random_tests(rng, 14, 6, 12)
     exp = O.ci_tests(cols, cd, tests, 6, threads=8)
     for n2, paths in (("304", (4,)), ("0", (2,))):
-        e = _engine_with(monkeypatch, FPGM_WIDE_N2=n2)
+        e = _engine_with(monkeypatch, FPGM_WIDE_N2=n2, FPGM_TUNE_TABLE="off")
         try:
             e.upload(raw)
             got = e.ci_test_batch(tests, 6, want_hash=True)
@@ -344,3 +368,36 @@ def test_known_answers_on_tiny_tables(eng, case):
             assert abs(g.g2 - g2) < 1e-10 and abs(g.p_value - p) < 1e-10
         else:
             assert abs(g.g2 - g2) <= max(G2_ATOL, G2_RTOL * g2) and abs(g.p_value - p) <= P_ATOL
+
+
+def test_autotuner_table_picks_the_tier2_method(monkeypatch, tmp_path):
+    """The autotuner's table (fastpgm_gb300/tune.py writes it) decides, per (samples, |Z|,
+    cells/samples) bucket, whether a test whose strata overflow the shared hash goes to the
+    partition kernel or the global strata hash: a table of all 1s sends 20,000-sample tests
+    to the partition kernel (path 3, below the fixed 65,536 cut-over), one of all 0s keeps
+    them on the global hash (path 2); results equal the oracle either way."""
+    from fastpgm_gb300 import tune
+    raw, _, _ = F.generate(n_nodes=14, n_samples=20000, seed=91, n_edges=20, max_indegree=4, card=(6, 9))
+    cols, cd = O.relabel(raw)
+    rng = np.random.default_rng(92)
+    tests = random_tests(rng, 14, 6, 16)
+    exp = O.ci_tests(cols, cd, tests, 6, threads=8)
+    for method, path in ((1, 3), (0, 2)):
+        table = tmp_path / ("t%d.txt" % method)
+        with open(table, "w") as f:
+            f.write("# test table\n")
+            for sb in range(tune.KTUNE_SB):
+                for db in range(tune.KTUNE_DB):
+                    for cb in range(tune.KTUNE_CB):
+                        f.write("%d %d %d %d\n" % (sb, db, cb, method))
+        e = _engine_with(monkeypatch, FPGM_TUNE_TABLE=str(table), FPGM_WIDE="0")
+        try:
+            e.upload(raw)
+            got = e.ci_test_batch(tests, 6, want_hash=True)
+        finally:
+            e.close()
+        # strata observed = cells / (dx dy); beyond 8,192 the shared hash overflowed
+        over = [g for g, t in zip(got, tests) if g.cells // (int(cd[t[0]]) * int(cd[t[1]])) > 8192]
+        assert len(over) >= 4 and all(g.path == path for g in over), [g.path for g in got]
+        for g, o in zip(got, exp):
+            check(g, o, exact_p=g.rechecked == 1)

@@ -303,3 +303,23 @@ def test_cxx_dag_and_root_options(tmp_path, add_root):
         assert n == n0 + 1 and any(a == n0 for a, _, _ in edges)
     else:
         assert n == n0
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_device_driven_waves_match_host_driven(monkeypatch, name):
+    """Levels >= 1 run as one CUDA graph each (a WHILE conditional node over the wave body,
+    the tail kernel deciding on the device whether another wave runs); FPGM_GRAPH=0 drives
+    every wave from the host.  Same skeleton, separating sets, and per-level test, executed
+    test and wave counts."""
+    raw, depth, _ = F.make_config(name)
+    out = {}
+    for graph in ("1", "0"):
+        monkeypatch.setenv("FPGM_GRAPH", graph)
+        with F.Engine(0) as e:
+            e.upload(raw)
+            st = e.pc_skeleton(depth=depth).to_dict()
+            out[graph] = (st, e.result())
+    (sg, rg), (sh, rh) = out["1"], out["0"]
+    assert np.array_equal(rg["adj"], rh["adj"]) and rg["sepsets"] == rh["sepsets"]
+    for k in ("tests", "tests_executed", "edges_after", "waves"):
+        assert sg[k] == sh[k], k

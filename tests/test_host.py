@@ -265,3 +265,14 @@ def test_parallel_csv_loader_matches_first_appearance_ids(tmp_path):
     assert [int(l) for l in lines[1 + n:1 + 2 * n]] == list(ref_card)
     got = np.frombuffer(lines[-1], dtype=np.uint8).reshape(n, S)
     assert np.array_equal(got, ref_cols)
+
+
+def test_autotuner_bucket_keys():
+    """tune.tune_index mirrors the engine's tune_index (ci_kernels.cuh): sample buckets from
+    12,500 doubling, |Z| 1..12, cells/samples in powers of 4 from 4."""
+    from fastpgm_gb300 import tune
+    assert tune.tune_index(12499, 1, 10) == (0, 0, 0)
+    assert tune.tune_index(12500, 1, 12500 * 4) == (1, 0, 1)
+    assert tune.tune_index(50000, 6, 50000 * 100) == (3, 5, 3)
+    assert tune.tune_index(10 ** 7, 40, 1e30) == (5, 11, 5)
+    assert tune.tune_index(100000, 0, 1) == (4, 0, 0)
