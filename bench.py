@@ -535,6 +535,11 @@ def run_ours(a, d):
         "precision": {"fp64_rechecks": tot["last"]["rechecks"], "near_ties": tot["last"]["near_ties"],
                       "max_abs_dp_fp32_vs_fp64": tot["last"]["max_abs_dp"],
                       "large_tests": tot["last"]["large_tests"]},
+        "autotuner": {"what": "online: per (samples, |Z|, cells/samples) bucket the tier-2 tests are timed with "
+                              "both methods (partition kernel, global strata hash); the faster is preferred",
+                      "buckets_timed_both_ways": tot["last"]["tune_buckets"],
+                      "buckets_preferring_partitions": tot["last"]["tune_partition"],
+                      "tests_timed": tot["last"]["tune_timed"]},
         "cpu_baseline": cpu,
         "gpu_on_cpu_sample": sample_gpu,
         "north_star": ns,

@@ -43,7 +43,8 @@ class PCStats(ctypes.Structure):
                 ("count_ms", ctypes.c_double), ("count_bytes", ctypes.c_double), ("large_ms", ctypes.c_double),
                 ("count_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("span_ms", ctypes.c_double),
                 ("total_ms", ctypes.c_double), ("large_bytes", ctypes.c_double), ("gram_ms", ctypes.c_double),
-                ("gram_flops", ctypes.c_double), ("gram_tests", ctypes.c_int64)]
+                ("gram_flops", ctypes.c_double), ("gram_tests", ctypes.c_int64), ("tune_buckets", ctypes.c_int32),
+                ("tune_partition", ctypes.c_int32), ("tune_timed", ctypes.c_int64)]
 
     def to_dict(self):
         L = self.n_levels
@@ -58,7 +59,9 @@ class PCStats(ctypes.Structure):
                 "count_launches": int(self.count_launches), "kernel_launches": int(self.kernel_launches),
                 "span_ms": float(self.span_ms), "total_ms": float(self.total_ms),
                 "large_bytes": float(self.large_bytes), "gram_ms": float(self.gram_ms),
-                "gram_flops": float(self.gram_flops), "gram_tests": int(self.gram_tests)}
+                "gram_flops": float(self.gram_flops), "gram_tests": int(self.gram_tests),
+                "tune_buckets": int(self.tune_buckets), "tune_partition": int(self.tune_partition),
+                "tune_timed": int(self.tune_timed)}
 
 
 class GenSpec(ctypes.Structure):

@@ -101,9 +101,11 @@ struct WaveArgs {
     int32_t wide_part_min;    // published tests are split no finer than this many samples per partition
     int32_t wide_direct;      // in such a wave, hand every tier-2 test over before any hashing
     // Tier-2 method for a test whose strata overflow the shared hash: partition kernel or the
-    // global strata hash.  tune (kTuneSB x kTuneDB x kTuneCB bytes, 1 = partitions) when the
-    // autotuner's table is loaded, else part_min_samples decides (samples >= it: partitions).
+    // global strata hash.  tune: a fixed table (kTuneSB x kTuneDB x kTuneCB bytes, 1 =
+    // partitions); else tune_obs: the online autotuner's per-bucket timings; else
+    // part_min_samples decides (samples >= it: partitions).
     const int8_t *tune;
+    unsigned long long *tune_obs;  // 8 per bucket: n_part, ns_part, n_hash, ns_hash, decisions
     int64_t part_min_samples;
 };
 
@@ -112,6 +114,9 @@ struct WaveArgs {
 constexpr int kTuneSB = 6;   // samples: < 12.5k, < 25k, < 50k, < 100k, < 200k, more
 constexpr int kTuneDB = 12;  // |Z| = 1 .. 11, 12 and more
 constexpr int kTuneCB = 6;   // cells / samples: < 4, < 16, < 64, < 256, < 1024, more
+constexpr int kTuneBuckets = kTuneSB * kTuneDB * kTuneCB;
+constexpr unsigned long long kTuneExplore = 16;  // tests timed with each method before either is preferred
+constexpr unsigned long long kTuneRefresh = 32;  // then one test in this many takes the other method
 __host__ __device__ inline int tune_index(int64_t S, int d, double cells) {
     int sb = 0;
     for (int64_t lim = 12500; sb < kTuneSB - 1 && S >= lim; lim *= 2) ++sb;
@@ -120,6 +125,32 @@ __host__ __device__ inline int tune_index(int64_t S, int d, double cells) {
     int cb = 0;
     for (double lim = 4.0; cb < kTuneCB - 1 && r >= lim; lim *= 4.0) ++cb;
     return (sb * kTuneDB + db) * kTuneCB + cb;
+}
+
+// Online autotuner (one thread decides for its CTA): per (samples, |Z|, cells/samples)
+// bucket, the device time of tests counted each way is summed as they finish; a bucket
+// first alternates the two methods until each has kTuneExplore timed tests, then takes the
+// faster on average, giving one test in kTuneRefresh to the other so both stay measured.
+// *bucket = the bucket whose hash-path time the caller must add (-1: none).
+__device__ inline bool tier2_pick_partitions(const WaveArgs &a, int64_t S, int d, double cells, int *bucket) {
+    *bucket = -1;
+    if (a.tune) return a.tune[tune_index(S, d, cells)] != 0;
+    if (!a.tune_obs) return S >= a.part_min_samples;
+    const int b = tune_index(S, d, cells);
+    unsigned long long *o = a.tune_obs + 8 * b;
+    const unsigned long long np = *(volatile unsigned long long *)&o[0], nh = *(volatile unsigned long long *)&o[2];
+    const unsigned long long k = atomicAdd(&o[4], 1ull);
+    bool part;
+    if (np < kTuneExplore || nh < kTuneExplore) {
+        part = (k & 1ull) == 0;
+    } else {
+        const double mp = (double)*(volatile unsigned long long *)&o[1] / (double)np;
+        const double mh = (double)*(volatile unsigned long long *)&o[3] / (double)nh;
+        part = mp <= mh;
+        if (k % kTuneRefresh == 0) part = !part;
+    }
+    if (!part) *bucket = b;
+    return part;
 }
 
 __device__ inline int upper_bound_i32(const int32_t *a, int n, int v) {
@@ -1215,7 +1246,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     int *swt = reinterpret_cast<int *>(smem_raw + kZTabOff);
     __shared__ const uint8_t *s_col[kMaxCols];
     __shared__ uint32_t s_dim[kMaxCols];
-    __shared__ int s_idx, s_over, s_distinct, s_flag, s_seen;
+    __shared__ int s_idx, s_over, s_distinct, s_flag, s_seen, s_pick;
     __shared__ int s_w[kWarps];
     __shared__ Partial scratch[kWarps];
     const int tid = threadIdx.x;
@@ -1251,6 +1282,8 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         FPGM_PHASE(-1);
         const int item = a.lists[(kRetry ? 5 : 2) * a.list_cap + idx];
         const int64_t S = a.var_S[a.item_vars[(int64_t)item * ncols + d]];  // <= the slots' layout size
+        int tune_bucket = -1;               // thread 0: the bucket this test's hash-path time goes to
+        unsigned long long t_hash = 0;
         const int64_t nvec = S >> 4;
         if (tid < ncols) {
             const int var = a.item_vars[(int64_t)item * ncols + tid];
@@ -1289,9 +1322,15 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             const bool k32 = !global && code32;
             if (attempt == 1) {
                 const double est = (double)zlimit * (double)(nvec > 1 ? nvec : 1) / (double)(seen > 1 ? seen : 1);
-                const bool part =
-                    a.tune ? a.tune[tune_index(S, d, (double)dz * s_dim[d] * s_dim[d + 1])] != 0 : S >= a.part_min_samples;
-                if (part || (a.wide != nullptr && n2 <= a.wide_small_n2)) {
+                const bool tail = a.wide != nullptr && n2 <= a.wide_small_n2;
+                if (tid == 0) {
+                    int b = -1;
+                    s_pick = tail || tier2_pick_partitions(a, S, d, (double)dz * s_dim[d] * s_dim[d + 1], &b);
+                    tune_bucket = b;
+                    t_hash = gtimer();
+                }
+                __syncthreads();
+                if (s_pick) {
                     if (tid == 0) {
                         const int q = atomicAdd(&a.counters[C_PART], 1);
                         a.lists[3 * a.list_cap + q] = item;
@@ -1522,6 +1561,10 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
                 reinterpret_cast<int4 *>(gtab)[i] = make_int4(0, 0, 0, 0);
             for (int64_t i = (ncell & ~(int64_t)3) + tid; i < ncell; i += kThreads) gtab[i] = 0;
         }
+        if (tid == 0 && tune_bucket >= 0) {
+            atomicAdd(&a.tune_obs[8 * tune_bucket + 2], 1ull);
+            atomicAdd(&a.tune_obs[8 * tune_bucket + 3], gtimer() - t_hash);
+        }
         FPGM_PHASE(6);
         __syncthreads();
     }
@@ -1570,6 +1613,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
         FPGM_PHASE(-1);
         const int item = a.lists[3 * a.list_cap + idx];
         const double est = (double)__int_as_float(a.lists[4 * a.list_cap + idx]);
+        const unsigned long long t_part = (tid == 0 && a.tune_obs) ? gtimer() : 0ull;
         const int64_t S = a.var_S[a.item_vars[(int64_t)item * ncols + d]];
         if (tid < ncols) {
             const int var = a.item_vars[(int64_t)item * ncols + tid];
@@ -1686,6 +1730,11 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
                                                dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over,
                                                &s_nbig, &s_nocc, s_bin, claims, nullptr);
             });
+        }
+        if (tid == 0 && a.tune_obs && !a.tune) {  // the partition path's time for the online autotuner
+            const int b = tune_index(S, d, (double)dz * dx * dy);
+            atomicAdd(&a.tune_obs[8 * b], 1ull);
+            atomicAdd(&a.tune_obs[8 * b + 1], gtimer() - t_part);
         }
         FPGM_PHASE(15);
         __syncthreads();

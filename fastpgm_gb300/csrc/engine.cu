@@ -17,7 +17,6 @@
 // launch (whole GPU) per CI test; it is the comparison baseline.
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
-#include <dlfcn.h>
 
 #include <algorithm>
 #include <chrono>
@@ -55,6 +54,42 @@ int set_error(int code, const char *fmt, ...) {
 
 extern "C" const char *fpgm_last_error(void) { return g_last_error.c_str(); }
 
+namespace {
+std::mutex g_alloc_mu;
+size_t g_alloc_bytes = 0;
+}  // namespace
+
+namespace fpgm {
+int dev_alloc(void **p, size_t bytes) {
+    *p = nullptr;
+    static const size_t cap = [] {
+        const char *c = getenv("FPGM_DEVICE_MEM_CAP");
+        return c ? (size_t)strtoull(c, nullptr, 10) : (size_t)0;
+    }();
+    {
+        std::lock_guard<std::mutex> lk(g_alloc_mu);
+        if (cap && g_alloc_bytes + bytes > cap)
+            return set_error(FPGM_ERR_OOM, "cudaMalloc(%zu) refused: %zu bytes held, cap %zu (FPGM_DEVICE_MEM_CAP)",
+                             bytes, g_alloc_bytes, cap);
+    }
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return set_error(FPGM_ERR_OOM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    std::lock_guard<std::mutex> lk(g_alloc_mu);
+    g_alloc_bytes += bytes;
+    return FPGM_OK;
+}
+
+void dev_free(void *p, size_t bytes) {
+    if (!p) return;
+    cudaFree(p);
+    std::lock_guard<std::mutex> lk(g_alloc_mu);
+    g_alloc_bytes -= std::min(bytes, g_alloc_bytes);
+}
+}  // namespace fpgm
+
 #define CK(call)                                                                                    \
     do {                                                                                            \
         cudaError_t e_ = (call);                                                                    \
@@ -79,25 +114,24 @@ struct DevBuf {
         if (need <= bytes) return FPGM_OK;
         size_t nb = std::max(need, bytes + bytes / 2);
         void *q = nullptr;
-        cudaError_t e = cudaMalloc(&q, nb);
-        if (e != cudaSuccess)
-            return set_error(FPGM_ERR_OOM, "cudaMalloc(%zu) failed: %s", nb, cudaGetErrorString(e));
+        const int rc = dev_alloc(&q, nb);
+        if (rc != FPGM_OK) return rc;
         if (keep && p && bytes) {
-            e = cudaMemcpyAsync(q, p, bytes, cudaMemcpyDeviceToDevice, st);
+            cudaError_t e = cudaMemcpyAsync(q, p, bytes, cudaMemcpyDeviceToDevice, st);
             if (e == cudaSuccess) e = cudaStreamSynchronize(st);
             if (e != cudaSuccess) {
-                cudaFree(q);
+                dev_free(q, nb);
                 return set_error(FPGM_ERR_CUDA, "buffer grow copy failed: %s", cudaGetErrorString(e));
             }
         }
-        if (p) cudaFree(p);
+        if (p) dev_free(p, bytes);
         p = q;
         bytes = nb;
         return FPGM_OK;
     }
     template <class T> T *as() const { return static_cast<T *>(p); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) dev_free(p, bytes);
         p = nullptr;
         bytes = 0;
     }
@@ -141,6 +175,7 @@ struct fpgm_engine {
     // level 0 on the tensor cores (FPGM_GRAM=0 keeps it on the counting kernels)
     GramLevel0 *gram = nullptr;
     bool gram_on = true, gram_planned = false, gram_ok = false;
+    int gram_score_ctas = 2;  // resident CTAs per SM of the level-0 scoring kernel for this dataset
     // partition-parallel scoring of the last partitioned tests of a wave (FPGM_WIDE=0 turns it off)
     bool wide_on = true;
     int wide_small_n2 = -1;    // tier-2 tests per wave at most for tests under 65,536 samples (-1: one per slot)
@@ -150,8 +185,8 @@ struct fpgm_engine {
     // tier-2 method: the autotuner's table (fastpgm_gb300/tune_table.txt, FPGM_TUNE_TABLE) or a
     // fixed sample-count cut-over (FPGM_PART_CUTOVER, default 65,536)
     int64_t part_min_samples = kPartMinSamples;
-    DevBuf tune;
-    bool tune_loaded = false;
+    DevBuf tune, tune_obs;  // a fixed table (FPGM_TUNE_TABLE) / the online autotuner's timings
+    bool tune_loaded = false, tune_online = true;
     std::string tune_source;
     // result
     bool has_result = false;
@@ -357,32 +392,47 @@ __global__ void wave_plan_kernel(int n_edges, const uint8_t *status, const uint6
 __global__ void wave_reduce_kernel(int n_edges, const int32_t *off, const uint8_t *flag, uint8_t *status,
                                    uint64_t *next, const uint64_t *total, uint64_t *seprank,
                                    unsigned long long *stats) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n_edges) return;
-    const int o = off[e], g = off[e + 1] - o;
-    if (g == 0) return;
-    int first = -1;
-    bool bad = false;
-    for (int k = 0; k < g; ++k) {
-        uint8_t f = flag[o + k];
-        if (f == 2) bad = true;
-        if (f == 1) {
-            first = k;
-            break;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long bad = 0, exec = 0, det = 0, unresolved = 0;
+    if (e < n_edges) {
+        const int o = off[e], g = off[e + 1] - o;
+        if (g > 0) {
+            int first = -1;
+            for (int k = 0; k < g; ++k) {
+                const uint8_t f = flag[o + k];
+                if (f == 2) bad = 1;
+                if (f == 1) {
+                    first = k;
+                    break;
+                }
+            }
+            exec = (unsigned long long)g;
+            if (first >= 0) {
+                status[e] = kStatusRemoved;
+                seprank[e] = next[e] + first;
+                det = (unsigned long long)(first + 1);
+            } else {
+                const uint64_t nx = next[e] + g;
+                next[e] = nx;
+                det = (unsigned long long)g;
+                if (nx == total[e]) status[e] = kStatusKept;
+                else unresolved = 1;
+            }
         }
     }
-    if (bad) atomicAdd(&stats[ST_UNSUPPORTED], 1ull);
-    atomicAdd(&stats[ST_EXEC], (unsigned long long)g);
-    if (first >= 0) {
-        status[e] = kStatusRemoved;
-        seprank[e] = next[e] + first;
-        atomicAdd(&stats[ST_DET], (unsigned long long)(first + 1));
-    } else {
-        uint64_t nx = next[e] + g;
-        next[e] = nx;
-        atomicAdd(&stats[ST_DET], (unsigned long long)g);
-        if (nx == total[e]) status[e] = kStatusKept;
-        else atomicAdd(&stats[ST_UNRESOLVED], 1ull);
+    // one atomic per warp and counter: the level-0 wave has one edge per thread
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        bad += __shfl_xor_sync(0xffffffffu, bad, s);
+        exec += __shfl_xor_sync(0xffffffffu, exec, s);
+        det += __shfl_xor_sync(0xffffffffu, det, s);
+        unresolved += __shfl_xor_sync(0xffffffffu, unresolved, s);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (bad) atomicAdd(&stats[ST_UNSUPPORTED], bad);
+        if (exec) atomicAdd(&stats[ST_EXEC], exec);
+        if (det) atomicAdd(&stats[ST_DET], det);
+        if (unresolved) atomicAdd(&stats[ST_UNRESOLVED], unresolved);
     }
 }
 
@@ -503,11 +553,11 @@ __global__ void wave_ctl_init_kernel(WaveCtl *c, unsigned long long *stats, long
 // item e is edge e, one test each).  The pair's dx x dy block of G -- rows of x's states,
 // columns of y's -- goes into the warp's shared slice, then the same scoring and decision
 // as the counting tiers (score_dense, CellTable.cpp:430-455 / IndependenceTest.cpp:295-364).
-__global__ void __launch_bounds__(kThreads, 2) level0_gram_score_kernel(WaveArgs a, const int32_t *G, int ld,
-                                                                        const int32_t *row_off, int n_items) {
+__global__ void __launch_bounds__(kThreads) level0_gram_score_kernel(WaveArgs a, const int32_t *G, int ld,
+                                                                     const int32_t *row_off, int n_items, int slice) {
     extern __shared__ int smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int *tab = smem + warp * kWarpInts;
+    int *tab = smem + warp * slice;  // slice: the largest pair table + marginals of this dataset
     const WarpGroup g{lane};
     for (int item = blockIdx.x * kWarps + warp; item < n_items; item += gridDim.x * kWarps) {
         const int x = a.ex[item], y = a.ey[item];
@@ -515,9 +565,18 @@ __global__ void __launch_bounds__(kThreads, 2) level0_gram_score_kernel(WaveArgs
         const int cells = dx * dy;
         int *ni = tab + cells, *nj = ni + dx, *nk = nj + dy;
         const int32_t *src = G + (int64_t)row_off[x] * ld + row_off[y];
-        for (int c = lane; c < cells; c += 32) {
-            const int i = c / dy, j = c - i * dy;
-            tab[c] = src[(int64_t)i * ld + j];
+        // the block's rows: every lane's loads issued before any is stored
+        for (int c0 = 0; c0 < cells; c0 += 128) {
+            int v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int c = c0 + 32 * u + lane;
+                const int i = c / dy, j = c - i * dy;
+                v[u] = c < cells ? __ldg(src + (int64_t)i * ld + j) : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (c0 + 32 * u + lane < cells) tab[c0 + 32 * u + lane] = v[u];
         }
         __syncwarp();
         const Verdict v = score_dense(g, tab, ni, nj, nk, dx, dy, 1, a.alpha, a.bt, a.detail != nullptr,
@@ -531,26 +590,18 @@ __global__ void __launch_bounds__(kThreads, 2) level0_gram_score_kernel(WaveArgs
 
 // ------------------------------------------------------------------ engine setup
 namespace {
-// The autotuner's table (written by fastpgm_gb300/tune.py from timings on the GPU): lines
-// "sb db cb method" after a '#' header; any entry not listed keeps the fixed cut-over.  Looked
-// for at $FPGM_TUNE_TABLE, else next to the library (../tune_table.txt); FPGM_TUNE_TABLE=off
-// or FPGM_PART_CUTOVER set keeps the fixed rule.
+// A fixed tier-2 method table in place of the online autotuner (FPGM_TUNE_TABLE=<file>, e.g.
+// written by fastpgm_gb300/tune.py): lines "sb db cb method"; any entry not listed keeps the
+// fixed cut-over.  FPGM_TUNE_TABLE=off keeps the fixed 65,536-sample cut-over alone.
 int load_tune_table(fpgm_engine *e) {
     const char *env = getenv("FPGM_TUNE_TABLE");
-    if ((env && strcmp(env, "off") == 0) || getenv("FPGM_PART_CUTOVER")) return FPGM_OK;
-    std::string path;
-    if (env) {
-        path = env;
-    } else {
-        Dl_info info;
-        if (dladdr(reinterpret_cast<void *>(&load_tune_table), &info) && info.dli_fname) {
-            path = info.dli_fname;
-            const size_t k = path.rfind('/');
-            path = (k == std::string::npos ? std::string(".") : path.substr(0, k)) + "/../tune_table.txt";
-        }
+    if (!env || !*env || strcmp(env, "off") == 0) {
+        if (env && strcmp(env, "off") == 0) e->tune_online = false;  // the fixed cut-over alone
+        return FPGM_OK;
     }
-    FILE *f = path.empty() ? nullptr : fopen(path.c_str(), "r");
-    if (!f) return FPGM_OK;
+    const std::string path = env;
+    FILE *f = fopen(path.c_str(), "r");
+    if (!f) return set_error(FPGM_ERR_IO, "FPGM_TUNE_TABLE: cannot open %s", path.c_str());
     std::vector<int8_t> t((size_t)kTuneSB * kTuneDB * kTuneCB);
     for (int sb = 0; sb < kTuneSB; ++sb)
         for (int db = 0; db < kTuneDB; ++db)
@@ -632,8 +683,16 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     if (const char *w = getenv("FPGM_WIDE_MIN_LOG")) e->wide_min_log = std::min(kPartMaxLog, std::max(0, atoi(w)));
     if (const char *w = getenv("FPGM_WIDE_PART_MIN")) e->wide_part_min = std::max(64, atoi(w));
     if (const char *w = getenv("FPGM_WIDE_DIRECT")) e->wide_direct = atoi(w) != 0;
-    if (const char *w = getenv("FPGM_PART_CUTOVER")) e->part_min_samples = std::max<int64_t>(0, atoll(w));
+    if (const char *w = getenv("FPGM_PART_CUTOVER")) {
+        e->part_min_samples = std::max<int64_t>(0, atoll(w));
+        e->tune_online = false;
+    }
+    if (const char *w = getenv("FPGM_TUNE")) e->tune_online = e->tune_online && atoi(w) != 0;
     RET(load_tune_table(e));
+    if (e->tune_online && !e->tune_loaded) {
+        RET(e->tune_obs.ensure((size_t)kTuneBuckets * 8 * 8));
+        CK(cudaMemset(e->tune_obs.p, 0, (size_t)kTuneBuckets * 8 * 8));
+    }
     if (getenv("FPGM_PHASE_TIMERS")) {
         RET(e->phase_timers.ensure(32 * 8));
         CK(cudaMemset(e->phase_timers.p, 0, 32 * 8));
@@ -651,7 +710,8 @@ extern "C" int fpgm_engine_destroy(fpgm_engine *e) {
                       &e->log_vars, &e->log_meta, &e->node_cnt, &e->node_off, &e->slots, &e->plain_ws,
                       &e->tests_buf, &e->detail_buf, &e->item_vars, &e->lists, &e->band,
                       &e->phase_timers, &e->var_off, &e->var_S, &e->var_lo, &e->var_hi, &e->mle_counts,
-                      &e->mle_pot, &e->mle_meta, &e->wide, &e->wide_items, &e->tune, &e->wave_ctl};
+                      &e->mle_pot, &e->mle_meta, &e->wide, &e->wide_items, &e->tune, &e->wave_ctl,
+                      &e->tune_obs};
     for (DevBuf *b : bufs) b->release();
     gram_destroy(e->gram);
     if (e->ev0) cudaEventDestroy(e->ev0);
@@ -851,6 +911,7 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t ite
             a.wide_direct = e->wide_direct;
         }
         a.tune = e->tune_loaded ? e->tune.as<int8_t>() : nullptr;
+        a.tune_obs = (e->tune_online && !e->tune_loaded) ? e->tune_obs.as<unsigned long long>() : nullptr;
         a.part_min_samples = e->part_min_samples;
     }
     a.part_max_log = e->part_max_log;
@@ -1035,8 +1096,9 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
         if (gram) {  // level 0: every pair's table from the tensor-core Gram matrix (one wave, one test per edge)
             int nl = 0;
             RET(gram_run(e->gram, e->stream, dstat + ST_TIMEOUT, &nl));
-            level0_gram_score_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(
-                a, gram_counts(e->gram), gram_ld(e->gram), gram_row_off(e->gram), (int)n_active);
+            const int slice = gram_slice_ints(e->gram);
+            level0_gram_score_kernel<<<e->num_sms * e->gram_score_ctas, kThreads, kWarps * slice * 4, e->stream>>>(
+                a, gram_counts(e->gram), gram_ld(e->gram), gram_row_off(e->gram), (int)n_active, slice);
             CK(cudaGetLastError());
             st->kernel_launches += nl + 3;  // plan, one-hot + GEMM, scoring, reduce
         } else {
@@ -1226,6 +1288,12 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
                     RET(gram_plan(e->gram, n, e->h_card.data(), e->S, e->cols.as<uint8_t>(), e->var_off.as<int64_t>(),
                                   e->card.as<uint8_t>(), e->num_sms, e->stream, &e->gram_ok));
                     e->gram_planned = true;
+                    if (e->gram_ok) {
+                        int occ = 0;
+                        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, level0_gram_score_kernel, kThreads,
+                                                                         kWarps * gram_slice_ints(e->gram) * 4));
+                        e->gram_score_ctas = std::max(1, occ);
+                    }
                 }
                 gram = e->gram_ok;
             }
@@ -1276,6 +1344,19 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
     double dp;
     memcpy(&dp, &mdp, 8);
     st->max_abs_dp = dp;
+    if (e->tune_online && e->tune_obs.p) {  // what the online autotuner has learnt so far
+        std::vector<unsigned long long> o((size_t)kTuneBuckets * 8);
+        CK(cudaMemcpyAsync(o.data(), e->tune_obs.p, o.size() * 8, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        for (int b = 0; b < kTuneBuckets; ++b) {
+            const unsigned long long *q = &o[(size_t)8 * b];
+            st->tune_timed += (int64_t)(q[0] + q[2]);
+            if (q[0] && q[2]) {
+                ++st->tune_buckets;
+                if ((double)q[1] / q[0] <= (double)q[3] / q[2]) ++st->tune_partition;
+            }
+        }
+    }
     // result: adjacency bitset + removal log
     std::vector<uint32_t> hb((size_t)n * W);
     std::vector<int32_t> lp((size_t)log_count * 2 + 2), lm((size_t)log_count * 2 + 2), lv((size_t)var_count + 1);

@@ -8,6 +8,12 @@ namespace fpgm {
 // Records a printf-style message as the calling thread's last error and returns code.
 int set_error(int code, const char *fmt, ...);
 
+// Device allocations of the engine go through these: cudaMalloc / cudaFree with a
+// process-wide byte count, refused with FPGM_ERR_OOM beyond FPGM_DEVICE_MEM_CAP bytes when
+// that is set (the allocation-failure path, testable without exhausting a GPU).
+int dev_alloc(void **p, size_t bytes);
+void dev_free(void *p, size_t bytes);
+
 #define RET_IF(call)                  \
     do {                              \
         int r_ = (call);              \
@@ -29,5 +35,6 @@ int gram_run(GramLevel0 *g, cudaStream_t stream, unsigned long long *err, int *l
 const int32_t *gram_counts(const GramLevel0 *g);   // G, row pitch gram_ld(g) int32
 const int32_t *gram_row_off(const GramLevel0 *g);  // device: first one-hot row of each variable
 int gram_ld(const GramLevel0 *g);
+int gram_slice_ints(const GramLevel0 *g);          // largest pair table + marginals (ints), 16-aligned
 double gram_flops(const GramLevel0 *g);            // tensor-core flops of one gram_run
 }  // namespace fpgm

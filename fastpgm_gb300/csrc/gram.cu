@@ -295,7 +295,7 @@ using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t,
 }  // namespace
 
 struct GramLevel0 {
-    int n = 0, R = 0, R_pad = 0, n_rt = 0, kblocks = 0, ksplit = 1, num_sms = 0;
+    int n = 0, R = 0, R_pad = 0, n_rt = 0, kblocks = 0, ksplit = 1, num_sms = 0, maxc = 1;
     int64_t S = 0, K_pad = 0;
     uint8_t *H = nullptr;
     size_t H_bytes = 0;
@@ -314,19 +314,18 @@ GramLevel0 *gram_create() { return new GramLevel0(); }
 
 void gram_destroy(GramLevel0 *g) {
     if (!g) return;
-    if (g->H) cudaFree(g->H);
-    if (g->G) cudaFree(g->G);
-    if (g->row_off) cudaFree(g->row_off);
+    dev_free(g->H, g->H_bytes);
+    dev_free(g->G, g->G_bytes);
+    dev_free(g->row_off, g->row_bytes);
     delete g;
 }
 
 static int grow(void **p, size_t *have, size_t need) {
     if (need <= *have) return FPGM_OK;
-    if (*p) cudaFree(*p);
+    dev_free(*p, *have);
     *p = nullptr;
     *have = 0;
-    cudaError_t e = cudaMalloc(p, need);
-    if (e != cudaSuccess) return set_error(FPGM_ERR_OOM, "cudaMalloc(%zu) failed: %s", need, cudaGetErrorString(e));
+    RET_IF(dev_alloc(p, need));
     *have = need;
     return FPGM_OK;
 }
@@ -345,6 +344,7 @@ int gram_plan(GramLevel0 *g, int n, const uint8_t *h_card, int64_t S, const uint
     // pair tables are scored by one warp in its 12 KB shared slice; the Gram matrix must fit
     if (maxc * maxc + 2 * maxc + 1 > 3000 || R > 32768 || S < 1 || S > (1 << 24) - 1) return FPGM_OK;
     g->n = n;
+    g->maxc = maxc;
     g->R = R;
     g->R_pad = (R + kTile - 1) / kTile * kTile;
     g->n_rt = g->R_pad / kTile;
@@ -411,6 +411,7 @@ int gram_run(GramLevel0 *g, cudaStream_t stream, unsigned long long *err, int *l
 const int32_t *gram_counts(const GramLevel0 *g) { return g->G; }
 const int32_t *gram_row_off(const GramLevel0 *g) { return g->row_off; }
 int gram_ld(const GramLevel0 *g) { return g->R_pad; }
+int gram_slice_ints(const GramLevel0 *g) { return (g->maxc * g->maxc + 2 * g->maxc + 1 + 15) & ~15; }
 double gram_flops(const GramLevel0 *g) {
     const double tiles = (double)g->n_rt * (g->n_rt + 1) / 2;
     return tiles * 2.0 * kTile * kTile * (double)g->K_pad;

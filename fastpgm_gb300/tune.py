@@ -1,16 +1,17 @@
-"""Autotuner of the tier-2 method, keyed by (samples, |Z|, joint cardinality).
+"""Offline sweep of the tier-2 method, keyed by (samples, |Z|, joint cardinality).
 
 A CI test whose joint table is too large for shared memory and whose Z strata overflow the
 compact kernel's shared hash is counted one of two ways: the compact kernel's global strata
-hash, or the partition kernel (samples split by stratum into shared-memory partitions).  Which
-is faster depends on the sample count, on |Z| and on how many strata the test has, i.e. on its
-joint cardinality dz*dx*dy against the sample count.  This sweep times both methods on the GPU
-over synthetic datasets of every sample-count bucket and several cardinality ranges, for |Z| =
-2 .. 12, and writes the faster method per (samples, |Z|, cells/samples) bucket to
-fastpgm_gb300/tune_table.txt, which every engine loads at creation (FPGM_TUNE_TABLE overrides
-the path; FPGM_TUNE_TABLE=off keeps the fixed 65,536-sample cut-over).
+hash, or the partition kernel (samples split by stratum into shared-memory partitions).  The
+engine chooses per test with its online autotuner (ci_kernels.cuh, tier2_pick_partitions):
+per (samples, |Z|, cells/samples) bucket it times both methods on the tests it runs and
+prefers the faster.  This script is the offline alternative: it times both methods on
+batches of random tests over synthetic datasets of every sample-count bucket and writes a
+fixed table, which an engine uses instead when FPGM_TUNE_TABLE names it.  (Measured on
+GB300, such a table lost 4% at the 1,041-node workload against the fixed cut-over: random
+batches are not the tests a skeleton runs, which is why the online tuner is the default.)
 
-Run on a GPU:  python -m fastpgm_gb300.tune [--out PATH] [--quick]
+Run on a GPU:  python -m fastpgm_gb300.tune --out PATH [--quick]
 """
 import argparse
 import datetime
@@ -21,7 +22,7 @@ import time
 import numpy as np
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-TABLE = os.path.join(PKG, "tune_table.txt")
+TABLE = os.path.join(PKG, "tune_table.txt")  # default output path (not loaded unless FPGM_TUNE_TABLE names it)
 
 KTUNE_SB, KTUNE_DB, KTUNE_CB = 6, 12, 6   # the engine's kTuneSB / kTuneDB / kTuneCB
 SAMPLES = [10000, 20000, 40000, 80000, 160000, 240000]  # one per sample bucket
@@ -114,17 +115,6 @@ def sweep(out=TABLE, quick=False, log=print):
             tp, th = votes[key]
             f.write("%d %d %d %d  %.3f %.3f\n" % (key[0], key[1], key[2], 1 if tp < th else 0, tp * 1e3, th * 1e3))
     return votes
-
-
-def summary(path=TABLE):
-    """What the table holds (for the benchmark line): entries and how many pick partitions."""
-    if not os.path.exists(path):
-        return None
-    rows = [l.split() for l in open(path) if l.strip() and not l.startswith("#")]
-    when = [l.split("(")[-1].rstrip(")\n") for l in open(path) if l.startswith("# written by")]
-    return {"table": os.path.relpath(path, os.path.dirname(PKG)), "entries": len(rows),
-            "partition_entries": sum(1 for r in rows if r[3] == "1"), "written": when[0] if when else None,
-            "keys": "samples (6 buckets from 12,500), |Z| (1..12), log4(cells/samples) (6 buckets)"}
 
 
 def main():

@@ -95,6 +95,9 @@ typedef struct {
                                     pair scoring; 0 when level 0 ran on the counting kernels) */
     double gram_flops;           /* tensor-core flops of that Gram GEMM */
     int64_t gram_tests;          /* level-0 tests decided from the Gram matrix */
+    int32_t tune_buckets;        /* online autotuner: (samples, |Z|, cells/samples) buckets timed both ways */
+    int32_t tune_partition;      /* ... of which the partition kernel is the faster tier-2 method */
+    int64_t tune_timed;          /* tier-2 tests timed by the autotuner since the engine was created */
 } fpgm_pc_stats;
 
 typedef struct {

@@ -401,3 +401,38 @@ def test_autotuner_table_picks_the_tier2_method(monkeypatch, tmp_path):
         assert len(over) >= 4 and all(g.path == path for g in over), [g.path for g in got]
         for g, o in zip(got, exp):
             check(g, o, exact_p=g.rechecked == 1)
+
+
+_OOM = r"""
+import sys
+sys.path.insert(0, sys.argv[1])
+import fastpgm_gb300 as F
+raw, _, _ = F.make_config("c1")
+e = F.Engine(0)
+e.upload(raw)
+try:
+    e.pc_skeleton()
+    print("NO_ERROR")
+except F.FpgmError as x:
+    print("CODE", x.code, "FPGM_DEVICE_MEM_CAP" in str(x))
+print("DEPTH1", e.pc_skeleton(depth=1).to_dict()["n_levels"])
+print("BATCH", e.ci_test_batch([[0, 1, 2]], 1)[0].df >= 0)
+e.close()
+print("CLOSED")
+"""
+
+
+def test_allocation_failure_is_an_error_status():
+    """Device allocation failure (SURVEY's failure path: FPGM_ERR_OOM) without exhausting a
+    GPU: FPGM_DEVICE_MEM_CAP caps the engine's device memory at 16 MB, so level 1 of c1 cannot
+    size its wave buffers.  The skeleton call returns FPGM_ERR_OOM with the message, the engine
+    stays usable for calls that fit (level 0 alone, a CI test batch) and closes cleanly."""
+    import subprocess
+    import sys
+    from conftest import ROOT
+    env = dict(os.environ, FPGM_DEVICE_MEM_CAP="16000000")
+    out = subprocess.run([sys.executable, "-c", _OOM, ROOT], capture_output=True, text=True, env=env, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = out.stdout.split("\n")
+    assert "CODE %d True" % F.FPGM_ERR_OOM in lines, out.stdout
+    assert "DEPTH1 1" in lines and "BATCH True" in lines and "CLOSED" in lines, out.stdout

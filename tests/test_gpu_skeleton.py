@@ -3,11 +3,12 @@ golden sepsets/CPDAGs and the oracle's per-level deterministic test counts."""
 import os
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, read_sepsets, sepset_arrays
+from conftest import GOLDEN, ROOT, read_sepsets, sepset_arrays
 from oracle import oracle as O
 import fastpgm_gb300 as F
 
@@ -105,8 +106,11 @@ def test_cli_and_python_binding_reproduce_alarm(alarm, tmp_path):
     golden = open(os.path.join(GOLDEN, "alarm_s5000_struct")).read()
     assert open(csv + "_struct").read() == golden
     os.remove(csv + "_struct")
-    from fastpgm_gb300 import cmake_example as fastpgm
-    fastpgm.BNSL_PCStable(0, 1, 1, 0.05, "", csv, True)
+    # the reference driver's own import line, resolved through PYTHONPATH from another directory
+    code = "import cmake_example as fastpgm; fastpgm.BNSL_PCStable(0, 1, 1, 0.05, '', %r, True)" % csv
+    env = dict(os.environ, PYTHONPATH=ROOT)
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=str(tmp_path), env=env)
+    assert out.returncode == 0, out.stdout + out.stderr
     assert open(csv + "_struct").read() == golden
     out = subprocess.run([F.CLI_PATH, "-j", "0", "-m", "0", "-e", "1", "-f2", csv], capture_output=True, text=True)
     assert out.returncode == 0
@@ -323,3 +327,24 @@ def test_device_driven_waves_match_host_driven(monkeypatch, name):
     assert np.array_equal(rg["adj"], rh["adj"]) and rg["sepsets"] == rh["sepsets"]
     for k in ("tests", "tests_executed", "edges_after", "waves"):
         assert sg[k] == sh[k], k
+
+
+def test_online_autotuner_times_both_tier2_methods(monkeypatch):
+    """The online autotuner times the partition kernel and the global strata hash per
+    (samples, |Z|, cells/samples) bucket on the tier-2 tests a skeleton runs (FPGM_WIDE=0 so
+    that no wave hands its tests over wholesale): after two skeletons of a 70,000-sample
+    dataset with 6-9 states it has timed tests both ways, and the skeleton equals the oracle's
+    whichever method each test took; FPGM_TUNE=0 times nothing."""
+    raw, _, _ = F.generate(n_nodes=12, n_samples=70000, seed=72, n_edges=30, max_indegree=5, card=(6, 10))
+    cols, card = O.relabel(raw)
+    ref = O.pc_skeleton(cols, card, threads=16)
+    for tune, timed in (("1", True), ("0", False)):
+        monkeypatch.setenv("FPGM_WIDE", "0")
+        monkeypatch.setenv("FPGM_TUNE", tune)
+        with F.Engine(0) as e:
+            e.upload(raw)
+            for _ in range(2):
+                st = e.pc_skeleton().to_dict()
+                res = e.result()
+                assert np.array_equal(res["adj"], ref["adj"]) and res["sepsets"] == ref["sepsets"]
+        assert (st["tune_timed"] > 0) == timed and (st["tune_buckets"] > 0) == timed

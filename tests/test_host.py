@@ -5,6 +5,7 @@ import ctypes
 import os
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -276,3 +277,13 @@ def test_autotuner_bucket_keys():
     assert tune.tune_index(50000, 6, 50000 * 100) == (3, 5, 3)
     assert tune.tune_index(10 ** 7, 40, 1e30) == (5, 11, 5)
     assert tune.tune_index(100000, 0, 1) == (4, 0, 0)
+
+
+def test_top_level_cmake_example_module():
+    """`import cmake_example` -- the first line of the reference's python/pyfastpgm.py --
+    resolves to this repository's drop-in when the repository is on PYTHONPATH."""
+    code = "import cmake_example as f; print(f.BNSL_PCStable.__module__, callable(f.BNL_PCStable))"
+    env = dict(os.environ, PYTHONPATH=ROOT)
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd="/", env=env)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split() == ["fastpgm_gb300.cmake_example", "True"]
