@@ -115,8 +115,8 @@ constexpr int kTuneSB = 6;   // samples: < 12.5k, < 25k, < 50k, < 100k, < 200k, 
 constexpr int kTuneDB = 12;  // |Z| = 1 .. 11, 12 and more
 constexpr int kTuneCB = 6;   // cells / samples: < 4, < 16, < 64, < 256, < 1024, more
 constexpr int kTuneBuckets = kTuneSB * kTuneDB * kTuneCB;
-constexpr unsigned long long kTuneExplore = 16;  // tests timed with each method before either is preferred
-constexpr unsigned long long kTuneRefresh = 32;  // then one test in this many takes the other method
+constexpr unsigned long long kTuneExplore = 8;    // tests timed with each method before either is preferred
+constexpr unsigned long long kTuneRefresh = 256;  // then one test in this many takes the other method
 __host__ __device__ inline int tune_index(int64_t S, int d, double cells) {
     int sb = 0;
     for (int64_t lim = 12500; sb < kTuneSB - 1 && S >= lim; lim *= 2) ++sb;
@@ -130,7 +130,9 @@ __host__ __device__ inline int tune_index(int64_t S, int d, double cells) {
 // Online autotuner (one thread decides for its CTA): per (samples, |Z|, cells/samples)
 // bucket, the device time of tests counted each way is summed as they finish; a bucket
 // first alternates the two methods until each has kTuneExplore timed tests, then takes the
-// faster on average, giving one test in kTuneRefresh to the other so both stay measured.
+// faster on average, giving one test in kTuneRefresh to the other so both stay measured
+// (measured at 1,041 variables x 100,000 samples: one in 32 cost 4% against the best fixed
+// rule, as the slower method is 1.5-3x slower there).
 // *bucket = the bucket whose hash-path time the caller must add (-1: none).
 __device__ inline bool tier2_pick_partitions(const WaveArgs &a, int64_t S, int d, double cells, int *bucket) {
     *bucket = -1;

@@ -16,7 +16,9 @@ Writes tests/golden/full_<cfg>.json with, per dataset (c5: per job):
   n_removed     removed edges (one separating set each)
 and, for c5, the level totals over all jobs (what a multi-dataset skeleton reports).
 
-Run:  python tests/golden/make_full.py [c3] [c4] [c5]   (default: all three; c5 takes longest)
+Run:  python tests/golden/make_full.py [c3] [c4] [c5] [--workers N]   (default: all three; c5 takes
+longest: its 64 jobs run N at a time in separate processes, each job's digest cached under
+tests/golden/.full_cache/ until the fixture is written)
 """
 import json
 import os
@@ -42,20 +44,44 @@ def dataset_digest(raw, depth, threads):
     return d, dt
 
 
+CACHE = os.path.join(HERE, ".full_cache")
+
+
+def _c5_job(args):
+    """One c5 job's digest in a worker process (cached by job index)."""
+    j, threads = args
+    path = os.path.join(CACHE, "c5_job%02d.json" % j)
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    spec = dict(C.c5_jobs()[j])
+    depth = spec.pop("depth")
+    raw, _, _ = O.generate(**spec)
+    d, dt = dataset_digest(raw, depth, threads)
+    os.makedirs(CACHE, exist_ok=True)
+    with open(path + ".tmp", "w") as f:
+        json.dump(d, f)
+    os.replace(path + ".tmp", path)
+    print("c5 job %d: %d x %d, %d tests, %.1f s" % (j, raw.shape[0], raw.shape[1], sum(d["tests"]), dt), flush=True)
+    return d
+
+
 def main():
     names = [a for a in sys.argv[1:] if a in ("c3", "c4", "c5")] or ["c3", "c4", "c5"]
-    threads = os.cpu_count() or 1
+    workers = int(sys.argv[sys.argv.index("--workers") + 1]) if "--workers" in sys.argv else 1
+    threads = max(1, (os.cpu_count() or 1) // workers)
     O.build()
     for name in names:
         t0 = time.perf_counter()
         if name == "c5":
-            data, depth = C.make_jobs(C.c5_jobs(), generate=O.generate)
-            jobs = []
-            for j, raw in enumerate(data):
-                d, dt = dataset_digest(raw, depth, threads)
-                jobs.append(d)
-                print("c5 job %d: %d x %d, %d tests, %.1f s" % (j, raw.shape[0], raw.shape[1], sum(d["tests"]), dt),
-                      flush=True)
+            import multiprocessing as mp
+            specs = C.c5_jobs()
+            depth = specs[0]["depth"]
+            # largest first, so the long jobs start at once
+            order = sorted(range(len(specs)), key=lambda j: -specs[j]["n_samples"] * specs[j]["n_nodes"])
+            with mp.get_context("spawn").Pool(workers) as pool:
+                done = dict(zip(order, pool.map(_c5_job, [(j, threads) for j in order], chunksize=1)))
+            jobs = [done[j] for j in range(len(specs))]
             L = max(len(d["tests"]) for d in jobs)
             out = {"config": name, "depth": depth, "jobs": jobs,
                    "level_tests": [sum(d["tests"][i] for d in jobs if i < len(d["tests"])) for i in range(L)]}
