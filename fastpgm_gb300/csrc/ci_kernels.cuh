@@ -129,8 +129,9 @@ __host__ __device__ inline int tune_index(int64_t S, int d, double cells) {
 
 // Online autotuner (one thread decides for its CTA): per (samples, |Z|, cells/samples)
 // bucket, the device time of tests counted each way is summed as they finish; a bucket
-// first alternates the two methods until each has kTuneExplore timed tests, then takes the
-// faster on average, giving one test in kTuneRefresh to the other so both stay measured
+// first alternates the two methods until each has kTuneExplore timed tests, then keeps the
+// fixed rule's method unless the other is at least 10% faster on average, giving one test
+// in kTuneRefresh to the other so both stay measured
 // (measured at 1,041 variables x 100,000 samples: one in 32 cost 4% against the best fixed
 // rule, as the slower method is 1.5-3x slower there).
 // *bucket = the bucket whose hash-path time the caller must add (-1: none).
@@ -146,9 +147,10 @@ __device__ inline bool tier2_pick_partitions(const WaveArgs &a, int64_t S, int d
     if (np < kTuneExplore || nh < kTuneExplore) {
         part = (k & 1ull) == 0;
     } else {
+        // leave the fixed rule's method only for one at least 10% faster on average
         const double mp = (double)*(volatile unsigned long long *)&o[1] / (double)np;
         const double mh = (double)*(volatile unsigned long long *)&o[3] / (double)nh;
-        part = mp <= mh;
+        part = S >= a.part_min_samples ? !(mh < 0.9 * mp) : mp < 0.9 * mh;
         if (k % kTuneRefresh == 0) part = !part;
     }
     if (!part) *bucket = b;
