@@ -29,6 +29,7 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kSmemBytes = 96 * 1024;
 constexpr int kCtaInts = kSmemBytes / 4;                 // CTA tier: table + marginals
 constexpr int kWarpInts = kSmemBytes / 4 / kWarps;      // warp tier: per-warp region
+constexpr int kWarpIntsSmall = 2048;                     // ... with 8 KB slices (3 CTAs per SM)
 constexpr int kGlobalWarpTab = 255 * 255 + 2 * 255 + 1;  // largest dx*dy + dx + dy
 constexpr int kBinomN = 4096;
 constexpr int kBinomK = 32;

@@ -106,6 +106,7 @@ struct WaveArgs {
     // part_min_samples decides (samples >= it: partitions).
     const int8_t *tune;
     unsigned long long *tune_obs;  // 8 per bucket: n_part, ns_part, n_hash, ns_hash, decisions
+    int32_t warp_ints;             // ints of the warp tier's per-warp slice (its table limit)
     int64_t part_min_samples;
 };
 
@@ -217,7 +218,7 @@ __global__ void classify_kernel(WaveArgs a) {
             tier = 3;  // stratum codes would not fit 64 bits
         } else {
             const int64_t need = dz * dx * dy + dz * (dx + dy + 1);
-            tier = need <= kWarpInts - 32 ? 0 : (need <= kCtaInts - 64 ? 1 : 2);
+            tier = need <= a.warp_ints - 32 ? 0 : (need <= kCtaInts - 64 ? 1 : 2);
             if (tier == 2 && a.slot_mem == nullptr) tier = 3;
         }
         if (tier == 3) {
@@ -289,7 +290,11 @@ __device__ inline void record(const WaveArgs &a, int item, const Verdict &v, int
 }
 
 // ---------------------------------------------------------------- tier 0: warp per test
-__global__ void __launch_bounds__(kThreads, 2) ci_warp_kernel(WaveArgs a) {
+// kSlice: ints of a warp's shared slice; kMinBlocks: resident CTAs per SM the launch bounds
+// ask for (12 KB slices: 2 CTAs; 8 KB slices: 3 CTAs, more warps per SM for smaller tables).
+template <int kSlice, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) ci_warp_kernel(WaveArgs a) {
+    constexpr int kWarpInts = kSlice;
     extern __shared__ int smem[];
     __shared__ const uint8_t *s_col[kWarps][kMaxCols];
     __shared__ uint32_t s_dim[kWarps][kMaxCols];

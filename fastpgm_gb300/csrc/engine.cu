@@ -172,6 +172,8 @@ struct fpgm_engine {
     int part_max_log = kPartMaxLog;  // FPGM_PART_MAX_LOG (tests): fewer partitions before the global hash
     int64_t slot_bytes = 0, slot_S = 0;  // slot_S: the sample count the slots' layout was made for
     bool wave_log = false;               // FPGM_WAVE_LOG: one stderr line per wave (tier sizes, kernel times)
+    bool warp_small = false;             // FPGM_WARP_SLICE=2048: 8 KB warp-tier slices, 3 CTAs per SM
+    int warp_blocks_small = 0;
     // level 0 on the tensor cores (FPGM_GRAM=0 keeps it on the counting kernels)
     GramLevel0 *gram = nullptr;
     bool gram_on = true, gram_planned = false, gram_ok = false;
@@ -647,7 +649,9 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     CK(cudaEventCreate(&e->ev0));
     CK(cudaEventCreate(&e->ev1));
     CK(cudaEventCreate(&e->ev2));
-    CK(cudaFuncSetAttribute(ci_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    CK(cudaFuncSetAttribute(ci_warp_kernel<kWarpInts, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    CK(cudaFuncSetAttribute(ci_warp_kernel<kWarpIntsSmall, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            kWarps * kWarpIntsSmall * 4));
     CK(cudaFuncSetAttribute(ci_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     CK(cudaFuncSetAttribute(ci_compact_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     CK(cudaFuncSetAttribute(ci_compact_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
@@ -656,8 +660,13 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     CK(cudaFuncSetAttribute(level0_gram_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     CK(cudaFuncSetAttribute(ci_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     int occ = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ci_warp_kernel, kThreads, kSmemBytes));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ci_warp_kernel<kWarpInts, 2>, kThreads, kSmemBytes));
     e->ci_blocks = e->num_sms * std::max(1, occ);
+    if (const char *w = getenv("FPGM_WARP_SLICE")) e->warp_small = atoi(w) == kWarpIntsSmall;
+    int occ_small = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_small, ci_warp_kernel<kWarpIntsSmall, 3>, kThreads,
+                                                     kWarps * kWarpIntsSmall * 4));
+    e->warp_blocks_small = e->num_sms * std::max(1, occ_small);
     // binomial table, saturating
     std::vector<uint64_t> bt((size_t)kBinomN * kBinomK, 0);
     for (int n = 0; n < kBinomN; ++n) {
@@ -915,7 +924,16 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t ite
         a.part_min_samples = e->part_min_samples;
     }
     a.part_max_log = e->part_max_log;
+    a.warp_ints = e->warp_small ? kWarpIntsSmall : kWarpInts;
     return FPGM_OK;
+}
+
+// The warp tier (tier 0) with the engine's slice size.
+void launch_warp_tier(fpgm_engine *e, const WaveArgs &a) {
+    if (e->warp_small)
+        ci_warp_kernel<kWarpIntsSmall, 3><<<e->warp_blocks_small, kThreads, kWarps * kWarpIntsSmall * 4, e->stream>>>(a);
+    else
+        ci_warp_kernel<kWarpInts, 2><<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
 }
 
 // Tier 2 on the current stream: the compact kernel, the partitioned kernel for the tests it
@@ -937,7 +955,7 @@ int launch_compact(fpgm_engine *e, const WaveArgs &a, int grid) {
 template <int kSource>
 int launch_tiers(fpgm_engine *e, const WaveArgs &a) {
     classify_kernel<kSource><<<e->ci_blocks, kThreads, 0, e->stream>>>(a);
-    ci_warp_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+    launch_warp_tier(e, a);
     ci_cta_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
     int n = 3;
     if (a.slot_mem) n += launch_compact(e, a, e->n_slots);
@@ -1002,7 +1020,7 @@ int run_waves_graph(fpgm_engine *e, double alpha, int d, int64_t n_active, fpgm_
                                       (int)(n_active + 1), e->stream);
         wave_stamp_kernel<<<1, 1, 0, e->stream>>>(ctl, -1);
         classify_kernel<SRC_WAVE><<<e->ci_blocks, kThreads, 0, e->stream>>>(a);
-        ci_warp_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+        launch_warp_tier(e, a);
         ci_cta_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
         wave_stamp_kernel<<<1, 1, 0, e->stream>>>(ctl, 0);
         per_wave = 9;  // prep, plan, 3 stamps, classify, warp tier, CTA tier, reduce, tail (+ tier 2)
@@ -1103,7 +1121,7 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
             st->kernel_launches += nl + 3;  // plan, one-hot + GEMM, scoring, reduce
         } else {
             classify_kernel<SRC_WAVE><<<e->ci_blocks, kThreads, 0, e->stream>>>(a);
-            ci_warp_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
+            launch_warp_tier(e, a);
             ci_cta_kernel<<<e->ci_blocks, kThreads, kSmemBytes, e->stream>>>(a);
             CK(cudaGetLastError());
             st->kernel_launches += 5;  // plan, classify, warp tier, CTA tier, reduce

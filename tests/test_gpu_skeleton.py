@@ -348,3 +348,18 @@ def test_online_autotuner_times_both_tier2_methods(monkeypatch):
                 res = e.result()
                 assert np.array_equal(res["adj"], ref["adj"]) and res["sepsets"] == ref["sepsets"]
         assert (st["tune_timed"] > 0) == timed and (st["tune_buckets"] > 0) == timed
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_small_warp_slices_match_reference(monkeypatch, tmp_path, name):
+    """The warp tier with 8 KB slices (FPGM_WARP_SLICE=2048: 3 CTAs per SM, tables over 2,016
+    ints to the CTA tier) gives the reference's separating sets and CPDAG."""
+    monkeypatch.setenv("FPGM_WARP_SLICE", "2048")
+    raw, depth, _ = F.make_config(name)
+    with F.Engine(0) as e:
+        e.upload(raw)
+        e.pc_skeleton(depth=depth)
+        res = e.result()
+    assert res["sepsets"] == read_sepsets(os.path.join(GOLDEN, name + "_sepsets"))
+    n = raw.shape[0]
+    assert struct_of(tmp_path, ["V%d" % i for i in range(n)], res) == open(os.path.join(GOLDEN, name + "_struct")).read()
