@@ -366,7 +366,7 @@ def gram_roofline(tot):
 def level_record(st):
     return {"levels": st["n_levels"], "tests_per_level": st["tests"], "tests_executed_per_level": st["tests_executed"],
             "edges_after": st["edges_after"], "waves": st["waves"], "level_ms": [round(x, 3) for x in st["ms"]],
-            "large_table_ms": st["large_ms"]}
+            "large_table_ms": st["large_ms"], "graph_build_ms": round(st["graph_ms"], 3)}
 
 
 def recorded(name):

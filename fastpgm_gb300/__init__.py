@@ -44,7 +44,7 @@ class PCStats(ctypes.Structure):
                 ("count_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("span_ms", ctypes.c_double),
                 ("total_ms", ctypes.c_double), ("large_bytes", ctypes.c_double), ("gram_ms", ctypes.c_double),
                 ("gram_flops", ctypes.c_double), ("gram_tests", ctypes.c_int64), ("tune_buckets", ctypes.c_int32),
-                ("tune_partition", ctypes.c_int32), ("tune_timed", ctypes.c_int64)]
+                ("tune_partition", ctypes.c_int32), ("tune_timed", ctypes.c_int64), ("graph_ms", ctypes.c_double)]
 
     def to_dict(self):
         L = self.n_levels
@@ -61,7 +61,7 @@ class PCStats(ctypes.Structure):
                 "large_bytes": float(self.large_bytes), "gram_ms": float(self.gram_ms),
                 "gram_flops": float(self.gram_flops), "gram_tests": int(self.gram_tests),
                 "tune_buckets": int(self.tune_buckets), "tune_partition": int(self.tune_partition),
-                "tune_timed": int(self.tune_timed)}
+                "tune_timed": int(self.tune_timed), "graph_ms": float(self.graph_ms)}
 
 
 class GenSpec(ctypes.Structure):

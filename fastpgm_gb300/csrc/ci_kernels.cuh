@@ -117,7 +117,8 @@ constexpr int kTuneDB = 12;  // |Z| = 1 .. 11, 12 and more
 constexpr int kTuneCB = 6;   // cells / samples: < 4, < 16, < 64, < 256, < 1024, more
 constexpr int kTuneBuckets = kTuneSB * kTuneDB * kTuneCB;
 constexpr unsigned long long kTuneExplore = 8;    // tests timed with each method before either is preferred
-constexpr unsigned long long kTuneRefresh = 256;  // then one test in this many takes the other method
+constexpr unsigned long long kTuneRefresh = 256;  // then one test in this many takes the other method ...
+constexpr unsigned long long kTuneSettled = 32;   // ... until that method has this many timed tests
 __host__ __device__ inline int tune_index(int64_t S, int d, double cells) {
     int sb = 0;
     for (int64_t lim = 12500; sb < kTuneSB - 1 && S >= lim; lim *= 2) ++sb;
@@ -132,7 +133,7 @@ __host__ __device__ inline int tune_index(int64_t S, int d, double cells) {
 // bucket, the device time of tests counted each way is summed as they finish; a bucket
 // first alternates the two methods until each has kTuneExplore timed tests, then keeps the
 // fixed rule's method unless the other is at least 10% faster on average, giving one test
-// in kTuneRefresh to the other so both stay measured
+// in kTuneRefresh to the other until it has kTuneSettled timed tests
 // (measured at 1,041 variables x 100,000 samples: one in 32 cost 4% against the best fixed
 // rule, as the slower method is 1.5-3x slower there).
 // *bucket = the bucket whose hash-path time the caller must add (-1: none).
@@ -152,7 +153,7 @@ __device__ inline bool tier2_pick_partitions(const WaveArgs &a, int64_t S, int d
         const double mp = (double)*(volatile unsigned long long *)&o[1] / (double)np;
         const double mh = (double)*(volatile unsigned long long *)&o[3] / (double)nh;
         part = S >= a.part_min_samples ? !(mh < 0.9 * mp) : mp < 0.9 * mh;
-        if (k % kTuneRefresh == 0) part = !part;
+        if (k % kTuneRefresh == 0 && (part ? nh : np) < kTuneSettled) part = !part;
     }
     if (!part) *bucket = b;
     return part;

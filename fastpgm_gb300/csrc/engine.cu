@@ -164,15 +164,15 @@ struct fpgm_engine {
     DevBuf slots, plain_ws, tests_buf, detail_buf, item_vars, lists, band, phase_timers;
     DevBuf wide, wide_items;  // partition-parallel scoring: one WideTest per slot, kPartMax items each
     DevBuf wave_ctl;          // device-driven wave loop: q, wave count, per-group device time
+    DevBuf res_adj_d, res_key, res_idx, res_removed_d, res_cnt, res_vars_d;  // result assembly
     bool graph_on = true;     // FPGM_GRAPH=0: the host drives every wave (as FPGM_WAVE_LOG does)
-    double graph_build_ms = 0.0;  // host time spent capturing and instantiating level graphs
     DevBuf mle_counts, mle_pot, mle_meta;  // parameter learning: counts, potentials, per-node tables
     double band_alpha = -1.0;
     int n_slots = 0, hash_cap_global = 0;
     int part_max_log = kPartMaxLog;  // FPGM_PART_MAX_LOG (tests): fewer partitions before the global hash
     int64_t slot_bytes = 0, slot_S = 0;  // slot_S: the sample count the slots' layout was made for
     bool wave_log = false;               // FPGM_WAVE_LOG: one stderr line per wave (tier sizes, kernel times)
-    bool warp_small = false;             // FPGM_WARP_SLICE=2048: 8 KB warp-tier slices, 3 CTAs per SM
+    bool warp_small = true;              // 8 KB warp-tier slices, 3 CTAs per SM (FPGM_WARP_SLICE=3072: 12 KB, 2)
     int warp_blocks_small = 0;
     // level 0 on the tensor cores (FPGM_GRAM=0 keeps it on the counting kernels)
     GramLevel0 *gram = nullptr;
@@ -483,6 +483,45 @@ __global__ void degree_kernel(const uint32_t *bits, int n, int W, unsigned long 
 
 inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
+// ---- result assembly: 0/1 adjacency, removal log sorted by pair
+__global__ void expand_adj_kernel(const uint32_t *bits, int n, int W, uint8_t *adj) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= (int64_t)n * n) return;
+    const int a = (int)(i / n), b = (int)(i - (int64_t)a * n);
+    adj[i] = (uint8_t)((bits[(int64_t)a * W + (b >> 5)] >> (b & 31)) & 1u);
+}
+
+__global__ void log_keys_kernel(int R, int n, const int32_t *log_pair, uint32_t *key, int32_t *idx) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R) return;
+    key[i] = (uint32_t)log_pair[2 * i] * (uint32_t)n + (uint32_t)log_pair[2 * i + 1];
+    idx[i] = i;
+}
+
+// k-th record in pair order: its pair and its separating set's size (cnt[R] = 0 ends the scan)
+__global__ void log_gather_kernel(int R, const int32_t *order, const int32_t *log_pair, const int32_t *log_meta,
+                                  int32_t *removed, int32_t *cnt) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > R) return;
+    if (k == R) {
+        cnt[R] = 0;
+        return;
+    }
+    const int i = order[k];
+    removed[2 * k] = log_pair[2 * i];
+    removed[2 * k + 1] = log_pair[2 * i + 1];
+    cnt[k] = log_meta[2 * i];
+}
+
+__global__ void log_vars_kernel(int R, const int32_t *order, const int32_t *log_meta, const int32_t *log_vars,
+                                const int32_t *off, int32_t *vars) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= R) return;
+    const int i = order[k];
+    const int dd = log_meta[2 * i], vo = log_meta[2 * i + 1];
+    for (int t = 0; t < dd; ++t) vars[off[k] + t] = log_vars[vo + t];
+}
+
 // ---- device-driven wave loop (one CUDA graph per level: a WHILE conditional node whose body
 // is one wave; the wave's tail kernel decides whether another wave runs)
 struct WaveCtl {
@@ -662,7 +701,7 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     int occ = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ci_warp_kernel<kWarpInts, 2>, kThreads, kSmemBytes));
     e->ci_blocks = e->num_sms * std::max(1, occ);
-    if (const char *w = getenv("FPGM_WARP_SLICE")) e->warp_small = atoi(w) == kWarpIntsSmall;
+    if (const char *w = getenv("FPGM_WARP_SLICE")) e->warp_small = atoi(w) != kWarpInts;
     int occ_small = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_small, ci_warp_kernel<kWarpIntsSmall, 3>, kThreads,
                                                      kWarps * kWarpIntsSmall * 4));
@@ -720,7 +759,8 @@ extern "C" int fpgm_engine_destroy(fpgm_engine *e) {
                       &e->tests_buf, &e->detail_buf, &e->item_vars, &e->lists, &e->band,
                       &e->phase_timers, &e->var_off, &e->var_S, &e->var_lo, &e->var_hi, &e->mle_counts,
                       &e->mle_pot, &e->mle_meta, &e->wide, &e->wide_items, &e->tune, &e->wave_ctl,
-                      &e->tune_obs};
+                      &e->tune_obs, &e->res_adj_d, &e->res_key, &e->res_idx, &e->res_removed_d, &e->res_cnt,
+                      &e->res_vars_d};
     for (DevBuf *b : bufs) b->release();
     gram_destroy(e->gram);
     if (e->ev0) cudaEventDestroy(e->ev0);
@@ -1038,7 +1078,7 @@ int run_waves_graph(fpgm_engine *e, double alpha, int d, int64_t n_active, fpgm_
         return FPGM_OK;
     };
     int rc = build();
-    e->graph_build_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    st->graph_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (rc == FPGM_OK) {
         const cudaError_t le = cudaGraphLaunch(exec, e->stream);
         if (le != cudaSuccess) rc = set_error(FPGM_ERR_CUDA, "cudaGraphLaunch: %s", cudaGetErrorString(le));
@@ -1375,36 +1415,64 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
             }
         }
     }
-    // result: adjacency bitset + removal log
-    std::vector<uint32_t> hb((size_t)n * W);
-    std::vector<int32_t> lp((size_t)log_count * 2 + 2), lm((size_t)log_count * 2 + 2), lv((size_t)var_count + 1);
-    CK(cudaMemcpyAsync(hb.data(), e->bits.p, hb.size() * 4, cudaMemcpyDeviceToHost, e->stream));
-    if (log_count) {
-        CK(cudaMemcpyAsync(lp.data(), e->log_pair.p, (size_t)log_count * 8, cudaMemcpyDeviceToHost, e->stream));
-        CK(cudaMemcpyAsync(lm.data(), e->log_meta.p, (size_t)log_count * 8, cudaMemcpyDeviceToHost, e->stream));
+    // result, assembled on the device: the 0/1 adjacency expanded from the bitset, and the
+    // removal log sorted by pair (a < b, ascending) with each separating set gathered in that
+    // order; the host only copies it back
+    RET(e->res_adj_d.ensure((size_t)n * n + 16));
+    expand_adj_kernel<<<blocks_for((int64_t)n * n, 256), 256, 0, e->stream>>>(e->bits.as<uint32_t>(), n, W,
+                                                                             e->res_adj_d.as<uint8_t>());
+    CK(cudaGetLastError());
+    st->kernel_launches += 1;
+    const int R = (int)log_count;
+    if (R > 0) {
+        RET(e->res_key.ensure((size_t)R * 4 * 2 + 16));
+        RET(e->res_idx.ensure((size_t)R * 4 * 2 + 16));
+        RET(e->res_removed_d.ensure((size_t)R * 8 + 16));
+        RET(e->res_cnt.ensure((size_t)(R + 1) * 4 * 2 + 16));
+        RET(e->res_vars_d.ensure((size_t)var_count * 4 + 16));
+        uint32_t *k0 = e->res_key.as<uint32_t>(), *k1 = k0 + R;
+        int32_t *i0 = e->res_idx.as<int32_t>(), *i1 = i0 + R;
+        int32_t *cnt = e->res_cnt.as<int32_t>(), *off = cnt + R + 1;
+        log_keys_kernel<<<blocks_for(R, 256), 256, 0, e->stream>>>(R, n, e->log_pair.as<int32_t>(), k0, i0);
+        CK(cudaGetLastError());
+        int bits = 1;
+        while (bits < 32 && ((uint64_t)1 << bits) < (uint64_t)n * n) ++bits;
+        size_t sb = 0;
+        CK(cub::DeviceRadixSort::SortPairs(nullptr, sb, k0, k1, i0, i1, R, 0, bits, e->stream));
+        size_t sb2 = 0;
+        CK(cub::DeviceScan::ExclusiveSum(nullptr, sb2, cnt, off, R + 1, e->stream));
+        RET(e->scan_tmp.ensure(std::max(sb, sb2) + 16));
+        sb = e->scan_tmp.bytes;
+        CK(cub::DeviceRadixSort::SortPairs(e->scan_tmp.p, sb, k0, k1, i0, i1, R, 0, bits, e->stream));
+        log_gather_kernel<<<blocks_for(R + 1, 256), 256, 0, e->stream>>>(R, i1, e->log_pair.as<int32_t>(),
+                                                                     e->log_meta.as<int32_t>(),
+                                                                     e->res_removed_d.as<int32_t>(), cnt);
+        CK(cudaGetLastError());
+        sb2 = e->scan_tmp.bytes;
+        CK(cub::DeviceScan::ExclusiveSum(e->scan_tmp.p, sb2, cnt, off, R + 1, e->stream));
+        if (var_count > 0) {
+            log_vars_kernel<<<blocks_for(R, 256), 256, 0, e->stream>>>(R, i1, e->log_meta.as<int32_t>(),
+                                                                       e->log_vars.as<int32_t>(), off,
+                                                                       e->res_vars_d.as<int32_t>());
+            CK(cudaGetLastError());
+        }
+        st->kernel_launches += 3;
     }
-    if (var_count) CK(cudaMemcpyAsync(lv.data(), e->log_vars.p, (size_t)var_count * 4, cudaMemcpyDeviceToHost, e->stream));
+    e->res_adj.resize((size_t)n * n);
+    e->res_removed.resize((size_t)R * 2);
+    e->res_off.assign((size_t)R + 1, 0);
+    e->res_vars.resize((size_t)var_count);
+    CK(cudaMemcpyAsync(e->res_adj.data(), e->res_adj_d.p, (size_t)n * n, cudaMemcpyDeviceToHost, e->stream));
+    if (R > 0) {
+        CK(cudaMemcpyAsync(e->res_removed.data(), e->res_removed_d.p, (size_t)R * 8, cudaMemcpyDeviceToHost,
+                           e->stream));
+        CK(cudaMemcpyAsync(e->res_off.data(), e->res_cnt.as<int32_t>() + R + 1, (size_t)(R + 1) * 4,
+                           cudaMemcpyDeviceToHost, e->stream));
+        if (var_count)
+            CK(cudaMemcpyAsync(e->res_vars.data(), e->res_vars_d.p, (size_t)var_count * 4, cudaMemcpyDeviceToHost,
+                               e->stream));
+    }
     CK(cudaStreamSynchronize(e->stream));
-    e->res_adj.assign((size_t)n * n, 0);
-    for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) e->res_adj[(size_t)i * n + j] = (hb[(size_t)i * W + (j >> 5)] >> (j & 31)) & 1u;
-    std::vector<int64_t> order((size_t)log_count);
-    for (int64_t i = 0; i < log_count; ++i) order[i] = i;
-    std::sort(order.begin(), order.end(), [&](int64_t p, int64_t q) {
-        return lp[2 * p] != lp[2 * q] ? lp[2 * p] < lp[2 * q] : lp[2 * p + 1] < lp[2 * q + 1];
-    });
-    e->res_removed.resize((size_t)log_count * 2);
-    e->res_off.assign((size_t)log_count + 1, 0);
-    e->res_vars.clear();
-    e->res_vars.reserve((size_t)var_count);
-    for (int64_t k = 0; k < log_count; ++k) {
-        int64_t i = order[k];
-        e->res_removed[2 * k] = lp[2 * i];
-        e->res_removed[2 * k + 1] = lp[2 * i + 1];
-        const int dd = lm[2 * i], vo = lm[2 * i + 1];
-        for (int t = 0; t < dd; ++t) e->res_vars.push_back(lv[(size_t)vo + t]);
-        e->res_off[k + 1] = (int32_t)e->res_vars.size();
-    }
     return FPGM_OK;
 }
 

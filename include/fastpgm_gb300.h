@@ -98,6 +98,7 @@ typedef struct {
     int32_t tune_buckets;        /* online autotuner: (samples, |Z|, cells/samples) buckets timed both ways */
     int32_t tune_partition;      /* ... of which the partition kernel is the faster tier-2 method */
     int64_t tune_timed;          /* tier-2 tests timed by the autotuner since the engine was created */
+    double graph_ms;             /* host time capturing and instantiating the levels' CUDA graphs */
 } fpgm_pc_stats;
 
 typedef struct {

@@ -351,10 +351,11 @@ def test_online_autotuner_times_both_tier2_methods(monkeypatch):
 
 
 @pytest.mark.parametrize("name", ["c1", "c2"])
-def test_small_warp_slices_match_reference(monkeypatch, tmp_path, name):
-    """The warp tier with 8 KB slices (FPGM_WARP_SLICE=2048: 3 CTAs per SM, tables over 2,016
-    ints to the CTA tier) gives the reference's separating sets and CPDAG."""
-    monkeypatch.setenv("FPGM_WARP_SLICE", "2048")
+def test_large_warp_slices_match_reference(monkeypatch, tmp_path, name):
+    """The warp tier with 12 KB slices (FPGM_WARP_SLICE=3072: 2 CTAs per SM, tables up to
+    3,040 ints; the default is 8 KB slices and 3 CTAs per SM) gives the reference's
+    separating sets and CPDAG."""
+    monkeypatch.setenv("FPGM_WARP_SLICE", "3072")
     raw, depth, _ = F.make_config(name)
     with F.Engine(0) as e:
         e.upload(raw)
