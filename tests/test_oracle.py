@@ -190,6 +190,8 @@ def test_full_size_fixtures_describe_this_hosts_data(name):
         data = [raw]
     assert depth == fx["depth"] and len(data) == len(fx["jobs"])
     for raw, job in zip(data, fx["jobs"]):
+        if job is None:
+            continue
         assert O.sha256(raw) == job["sha256"]
         assert list(raw.shape) == job["shape"]
         assert len(job["tests"]) == len(job["edges_after"]) >= 1
