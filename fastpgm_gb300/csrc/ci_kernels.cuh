@@ -107,6 +107,7 @@ struct WaveArgs {
     const int8_t *tune;
     unsigned long long *tune_obs;  // 8 per bucket: n_part, ns_part, n_hash, ns_hash, decisions
     int32_t warp_ints;             // ints of the warp tier's per-warp slice (its table limit)
+    int32_t dense_rows;            // compact kernel's dense strata table: a thread per stratum (else lane groups)
     int64_t part_min_samples;
 };
 
@@ -469,6 +470,7 @@ constexpr int kZIdsOff = kZCap64 * 8;
 constexpr int kZCurOff = ((kZStrata + 1) * 4 + 15) / 16 * 16;
 constexpr int kZTabOff = (kZCurOff + (kZStrata + 1) * 4 + 15) / 16 * 16;
 static_assert(kZIdsOff + kZCap32 * 2 <= kSmemBytes, "shared hash ids");
+static_assert(3 * 32 * kThreads * 4 <= kSmemBytes, "dense-table scoring columns");
 constexpr int kSparseWarpTab = (kSmemBytes - kZTabOff) / 4 / kWarps;  // ints per warp
 constexpr int kLaneStratum = 8;   // strata of up to this many samples: one lane each
 constexpr int kRegStratum = 64;   // larger strata up to this size keep their codes in registers
@@ -841,6 +843,53 @@ __device__ inline Partial score_dense_groups(const int *T, int n_obs, int dx, in
                     acc.hash += cell_mix((gzk[k] * (uint64_t)dx + x) * (uint64_t)dy + y, (uint32_t)O[u]);
             }
         }
+    }
+    ta.into(acc);
+    return acc;
+}
+
+// Dense strata x cells table T[k * dxy + x * dy + y] (k = stratum id), at most 32 cells per
+// stratum, one thread per stratum: its counts are loaded together (one round trip) into a
+// column of shared scratch, the x and y margins summed into two more, then the terms. Each
+// thread owns column threadIdx.x of smem (96 ints at stride kThreads: a warp's threads hit
+// 32 distinct banks). Every thread of the CTA calls it; returns the thread's share.
+template <bool kFp64>
+__device__ inline Partial score_dense_rows(const int *T, int n_obs, int dx, int dy, const uint64_t *gzk,
+                                           bool want_hash, int *smem) {
+    const int dxy = dx * dy;
+    int *so = smem + threadIdx.x, *mx = so + 32 * kThreads, *my = mx + 32 * kThreads;
+    Partial acc{0, 0.0, 0.0, 0.0, 0ull};
+    TermAcc<kFp64> ta;
+    for (int k = threadIdx.x; k < n_obs; k += kThreads) {
+        const int *row = T + (int64_t)k * dxy;
+        int o[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) o[c] = c < dxy ? __ldcg(row + c) : 0;
+#pragma unroll
+        for (int c = 0; c < 32; ++c)
+            if (c < dxy) so[c * kThreads] = o[c];
+        for (int i = 0; i < dx; ++i) mx[i * kThreads] = 0;
+        for (int j = 0; j < dy; ++j) my[j * kThreads] = 0;
+        int m = 0;
+        for (int i = 0, c = 0; i < dx; ++i)
+            for (int j = 0; j < dy; ++j, ++c) {
+                const int v = so[c * kThreads];
+                mx[i * kThreads] += v;
+                my[j * kThreads] += v;
+                m += v;
+            }
+        int r = 0, q = 0;
+        for (int i = 0; i < dx; ++i) r += mx[i * kThreads] > 0;
+        for (int j = 0; j < dy; ++j) q += my[j * kThreads] > 0;
+        acc.df += (long long)(max(r, 1) - 1) * (max(q, 1) - 1);
+        for (int i = 0, c = 0; i < dx; ++i)
+            for (int j = 0; j < dy; ++j, ++c) {
+                const int O = so[c * kThreads];
+                if (O > 0) {
+                    ta.add(O, mx[i * kThreads], my[j * kThreads], m);
+                    if (want_hash) acc.hash += cell_mix((gzk[k] * (uint64_t)dx + i) * (uint64_t)dy + j, (uint32_t)O);
+                }
+            }
     }
     ta.into(acc);
     return acc;
@@ -1483,7 +1532,10 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             }
             __syncthreads();
             FPGM_PHASE(7);
-            acc = score_dense_groups<false>(gtab, n_obs, dx, dy, zk, a.want_hash != 0);
+            // the hash keys and ids are dead: their 96 KB hold the per-thread scoring columns
+            acc = a.dense_rows ? score_dense_rows<false>(gtab, n_obs, dx, dy, zk, a.want_hash != 0,
+                                                         reinterpret_cast<int *>(smem_raw))
+                               : score_dense_groups<false>(gtab, n_obs, dx, dy, zk, a.want_hash != 0);
             FPGM_PHASE(8);
         } else {
             // 2. counting sort of the samples by stratum
@@ -1557,7 +1609,9 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
         decide_record(a, item, r, (int64_t)n_obs * dxy, 2, s_flag, scratch, [&]() {
             Partial q;
             if (dense) {
-                q = score_dense_groups<true>(gtab, n_obs, dx, dy, nullptr, false);
+                q = a.dense_rows ? score_dense_rows<true>(gtab, n_obs, dx, dy, nullptr, false,
+                                                          reinterpret_cast<int *>(smem_raw))
+                                 : score_dense_groups<true>(gtab, n_obs, dx, dy, nullptr, false);
             } else {
                 q = score_small_strata<true>(cnt, gord, n_obs, dx, dy, big, nullptr, nullptr, false, false);
                 q = score_big_strata<true>(q, cnt, gord, big, n_big, dx, dy, wt, nullptr, false);

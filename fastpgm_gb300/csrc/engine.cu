@@ -173,6 +173,7 @@ struct fpgm_engine {
     int64_t slot_bytes = 0, slot_S = 0;  // slot_S: the sample count the slots' layout was made for
     bool wave_log = false;               // FPGM_WAVE_LOG: one stderr line per wave (tier sizes, kernel times)
     bool warp_small = true;              // 8 KB warp-tier slices, 3 CTAs per SM (FPGM_WARP_SLICE=3072: 12 KB, 2)
+    bool dense_rows = true;              // FPGM_DENSE_ROWS=0: lane groups score the dense strata table
     int warp_blocks_small = 0;
     // level 0 on the tensor cores (FPGM_GRAM=0 keeps it on the counting kernels)
     GramLevel0 *gram = nullptr;
@@ -702,6 +703,7 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ci_warp_kernel<kWarpInts, 2>, kThreads, kSmemBytes));
     e->ci_blocks = e->num_sms * std::max(1, occ);
     if (const char *w = getenv("FPGM_WARP_SLICE")) e->warp_small = atoi(w) != kWarpInts;
+    if (const char *w = getenv("FPGM_DENSE_ROWS")) e->dense_rows = atoi(w) != 0;
     int occ_small = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_small, ci_warp_kernel<kWarpIntsSmall, 3>, kThreads,
                                                      kWarps * kWarpIntsSmall * 4));
@@ -965,6 +967,7 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t ite
     }
     a.part_max_log = e->part_max_log;
     a.warp_ints = e->warp_small ? kWarpIntsSmall : kWarpInts;
+    a.dense_rows = e->dense_rows;
     return FPGM_OK;
 }
 

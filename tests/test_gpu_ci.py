@@ -442,3 +442,28 @@ def test_allocation_failure_is_an_error_status():
     lines = out.stdout.split("\n")
     assert "CODE %d True" % F.FPGM_ERR_OOM in lines, out.stdout
     assert "DEPTH1 1" in lines and "BATCH True" in lines and "CLOSED" in lines, out.stdout
+
+
+def test_dense_strata_table_scorers_agree(monkeypatch):
+    """The compact kernel's dense strata x cells table scored one thread per stratum (the
+    default) and by lane groups with shuffles (FPGM_DENSE_ROWS=0): identical counts, df and
+    decisions, G^2 within the FP32 tolerance, both equal to the oracle (cards 4-5, |Z| = 5:
+    joint tables beyond shared memory, at most 25 cells per stratum: the dense path)."""
+    raw, _, _ = F.generate(n_nodes=12, n_samples=20000, seed=121, n_edges=16, max_indegree=3, card=(4, 5))
+    cols, cd = O.relabel(raw)
+    rng = np.random.default_rng(122)
+    tests = random_tests(rng, 12, 5, 24)
+    exp = O.ci_tests(cols, cd, tests, 5, threads=8)
+    got = {}
+    for rows in ("1", "0"):
+        e = _engine_with(monkeypatch, FPGM_DENSE_ROWS=rows, FPGM_WIDE="0", FPGM_TUNE_TABLE="off")
+        try:
+            e.upload(raw)
+            got[rows] = e.ci_test_batch(tests, 5, want_hash=True)
+        finally:
+            e.close()
+    assert sum(g.path == 2 for g in got["1"]) >= 12
+    for a, b, o in zip(got["1"], got["0"], exp):
+        assert a.cell_hash == b.cell_hash and a.df == b.df and a.independent == b.independent
+        check(a, o, exact_p=a.rechecked == 1)
+        check(b, o, exact_p=b.rechecked == 1)
