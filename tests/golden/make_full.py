@@ -18,8 +18,9 @@ and, for c5, the level totals over all jobs (what a multi-dataset skeleton repor
 
 Run:  python tests/golden/make_full.py [c3] [c4] [c5] [--workers N] [--partial]   (default: all
 three; c5 takes longest: its 64 jobs run N at a time in separate processes, each job's digest
-cached under tests/golden/.full_cache/; --partial writes c5 from the cached jobs alone, a
-missing job as null, which the GPU test then skips)
+cached under tests/golden/.full_cache/; jobs already in full_c5.json are kept and only the
+missing ones run; --partial writes c5 from the fixture and the cached jobs alone, a missing
+job as null, which the GPU test then skips)
 """
 import json
 import os
@@ -80,16 +81,22 @@ def main():
             depth = specs[0]["depth"]
             # largest first, so the long jobs start at once
             order = sorted(range(len(specs)), key=lambda j: -specs[j]["n_samples"] * specs[j]["n_nodes"])
-            if "--partial" in sys.argv:  # the cached jobs only (a missing job stays null)
-                done = {}
-                for j in order:
-                    path = os.path.join(CACHE, "c5_job%02d.json" % j)
-                    if os.path.exists(path):
-                        with open(path) as f:
-                            done[j] = json.load(f)
-            else:
-                with mp.get_context("spawn").Pool(workers) as pool:
-                    done = dict(zip(order, pool.map(_c5_job, [(j, threads) for j in order], chunksize=1)))
+            done = {}
+            fixture = os.path.join(HERE, "full_c5.json")
+            if os.path.exists(fixture):  # jobs already in the fixture are kept
+                with open(fixture) as f:
+                    old = json.load(f)
+                if len(old.get("jobs", [])) == len(specs):
+                    done = {j: d for j, d in enumerate(old["jobs"]) if d is not None}
+            for j in order:
+                path = os.path.join(CACHE, "c5_job%02d.json" % j)
+                if j not in done and os.path.exists(path):
+                    with open(path) as f:
+                        done[j] = json.load(f)
+            todo = [j for j in order if j not in done]
+            if todo and "--partial" not in sys.argv:  # --partial: a missing job stays null
+                with mp.get_context("spawn").Pool(min(workers, len(todo))) as pool:
+                    done.update(zip(todo, pool.map(_c5_job, [(j, threads) for j in todo], chunksize=1)))
             jobs = [done.get(j) for j in range(len(specs))]
             have = [d for d in jobs if d is not None]
             L = max(len(d["tests"]) for d in have)
