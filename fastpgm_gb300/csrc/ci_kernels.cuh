@@ -52,6 +52,7 @@ struct WideTest {
     unsigned long long hash;
     int32_t pcnt[kPartMax];      // records per partition
     int32_t poff[kPartMax + 1];  // first record of each partition (runs padded to 8 records)
+    int32_t sp[kPartMax + 1];    // super-partitions (queue items): partitions sp[i] .. sp[i + 1] - 1
 };
 
 struct WaveArgs {
@@ -106,6 +107,10 @@ struct WaveArgs {
     // part_min_samples decides (samples >= it: partitions).
     const int8_t *tune;
     unsigned long long *tune_obs;  // 8 per bucket: n_part, ns_part, n_hash, ns_hash, decisions
+    // Shared-hash overflow record per autotuner bucket (8 each: tests that overflowed, tests
+    // that fit, sum of strata / samples * 2^16 and its count, tests seen); null: every tier-2
+    // test tries the shared hash first.
+    unsigned long long *ovf;
     int32_t warp_ints;             // ints of the warp tier's per-warp slice (its table limit)
     int32_t dense_rows;            // compact kernel's dense strata table: a thread per stratum (else lane groups)
     int64_t part_min_samples;
@@ -158,6 +163,26 @@ __device__ inline bool tier2_pick_partitions(const WaveArgs &a, int64_t S, int d
     }
     if (!part) *bucket = b;
     return part;
+}
+
+// A bucket whose tests have (almost) all overflowed the compact kernel's shared hash skips
+// that attempt: est gets the strata expected from the bucket's observed strata per sample
+// (raised by a third, so it errs high); one test in 64 still tries, to keep the record fresh.
+constexpr unsigned long long kOvfMin = 16;  // overflowed tests before any is skipped
+__device__ inline bool ovf_skip(const WaveArgs &a, int b, int64_t S, double *est) {
+    if (!a.ovf || b < 0) return false;
+    unsigned long long *o = a.ovf + 8 * b;
+    const unsigned long long over = *(volatile unsigned long long *)&o[0], fit = *(volatile unsigned long long *)&o[1];
+    const unsigned long long rs = *(volatile unsigned long long *)&o[2], rn = *(volatile unsigned long long *)&o[3];
+    if (over < kOvfMin || over <= 8 * fit || rn < 4) return false;
+    if ((atomicAdd(&o[4], 1ull) & 63ull) == 0) return false;
+    *est = fmin((double)S, 1.34 * ((double)rs / 65536.0 / (double)rn) * (double)S);
+    return true;
+}
+__device__ inline void ovf_strata(const WaveArgs &a, int b, int64_t S, int n_obs) {
+    if (!a.ovf || b < 0 || S <= 0) return;
+    atomicAdd(&a.ovf[8 * b + 2], (unsigned long long)(((double)n_obs * 65536.0) / (double)S));
+    atomicAdd(&a.ovf[8 * b + 3], 1ull);
 }
 
 __device__ inline int upper_bound_i32(const int32_t *a, int n, int v) {
@@ -676,12 +701,14 @@ __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gor
     return acc;
 }
 
-// Strata listed in big[]: one warp each, dense x,y table read back with atomicExch.
+// Strata listed in big[] (or, when big is null, strata k_first .. k_first + n_big - 1): one
+// warp each, dense x,y table read back with atomicExch.
 // Strata of up to kRegStratum samples keep their packed (x << 8) | y codes in registers,
 // and the next stratum's codes are loaded while the current one is scored.
 template <bool kFp64>
 __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const uint16_t *gord, const int *big, int n_big,
-                                           int dx, int dy, int *wt, const uint64_t *gzk, bool want_hash) {
+                                           int dx, int dy, int *wt, const uint64_t *gzk, bool want_hash,
+                                           int k_first = 0) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int dxy = dx * dy;
@@ -691,7 +718,7 @@ __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const ui
     auto fetch = [&](int bb, int &kk, int &mm, int &oo, int &q0, int &q1) {
         q0 = q1 = -1;
         if (bb >= n_big) return;
-        kk = big[bb];
+        kk = big ? big[bb] : k_first + bb;
         oo = cnt[kk];
         mm = cnt[kk + 1] - oo;
         if (mm <= kRegStratum) {
@@ -1006,23 +1033,45 @@ __device__ __forceinline__ void load8(K (&z)[8], const K *src) {
 
 // Partition histogram, offsets (every run padded to a multiple of 8 records) and the
 // record pass.  s_poff[P] = records written, padding included.
+// Pass 1 computes every stratum code once, stores it to zbuf (coalesced; S codes) and counts
+// the partitions.  Pass 2 takes the codes back in chunks of kThreads x 16 samples, sorts a
+// chunk's records by partition in shared memory (smem, dead at this point) and copies each
+// partition's run out to consecutive records, so the global stores are coalesced.
+constexpr int kScatterChunk = kThreads * 16;
 template <class K>
-__device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint32_t *dim, int d, int64_t S, int lp, K *rec_z,
-                             uint16_t *rec_xy, int *s_pcnt, int *s_poff, int *s_pcur) {
+__device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint32_t *dim, int d, int64_t S, int lp,
+                                          K *rec_z, uint16_t *rec_xy, int *s_pcnt, int *s_poff, int *s_pcur, K *zbuf,
+                                          unsigned char *smem) {
     const int tid = threadIdx.x, P = 1 << lp;
     const int64_t nvec = S >> 4;
     const uint8_t *colx = col[d], *coly = col[d + 1];
+    K *cz = reinterpret_cast<K *>(smem);
+    uint16_t *cxy = reinterpret_cast<uint16_t *>(smem + kScatterChunk * sizeof(K));
+    uint8_t *cp = reinterpret_cast<uint8_t *>(smem + kScatterChunk * (sizeof(K) + 2));
+    int *lcnt = reinterpret_cast<int *>(smem + kScatterChunk * (sizeof(K) + 3));
+    int *lstart = lcnt + kPartMax, *gbase = lstart + kPartMax;
     for (int i = tid; i < P; i += kThreads) s_pcnt[i] = 0;
     __syncthreads();
     for (int64_t v = tid; v < nvec; v += kThreads) {
         K z[16];
         zcodes16(z, col, dim, d, v);
+        uint4 *dst = reinterpret_cast<uint4 *>(zbuf + 16 * v);
+        if constexpr (sizeof(K) == 4) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) dst[q] = make_uint4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                dst[q] = make_uint4((uint32_t)z[2 * q], (uint32_t)(z[2 * q] >> 32), (uint32_t)z[2 * q + 1],
+                                    (uint32_t)(z[2 * q + 1] >> 32));
+        }
 #pragma unroll
         for (int b = 0; b < 16; ++b) atomicAdd(&s_pcnt[part_of(z[b], lp)], 1);
     }
     for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
         K z = 0;
         for (int j = 0; j < d; ++j) z = z * (K)dim[j] + col[j][s];
+        zbuf[s] = z;
         atomicAdd(&s_pcnt[part_of(z, lp)], 1);
     }
     __syncthreads();
@@ -1051,29 +1100,99 @@ __device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint3
         if (tid == 31) s_poff[P] = incl;
     }
     __syncthreads();
-    for (int64_t v = tid; v < nvec; v += kThreads) {
+    const int64_t nchunks = (nvec + kThreads - 1) / kThreads;
+    for (int64_t c = 0; c < nchunks; ++c) {
+        const int64_t v = c * kThreads + tid;
+        const bool have = v < nvec;
+        for (int i = tid; i < P; i += kThreads) lcnt[i] = 0;
+        __syncthreads();
         K z[16];
-        zcodes16(z, col, dim, d, v);
-        const uint4 wx = __ldg(reinterpret_cast<const uint4 *>(colx) + v);
-        const uint4 wy = __ldg(reinterpret_cast<const uint4 *>(coly) + v);
-        const uint32_t xx[4] = {wx.x, wx.y, wx.z, wx.w}, yy[4] = {wy.x, wy.y, wy.z, wy.w};
+        int rk[16];
+        uint32_t xx[4] = {0u, 0u, 0u, 0u}, yy[4] = {0u, 0u, 0u, 0u};
+        if (have) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(zbuf + 16 * v);
+            if constexpr (sizeof(K) == 4) {
 #pragma unroll
-        for (int b = 0; b < 16; ++b) {
-            const int pos = atomicAdd(&s_pcur[part_of(z[b], lp)], 1);
-            const int sh = 8 * (b & 3);
-            rec_z[pos] = z[b];
-            rec_xy[pos] = (uint16_t)((((xx[b >> 2] >> sh) & 0xffu) << 8) | ((yy[b >> 2] >> sh) & 0xffu));
+                for (int q = 0; q < 4; ++q) {
+                    const uint4 w = __ldcg(src + q);
+                    z[4 * q] = w.x;
+                    z[4 * q + 1] = w.y;
+                    z[4 * q + 2] = w.z;
+                    z[4 * q + 3] = w.w;
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const uint4 w = __ldcg(src + q);
+                    z[2 * q] = (K)w.x | ((K)w.y << 32);
+                    z[2 * q + 1] = (K)w.z | ((K)w.w << 32);
+                }
+            }
+            const uint4 wx = __ldg(reinterpret_cast<const uint4 *>(colx) + v);
+            const uint4 wy = __ldg(reinterpret_cast<const uint4 *>(coly) + v);
+            xx[0] = wx.x; xx[1] = wx.y; xx[2] = wx.z; xx[3] = wx.w;
+            yy[0] = wy.x; yy[1] = wy.y; yy[2] = wy.z; yy[3] = wy.w;
+#pragma unroll
+            for (int b = 0; b < 16; ++b) rk[b] = atomicAdd(&lcnt[part_of(z[b], lp)], 1);
         }
+        __syncthreads();
+        if (tid < 32) {  // chunk offsets per partition, and each run's place in the records
+            const int per = (P + 31) / 32;
+            int sum = 0;
+            for (int i = 0; i < per; ++i) {
+                const int p = tid * per + i;
+                if (p < P) sum += lcnt[p];
+            }
+            int incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (tid >= o) incl += t;
+            }
+            int run = incl - sum;
+            for (int i = 0; i < per; ++i) {
+                const int p = tid * per + i;
+                if (p < P) {
+                    lstart[p] = run;
+                    gbase[p] = lcnt[p] ? atomicAdd(&s_pcur[p], lcnt[p]) : 0;
+                    run += lcnt[p];
+                }
+            }
+        }
+        __syncthreads();
+        if (have) {
+#pragma unroll
+            for (int b = 0; b < 16; ++b) {
+                const int p = part_of(z[b], lp), pos = lstart[p] + rk[b], sh = 8 * (b & 3);
+                cz[pos] = z[b];
+                cxy[pos] = (uint16_t)((((xx[b >> 2] >> sh) & 0xffu) << 8) | ((yy[b >> 2] >> sh) & 0xffu));
+                cp[pos] = (uint8_t)p;
+            }
+        }
+        __syncthreads();
+        const int64_t left = 16 * (nvec - c * kThreads);
+        const int n_in = left < kScatterChunk ? (int)left : kScatterChunk;
+        for (int i = tid; i < n_in; i += kThreads) {
+            const int p = cp[i];
+            const int g = gbase[p] + (i - lstart[p]);
+            rec_z[g] = cz[i];
+            rec_xy[g] = cxy[i];
+        }
+        __syncthreads();
     }
     for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
-        K z = 0;
-        for (int j = 0; j < d; ++j) z = z * (K)dim[j] + col[j][s];
+        const K z = zbuf[s];
         const int pos = atomicAdd(&s_pcur[part_of(z, lp)], 1);
         rec_z[pos] = z;
         rec_xy[pos] = (uint16_t)((colx[s] << 8) | coly[s]);
     }
+    // padding records carry the empty key (never a stratum code), so a run of partitions
+    // can be read as one
+    for (int p = tid; p < P; p += kThreads)
+        for (int i = s_poff[p] + s_pcnt[p]; i < s_poff[p + 1]; ++i) rec_z[i] = (K)kEmptyKey;
     __syncthreads();
 }
+static_assert(kScatterChunk * (8 + 3) + 3 * kPartMax * 4 <= kSmemBytes, "scatter chunk in shared memory");
 
 // Counts and scores one partition (n records from rec_z/rec_xy + base) in shared memory;
 // returns this thread's share of the statistic.  *s_over is set when the partition's codes
@@ -1217,24 +1336,401 @@ __device__ __forceinline__ void partial_add(Partial &a, const Partial &b) {
     a.hash += b.hash;
 }
 
-// Counts and scores every partition of a test in shared memory, one after another; returns
-// this thread's share of the statistic (see part_partition; stops at the first overflow).
-// s_pcnt / s_poff: records per partition and each partition's first record.
+// ---------------------------------------------------------------- staged partitions
+// A run of consecutive partitions ("super-partition", at most StagePlan<K>::rec records,
+// padding included) is copied from the records into shared memory first, so the passes over
+// it never wait on global memory:
+//   insert  codes hashed to slots as in part_partition; the slot replaces the code in place;
+//           samples per slot summed with one atomic per group of equal slots in a warp
+//           (match.any), new strata appended to occ[] with one atomic per warp;
+//   rank    strata ranked by size (2 .. 8 samples, larger; single-sample strata, which add
+//           neither a degree of freedom nor a G^2 term, are left out unless the cell
+//           fingerprint is wanted), ranks handed out with one atomic per warp and size;
+//   place   (x << 8) | y codes sorted by stratum over the dead hash keys;
+//   score   one lane per stratum of at most kLaneStratum samples, one warp per larger one
+//           (per-warp x,y tables over the dead records).
+// Padding records (a run is padded to 8 records) carry the empty key and are skipped.
+template <class K>
+struct StagePlan {
+    static constexpr int cap = PartPlan<K>::cap, lcap = PartPlan<K>::lcap, lim = PartPlan<K>::lim;
+    static constexpr int a_off = cap * (int)sizeof(K);
+    static constexpr int occ_off = a_off + cap * 4;
+    static constexpr int e_off = occ_off + lim * 4;
+    static constexpr int rec_off = (e_off + (lim + 1) * 4 + 15) / 16 * 16;
+    static constexpr int rec = (kSmemBytes - rec_off) / ((int)sizeof(K) + 2) / 8 * 8;  // records at most
+    static constexpr int xy_off = rec_off + rec * (int)sizeof(K);
+    static constexpr int wtab = (rec * ((int)sizeof(K) + 2)) / 4 / kWarps;  // ints per warp over the records
+};
+static_assert(StagePlan<uint32_t>::rec * 2 <= StagePlan<uint32_t>::a_off, "sorted codes over the u32 keys");
+static_assert(StagePlan<uint64_t>::rec * 2 <= StagePlan<uint64_t>::a_off, "sorted codes over the u64 keys");
+static_assert(StagePlan<uint32_t>::xy_off + StagePlan<uint32_t>::rec * 2 <= kSmemBytes, "u32 stage plan");
+static_assert(StagePlan<uint64_t>::xy_off + StagePlan<uint64_t>::rec * 2 <= kSmemBytes, "u64 stage plan");
+static_assert(StagePlan<uint32_t>::rec >= 4096 && StagePlan<uint64_t>::rec >= 4096, "stage plan records");
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Eight consecutive staged codes from shared memory (vector loads).
+template <class K>
+__device__ __forceinline__ void sload8(K (&z)[8], const K *src) {
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    if constexpr (sizeof(K) == 4) {
+        const uint4 w0 = s4[0], w1 = s4[1];
+        z[0] = w0.x; z[1] = w0.y; z[2] = w0.z; z[3] = w0.w;
+        z[4] = w1.x; z[5] = w1.y; z[6] = w1.z; z[7] = w1.w;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const uint4 w = s4[i];
+            z[2 * i] = (K)w.x | ((K)w.y << 32);
+            z[2 * i + 1] = (K)w.z | ((K)w.w << 32);
+        }
+    }
+}
+
+// The slots of eight consecutive records replace their codes in place (low word of each
+// code's place), and are read back the same way.
+template <class K>
+__device__ __forceinline__ void slot_store8(K *dst, const int (&sl)[8]) {
+    uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+    if constexpr (sizeof(K) == 4) {
+        d4[0] = make_uint4(sl[0], sl[1], sl[2], sl[3]);
+        d4[1] = make_uint4(sl[4], sl[5], sl[6], sl[7]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) d4[i] = make_uint4(sl[2 * i], 0u, sl[2 * i + 1], 0u);
+    }
+}
+template <class K>
+__device__ __forceinline__ void slot_load8(int (&sl)[8], const K *src) {
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    if constexpr (sizeof(K) == 4) {
+        const uint4 w0 = s4[0], w1 = s4[1];
+        sl[0] = w0.x; sl[1] = w0.y; sl[2] = w0.z; sl[3] = w0.w;
+        sl[4] = w1.x; sl[5] = w1.y; sl[6] = w1.z; sl[7] = w1.w;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const uint4 w = s4[i];
+            sl[2 * i] = (int)w.x;
+            sl[2 * i + 1] = (int)w.z;
+        }
+    }
+}
+
+// Counts and scores n records (a multiple of 8, padding included) from base in shared
+// memory; n <= StagePlan<K>::rec.  As part_partition: *s_over is set when the strata
+// overflow the table (first pass only), claims gets the strata seen, and it ends on a
+// barrier.  s_bin: 16 ints of shared scratch.
+template <bool kFp64, class K>
+__device__ __noinline__ Partial part_staged(int lp, const K *rec_z, const uint16_t *rec_xy, int base, int n, int dx,
+                                            int dy, unsigned char *smem, int *gwt, uint64_t *gzk, bool want_hash,
+                                            int *s_w, int *s_over, int *s_nocc, int *s_bin, int &claims,
+                                            unsigned long long *dbg) {
+    using Plan = StagePlan<K>;
+    constexpr uint32_t cap = Plan::cap;
+    const unsigned full = 0xffffffffu;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    K *keys = reinterpret_cast<K *>(smem);
+    int *A = reinterpret_cast<int *>(smem + Plan::a_off);
+    int *occ = reinterpret_cast<int *>(smem + Plan::occ_off);
+    int *E = reinterpret_cast<int *>(smem + Plan::e_off);
+    K *zr = reinterpret_cast<K *>(smem + Plan::rec_off);
+    uint16_t *xyr = reinterpret_cast<uint16_t *>(smem + Plan::xy_off);
+    uint16_t *sorted = reinterpret_cast<uint16_t *>(smem);  // over the keys once they are dead
+    const int dxy = dx * dy;
+    const bool wsmem = dxy + dx + dy <= Plan::wtab;
+    int *wt = wsmem ? reinterpret_cast<int *>(smem + Plan::rec_off) + warp * Plan::wtab
+                    : gwt + (int64_t)warp * kGlobalWarpTab;
+    const int max_probe = kFp64 ? (int)cap : kPartProbe;
+    const K empty = (K)kEmptyKey;
+    Partial acc{0, 0.0, 0.0, 0.0, 0ull};
+    // sub-phase timers of thread 0 (FPGM_PHASE_TIMERS): dbg[16..21]
+    unsigned long long tp = (dbg && tid == 0) ? gtimer() : 0ull;
+    auto lap = [&](int i) {
+        if (dbg && tid == 0) {
+            const unsigned long long t = gtimer();
+            atomicAdd(&dbg[i], t - tp);
+            tp = t;
+        }
+    };
+    for (uint32_t i = tid; i < cap; i += kThreads) {
+        keys[i] = empty;
+        A[i] = 0;
+    }
+    if (tid == 0) *s_nocc = 0;
+    if (tid < 16) s_bin[tid] = 0;
+    {  // the records, every load in flight before the first store
+        const uint4 *gz = reinterpret_cast<const uint4 *>(rec_z + base);
+        const uint4 *gxy = reinterpret_cast<const uint4 *>(rec_xy + base);
+        uint4 *sz = reinterpret_cast<uint4 *>(zr), *sxy = reinterpret_cast<uint4 *>(xyr);
+        const int nz4 = n * (int)sizeof(K) / 16, nx4 = n / 8;
+        for (int i = tid; i < nz4; i += 4 * kThreads) {
+            uint4 w[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (i + u * kThreads < nz4) w[u] = __ldcg(gz + i + u * kThreads);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (i + u * kThreads < nz4) sz[i + u * kThreads] = w[u];
+        }
+        for (int i = tid; i < nx4; i += kThreads) sxy[i] = __ldcg(gxy + i);
+    }
+    __syncthreads();
+    lap(16);
+    // insert: eight records per thread and round; every lane runs every round (warp collectives)
+    const int ngroups = n >> 3;
+    const int rounds = (ngroups + kThreads - 1) / kThreads;
+    for (int rd = 0; rd < rounds; ++rd) {
+        const int g = rd * kThreads + tid;
+        const bool have = g < ngroups;
+        int sl[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) sl[j] = -1;
+        unsigned claimed = 0;
+        if (have) {
+            K z[8];
+            sload8(z, zr + 8 * g);
+            uint32_t h[8];
+            K k0[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                h[j] = part_slot(z[j], lp, Plan::lcap);
+                k0[j] = z[j] == empty ? empty : keys[h[j]];
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                if (z[j] == empty) continue;
+                if (k0[j] == z[j]) {
+                    sl[j] = (int)h[j];
+                    continue;
+                }
+                uint32_t hh = h[j];
+                for (int p = 0; p < max_probe; ++p) {
+                    const K k = keys[hh];
+                    if (k == z[j]) {
+                        sl[j] = (int)hh;
+                        break;
+                    }
+                    if (k == empty) {
+                        const K old = key_cas(&keys[hh], empty, z[j]);
+                        if (old == empty) {
+                            sl[j] = (int)hh;
+                            claimed |= 1u << j;
+                            break;
+                        }
+                        if (old == z[j]) {
+                            sl[j] = (int)hh;
+                            break;
+                        }
+                    }
+                    hh = (hh + 1) & (cap - 1);
+                }
+                if (sl[j] < 0) *s_over = 1;  // probe bound reached
+            }
+            slot_store8(zr + 8 * g, sl);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (sl[j] >= 0) atomicAdd(&A[sl[j]], 1);
+        }
+        // new strata appended to occ[]: one atomic per warp
+        const int c = __popc(claimed);
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(full, incl, o);
+            if (lane >= o) incl += t;
+        }
+        int first = 0;
+        if (lane == 31 && incl > 0) first = atomicAdd(s_nocc, incl);
+        first = __shfl_sync(full, first, 31) + incl - c;
+        while (claimed) {
+            const int j = __ffs(claimed) - 1;
+            claimed &= claimed - 1;
+            if (first < Plan::lim) occ[first] = sl[j];
+            ++first;
+        }
+    }
+    __syncthreads();
+    const int n_occ = *s_nocc;
+    if (n_occ > Plan::lim) *s_over = 1;
+    __syncthreads();
+    lap(17);
+    if (*s_over == 0) {
+        if (tid == 0) claims += n_occ;
+        // rank by size: bin 0 unscored (single samples), 1 .. 8 samples, 9 larger.  Per warp and
+        // round, lane b adds the warp's count of bin b (one atomic instruction for all bins).
+        auto bin_of = [&](int m) { return (m <= 1 && !want_hash) ? 0 : (m <= 8 ? m : 9); };
+        const int orounds = (n_occ + kThreads - 1) / kThreads;
+        for (int rd = 0; rd < orounds; ++rd) {
+            const int i = rd * kThreads + tid;
+            const int b = i < n_occ ? bin_of(A[occ[i]]) : 0;
+            unsigned mine = 0;
+#pragma unroll
+            for (int bb = 1; bb <= 9; ++bb) {
+                const unsigned bal = __ballot_sync(full, b == bb);
+                if (lane == bb) mine = bal;
+            }
+            if (lane >= 1 && lane <= 9 && mine) atomicAdd(&s_bin[lane], __popc(mine));
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int run = 0;
+            for (int bb = 1; bb <= 9; ++bb) {
+                const int cnt = s_bin[bb];
+                s_bin[bb] = run;
+                if (bb == 9) s_bin[12] = run;  // first stratum of more than kLaneStratum samples
+                run += cnt;
+            }
+            s_bin[15] = run;  // strata scored
+            E[0] = 0;
+        }
+        __syncthreads();
+        for (int rd = 0; rd < orounds; ++rd) {
+            const int i = rd * kThreads + tid;
+            int b = 0, m = 0, s = -1;
+            if (i < n_occ) {
+                s = occ[i];
+                m = A[s];
+                b = bin_of(m);
+            }
+            unsigned mine = 0, bal_b = 0;
+#pragma unroll
+            for (int bb = 1; bb <= 9; ++bb) {
+                const unsigned bal = __ballot_sync(full, b == bb);
+                if (lane == bb) mine = bal;
+                if (b == bb) bal_b = bal;
+            }
+            int r0 = 0;
+            if (lane >= 1 && lane <= 9 && mine) r0 = atomicAdd(&s_bin[lane], __popc(mine));
+            r0 = __shfl_sync(full, r0, b);  // lane b holds this bin's first rank for the warp
+            const int r = b > 0 ? r0 + __popc(bal_b & lanemask_lt()) : -1;
+            if (s >= 0) {
+                if (r >= 0) {
+                    E[1 + r] = m;
+                    if (want_hash) gzk[r] = (uint64_t)keys[s];
+                }
+                A[s] = r;  // -1: not scored
+            }
+        }
+        __syncthreads();
+        const int n_live = s_bin[15], first_big = s_bin[12];
+        block_exclusive_scan(E + 1, n_live, s_w);  // ends with a barrier; the keys are dead
+        lap(18);
+        // place: (x << 8) | y codes by stratum, one atomic per group of lanes with the same stratum
+        for (int rd = 0; rd < rounds; ++rd) {
+            const int g = rd * kThreads + tid;
+            const bool have = g < ngroups;
+            if (have) {
+                const uint4 c4 = reinterpret_cast<const uint4 *>(xyr)[g];
+                const uint32_t cw[4] = {c4.x, c4.y, c4.z, c4.w};
+                int sl[8], r[8];
+                slot_load8(sl, zr + 8 * g);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) r[j] = sl[j] >= 0 ? A[sl[j]] : -1;
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    if (r[j] >= 0) sorted[atomicAdd(&E[1 + r[j]], 1)] = (uint16_t)(cw[j >> 1] >> (16 * (j & 1)));
+            }
+        }
+        __syncthreads();
+        if (wsmem)  // the records are dead: per-warp x,y tables
+            for (int i = tid; i < kWarps * Plan::wtab; i += kThreads)
+                reinterpret_cast<int *>(smem + Plan::rec_off)[i] = 0;
+        __syncthreads();
+        lap(19);
+        Partial q = score_small_strata<kFp64>(E, sorted, first_big, dx, dy, nullptr, nullptr, gzk, want_hash, false);
+        if (dbg) {
+            __syncthreads();
+            lap(20);
+            if (tid == 0) {  // strata of more than kLaneStratum samples, and their samples
+                atomicAdd(&dbg[25], (unsigned long long)(n_live - first_big));
+                atomicAdd(&dbg[26], (unsigned long long)(E[n_live] - E[first_big]));
+                atomicAdd(&dbg[27], (unsigned long long)n);
+            }
+        }
+        acc = score_big_strata<kFp64>(q, E, sorted, nullptr, n_live - first_big, dx, dy, wt, gzk, want_hash,
+                                      first_big);
+    }
+    __syncthreads();  // before the next super-partition reuses shared memory
+    lap(21);
+    return acc;
+}
+
+// Super-partitions: consecutive partitions [sp[i], sp[i + 1]) whose padded records total at
+// most rmax (a single partition beyond rmax stands alone).  One thread; returns their count.
+__device__ inline int plan_super(const int *pcnt, int P, int rmax, int *sp) {
+    int ns = 0, run = 0;
+    sp[0] = 0;
+    for (int p = 0; p < P; ++p) {
+        const int w = (pcnt[p] + 7) & ~7;
+        if (run > 0 && run + w > rmax) {
+            sp[++ns] = p;
+            run = 0;
+        }
+        run += w;
+    }
+    sp[++ns] = P;
+    return ns;
+}
+
+// One super-partition [b0, b1): staged as a whole when its records fit; when its strata
+// overflow, its partitions one by one; a partition beyond the staged records goes through
+// part_partition (records read from global memory).  *s_over is left set only when a single
+// partition overflows.
+template <bool kFp64, class K>
+__device__ inline Partial part_super(int lp, const K *rec_z, const uint16_t *rec_xy, const int *pcnt, const int *poff,
+                                     int b0, int b1, int dx, int dy, unsigned char *smem, uint16_t *gord, int *gwt,
+                                     uint64_t *gzk, bool want_hash, int *s_w, int *s_over, int *s_nbig, int *s_nocc,
+                                     int *s_bin, int &claims, unsigned long long *dbg = nullptr) {
+    constexpr int R = StagePlan<K>::rec;
+    const int n = poff[b1] - poff[b0];
+    if (n == 0) return Partial{0, 0.0, 0.0, 0.0, 0ull};
+    if (n <= R) {
+        const Partial q = part_staged<kFp64, K>(lp, rec_z, rec_xy, poff[b0], n, dx, dy, smem, gwt, gzk, want_hash, s_w,
+                                                s_over, s_nocc, s_bin, claims, dbg);
+        if (*s_over == 0 || b1 - b0 == 1) return q;  // read after part_staged's closing barrier
+        __syncthreads();  // every thread has read s_over
+        if (threadIdx.x == 0) {
+            *s_over = 0;
+            if (dbg) atomicAdd(&dbg[24], 1ull);  // super-partitions split again
+        }
+        __syncthreads();
+    }
+    Partial acc{0, 0.0, 0.0, 0.0, 0ull};
+    for (int b = b0; b < b1; ++b) {
+        if (pcnt[b] == 0) continue;
+        const int nb = poff[b + 1] - poff[b];
+        const Partial q =
+            nb <= R ? part_staged<kFp64, K>(lp, rec_z, rec_xy, poff[b], nb, dx, dy, smem, gwt, gzk, want_hash, s_w,
+                                            s_over, s_nocc, s_bin, claims, dbg)
+                    : part_partition<kFp64, K>(lp, rec_z, rec_xy, pcnt[b], poff[b], dx, dy, smem, gord, gwt, gzk,
+                                               want_hash, s_w, s_over, s_nbig, s_nocc, s_bin, claims, dbg);
+        if (*s_over) return acc;
+        partial_add(acc, q);
+    }
+    return acc;
+}
+
+// Counts and scores every super-partition of a test (sp[0 .. n_sp]: partition boundaries,
+// plan_super) in shared memory, one after another; returns this thread's share of the
+// statistic (see part_super; stops at the first overflow).  s_pcnt / s_poff: records per
+// partition and each partition's first record.
 template <bool kFp64, class K>
 __device__ __noinline__ Partial part_run(int lp, const K *rec_z, const uint16_t *rec_xy, const int *s_pcnt,
-                                         const int *s_poff, int dx, int dy, unsigned char *smem, uint16_t *gord,
-                                         int *gwt, uint64_t *gzk, bool want_hash, int *s_w, int *s_over,
-                                         int *s_nbig, int *s_nocc, int *s_bin, int &claims,
+                                         const int *s_poff, const int *sp, int n_sp, int dx, int dy,
+                                         unsigned char *smem, uint16_t *gord, int *gwt, uint64_t *gzk, bool want_hash,
+                                         int *s_w, int *s_over, int *s_nbig, int *s_nocc, int *s_bin, int &claims,
                                          unsigned long long *dbg) {
-    const int P = 1 << lp;
     Partial acc{0, 0.0, 0.0, 0.0, 0ull};
-    if (dbg && threadIdx.x == 0) atomicAdd(&dbg[22], (unsigned long long)P);
-    for (int p = 0; p < P; ++p) {
-        const int n = s_pcnt[p];
-        if (n == 0) continue;
-        const Partial q = part_partition<kFp64, K>(lp, rec_z, rec_xy, n, s_poff[p], dx, dy, smem, gord, gwt, gzk,
-                                                   want_hash, s_w, s_over, s_nbig, s_nocc, s_bin, claims, dbg);
-        if (*s_over) break;  // read after part_partition's closing barrier, same in every thread
+    if (dbg && threadIdx.x == 0) atomicAdd(&dbg[22], (unsigned long long)n_sp);
+    for (int i = 0; i < n_sp; ++i) {
+        const Partial q = part_super<kFp64, K>(lp, rec_z, rec_xy, s_pcnt, s_poff, sp[i], sp[i + 1], dx, dy, smem, gord,
+                                               gwt, gzk, want_hash, s_w, s_over, s_nbig, s_nocc, s_bin, claims, dbg);
+        if (*s_over) break;  // read after part_super's closing barrier, same in every thread
         partial_add(acc, q);
     }
     return acc;
@@ -1305,7 +1801,8 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
     int *swt = reinterpret_cast<int *>(smem_raw + kZTabOff);
     __shared__ const uint8_t *s_col[kMaxCols];
     __shared__ uint32_t s_dim[kMaxCols];
-    __shared__ int s_idx, s_over, s_distinct, s_flag, s_seen, s_pick;
+    __shared__ int s_idx, s_over, s_distinct, s_flag, s_seen, s_pick, s_skip;
+    __shared__ double s_est;
     __shared__ int s_w[kWarps];
     __shared__ Partial scratch[kWarps];
     const int tid = threadIdx.x;
@@ -1376,11 +1873,22 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             __syncthreads();
             continue;
         }
-        for (int attempt = kRetry ? 2 : 0; attempt < 3; ++attempt) {
+        // the autotuner bucket's overflow record may skip the shared-hash attempt
+        const int obucket = a.ovf ? tune_index(S, d, (double)dz * s_dim[d] * s_dim[d + 1]) : -1;
+        if (!kRetry && tid == 0) {
+            double e = 0.0;
+            s_skip = ovf_skip(a, obucket, S, &e);
+            s_est = e;
+            if (s_skip) s_over = 1;  // as after an overflowing attempt 0 (a hand-over keeps it set)
+        }
+        __syncthreads();
+        const bool skip0 = !kRetry && s_skip;
+        for (int attempt = kRetry ? 2 : (skip0 ? 1 : 0); attempt < 3; ++attempt) {
             global = attempt >= 1;
             const bool k32 = !global && code32;
             if (attempt == 1) {
-                const double est = (double)zlimit * (double)(nvec > 1 ? nvec : 1) / (double)(seen > 1 ? seen : 1);
+                const double est = skip0 ? s_est
+                                         : (double)zlimit * (double)(nvec > 1 ? nvec : 1) / (double)(seen > 1 ? seen : 1);
                 const bool tail = a.wide != nullptr && n2 <= a.wide_small_n2;
                 if (tid == 0) {
                     int b = -1;
@@ -1471,6 +1979,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             __syncthreads();
             FPGM_PHASE(attempt > 0 ? 1 : 0);
             seen = s_seen > 0 ? s_seen : (int)nvec;
+            if (attempt == 0 && tid == 0 && obucket >= 0) atomicAdd(&a.ovf[8 * obucket + (s_over ? 0 : 1)], 1ull);
             if (!s_over) break;
             __syncthreads();
         }
@@ -1483,6 +1992,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             continue;
         }
         const int n_obs = s_distinct;
+        if (tid == 0 && global) ovf_strata(a, obucket, S, n_obs);
         if (a.dbg && tid == 0) {
             atomicAdd(&a.dbg[10], (unsigned long long)n_obs);
             atomicAdd(&a.dbg[11], 1ull);
@@ -1648,7 +2158,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
     __shared__ int s_bin[16];
     __shared__ int s_w[kWarps];
     __shared__ Partial scratch[kWarps];
-    __shared__ int s_pcnt[kPartMax], s_poff[kPartMax + 1], s_pcur[kPartMax];
+    __shared__ int s_pcnt[kPartMax], s_poff[kPartMax + 1], s_pcur[kPartMax], s_sp[kPartMax + 1], s_nsp;
     const int tid = threadIdx.x;
     char *slot = a.slot_mem + (int64_t)blockIdx.x * a.slot_bytes;
     const SlotLayout L = slot_layout(a.slot_S, (uint32_t)a.hash_cap_global);
@@ -1689,26 +2199,34 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
         for (int j = 0; j < d; ++j) dz *= s_dim[j];
         const bool code32 = dz <= 0xFFFFFFFFull;
         const int dx = s_dim[d], dy = s_dim[d + 1];
-        // partitions: about 30% of a partition table's slots (strata are estimated high) and
-        // half the shared sorted array expected per partition
-        const double capmax = code32 ? PartPlan<uint32_t>::cap : PartPlan<uint64_t>::cap;
-        const double ordcap = code32 ? PartPlan<uint32_t>::ord_cap : PartPlan<uint64_t>::ord_cap;
+        // Super-partitions of at most rmax records (the staged shared-memory plan), few enough
+        // that their strata -- est per sample, which errs high -- fill at most 70% of a table;
+        // partitions of about a quarter of that, so that runs of them pack well.
+        const int rstage = code32 ? StagePlan<uint32_t>::rec : StagePlan<uint64_t>::rec;
+        const int lim = code32 ? StagePlan<uint32_t>::lim : StagePlan<uint64_t>::lim;
+        const double ratio = fmax(est / (double)(S > 0 ? S : 1), 1e-6);
+        int rmax = (int)fmin((double)rstage, 0.7 * lim / ratio) & ~7;
+        if (rmax < 64) rmax = 64;
         int lp = 1;
         const int maxlog = a.part_max_log;
-        while ((double)(1 << lp) < fmax(est / (0.3 * capmax), (double)S / (0.5 * ordcap)) && lp < maxlog) ++lp;
+        while ((S >> lp) > rmax / 4 && lp < maxlog) ++lp;
         if (a.wide != nullptr && idx >= np - (int)gridDim.x) {
             // One of the list's last tests (all of them when there are no more tests than
-            // CTAs): its records are written here, then its partitions are queued for
+            // CTAs): its records are written here, then its super-partitions are queued for
             // ci_part_wide_kernel, which scores them on whichever CTAs are free.  This CTA
-            // takes no further test, so its slot keeps the records.
+            // takes no further test, so its slot keeps the records.  Super-partitions are cut
+            // small enough for about two per CTA over the published tests.
             const int nw = np < (int)gridDim.x ? np : (int)gridDim.x;
-            int lw = lp > a.wide_min_log ? lp : a.wide_min_log;
-            if (lw > maxlog) lw = maxlog;
-            while ((1 << lw) * nw < 2 * (int)gridDim.x && lw < maxlog && (S >> (lw + 1)) >= a.wide_part_min) ++lw;
+            int rw = (int)fmin((double)rmax, (double)S * nw / (2.0 * gridDim.x)) & ~7;
+            if (rw < a.wide_part_min) rw = a.wide_part_min < rmax ? a.wide_part_min : rmax;
+            int lw = a.wide_min_log < maxlog ? a.wide_min_log : maxlog;
+            while ((S >> lw) > rw / 4 && lw < maxlog) ++lw;
             if (code32)
-                part_scatter(s_col, s_dim, d, S, lw, reinterpret_cast<uint32_t *>(rz), rxy, s_pcnt, s_poff, s_pcur);
+                part_scatter(s_col, s_dim, d, S, lw, reinterpret_cast<uint32_t *>(rz), rxy, s_pcnt, s_poff, s_pcur,
+                             reinterpret_cast<uint32_t *>(gzk), smem_raw);
             else
-                part_scatter(s_col, s_dim, d, S, lw, reinterpret_cast<uint64_t *>(rz), rxy, s_pcnt, s_poff, s_pcur);
+                part_scatter(s_col, s_dim, d, S, lw, reinterpret_cast<uint64_t *>(rz), rxy, s_pcnt, s_poff, s_pcur,
+                             reinterpret_cast<uint64_t *>(gzk), smem_raw);
             FPGM_PHASE(14);
             if (tid == 0) s_idx = atomicAdd(&a.counters[C_WIDET], 1);
             __syncthreads();
@@ -1720,8 +2238,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
             }
             if (tid == 0) {
                 w->poff[P] = s_poff[P];
-                int nne = 0;
-                for (int i = 0; i < P; ++i) nne += s_pcnt[i] > 0;
+                const int nne = plan_super(s_pcnt, P, rw, w->sp);
                 w->item = item;
                 w->owner = blockIdx.x;
                 w->lp = lw;
@@ -1738,8 +2255,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
                 w->abs_g2 = 0.0;
                 w->hash = 0ull;
                 const int q0 = atomicAdd(&a.counters[C_WIDEQ], nne);
-                for (int i = 0, q = q0; i < P; ++i)
-                    if (s_pcnt[i] > 0) a.wide_items[q++] = (s_idx << 8) | i;
+                for (int i = 0; i < nne; ++i) a.wide_items[q0 + i] = (s_idx << 8) | i;
                 if (a.dbg) atomicAdd(&a.dbg[23], 1ull);
             }
             __syncthreads();
@@ -1753,19 +2269,23 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
                 s_distinct = 0;
             }  // visible after part_scatter's first barrier
             int claims = 0;
-            if (code32) {
-                part_scatter(s_col, s_dim, d, S, lp, reinterpret_cast<uint32_t *>(rz), rxy, s_pcnt, s_poff, s_pcur);
-                FPGM_PHASE(14);
-                acc = part_run<false>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, s_pcnt, s_poff, dx, dy,
-                                      smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
+            if (code32)
+                part_scatter(s_col, s_dim, d, S, lp, reinterpret_cast<uint32_t *>(rz), rxy, s_pcnt, s_poff, s_pcur,
+                             reinterpret_cast<uint32_t *>(gzk), smem_raw);
+            else
+                part_scatter(s_col, s_dim, d, S, lp, reinterpret_cast<uint64_t *>(rz), rxy, s_pcnt, s_poff, s_pcur,
+                             reinterpret_cast<uint64_t *>(gzk), smem_raw);
+            if (tid == 0) s_nsp = plan_super(s_pcnt, 1 << lp, rmax, s_sp);
+            __syncthreads();
+            FPGM_PHASE(14);
+            if (code32)
+                acc = part_run<false>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, s_pcnt, s_poff, s_sp, s_nsp, dx,
+                                      dy, smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
                                       s_bin, claims, a.dbg);
-            } else {
-                part_scatter(s_col, s_dim, d, S, lp, reinterpret_cast<uint64_t *>(rz), rxy, s_pcnt, s_poff, s_pcur);
-                FPGM_PHASE(14);
-                acc = part_run<false>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, s_pcnt, s_poff, dx, dy,
-                                      smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
+            else
+                acc = part_run<false>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, s_pcnt, s_poff, s_sp, s_nsp, dx,
+                                      dy, smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
                                       s_bin, claims, a.dbg);
-            }
             atomicAdd(&s_distinct, claims);
             __syncthreads();
             over = s_over != 0;
@@ -1780,6 +2300,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
             }
         } else {
             const int n_obs = s_distinct;
+            if (tid == 0) ovf_strata(a, a.ovf ? tune_index(S, d, (double)dz * dx * dy) : -1, S, n_obs);
             if (a.dbg && tid == 0) {
                 atomicAdd(&a.dbg[9], (unsigned long long)n_obs);
                 atomicAdd(&a.dbg[13], 1ull);
@@ -1787,11 +2308,11 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
             const Partial r = block_sum(acc, scratch);
             decide_record(a, item, r, (int64_t)n_obs * dx * dy, 3, s_flag, scratch, [&]() {
                 int claims = 0;
-                return code32 ? part_run<true>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, s_pcnt, s_poff, dx,
-                                               dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over,
+                return code32 ? part_run<true>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, s_pcnt, s_poff, s_sp,
+                                               s_nsp, dx, dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over,
                                                &s_nbig, &s_nocc, s_bin, claims, nullptr)
-                              : part_run<true>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, s_pcnt, s_poff, dx,
-                                               dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over,
+                              : part_run<true>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, s_pcnt, s_poff, s_sp,
+                                               s_nsp, dx, dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over,
                                                &s_nbig, &s_nocc, s_bin, claims, nullptr);
             });
         }
@@ -1844,13 +2365,13 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_wide_kernel(WaveArgs a) {
         __syncthreads();
         int claims = 0;
         const Partial q =
-            code32 ? part_partition<false, uint32_t>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, w->pcnt[p],
-                                                     w->poff[p], dx, dy, smem_raw, gord, gwt, zk, a.want_hash != 0, s_w,
-                                                     &s_over, &s_nbig, &s_nocc, s_bin, claims, nullptr)
-                   : part_partition<false, uint64_t>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, w->pcnt[p],
-                                                     w->poff[p], dx, dy, smem_raw, gord, gwt, zk, a.want_hash != 0, s_w,
-                                                     &s_over, &s_nbig, &s_nocc, s_bin, claims, nullptr);
-        const bool over = s_over != 0;  // read after part_partition's closing barrier
+            code32 ? part_super<false, uint32_t>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, w->pcnt, w->poff,
+                                                 w->sp[p], w->sp[p + 1], dx, dy, smem_raw, gord, gwt, zk,
+                                                 a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc, s_bin, claims)
+                   : part_super<false, uint64_t>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, w->pcnt, w->poff,
+                                                 w->sp[p], w->sp[p + 1], dx, dy, smem_raw, gord, gwt, zk,
+                                                 a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc, s_bin, claims);
+        const bool over = s_over != 0;  // read after part_super's closing barrier
         const Partial r = block_sum(q, scratch);
         if (tid == 0) {
             if (over) {
@@ -1890,11 +2411,11 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_wide_kernel(WaveArgs a) {
                 decide_record(a, item, R, (int64_t)n_obs * dx * dy, 4, s_flag, scratch, [&]() {
                     int cl = 0;
                     return code32 ? part_run<true>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, w->pcnt, w->poff,
-                                                   dx, dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over, &s_nbig,
-                                                   &s_nocc, s_bin, cl, nullptr)
+                                                   w->sp, w->n_items, dx, dy, smem_raw, gord, gwt, nullptr, false, s_w,
+                                                   &s_over, &s_nbig, &s_nocc, s_bin, cl, nullptr)
                                   : part_run<true>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, w->pcnt, w->poff,
-                                                   dx, dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over, &s_nbig,
-                                                   &s_nocc, s_bin, cl, nullptr);
+                                                   w->sp, w->n_items, dx, dy, smem_raw, gord, gwt, nullptr, false, s_w,
+                                                   &s_over, &s_nbig, &s_nocc, s_bin, cl, nullptr);
                 });
             }
         }

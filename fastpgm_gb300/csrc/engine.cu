@@ -189,6 +189,8 @@ struct fpgm_engine {
     // fixed sample-count cut-over (FPGM_PART_CUTOVER, default 65,536)
     int64_t part_min_samples = kPartMinSamples;
     DevBuf tune, tune_obs;  // a fixed table (FPGM_TUNE_TABLE) / the online autotuner's timings
+    DevBuf ovf;             // per bucket: how often tier-2 tests overflowed the shared strata hash
+    bool ovf_on = true;     // FPGM_OVF_SKIP=0: every tier-2 test tries the shared hash first
     bool tune_loaded = false, tune_online = true;
     std::string tune_source;
     // result
@@ -743,6 +745,11 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
         RET(e->tune_obs.ensure((size_t)kTuneBuckets * 8 * 8));
         CK(cudaMemset(e->tune_obs.p, 0, (size_t)kTuneBuckets * 8 * 8));
     }
+    if (const char *w = getenv("FPGM_OVF_SKIP")) e->ovf_on = atoi(w) != 0;
+    if (e->ovf_on) {
+        RET(e->ovf.ensure((size_t)kTuneBuckets * 8 * 8));
+        CK(cudaMemset(e->ovf.p, 0, (size_t)kTuneBuckets * 8 * 8));
+    }
     if (getenv("FPGM_PHASE_TIMERS")) {
         RET(e->phase_timers.ensure(32 * 8));
         CK(cudaMemset(e->phase_timers.p, 0, 32 * 8));
@@ -761,7 +768,7 @@ extern "C" int fpgm_engine_destroy(fpgm_engine *e) {
                       &e->tests_buf, &e->detail_buf, &e->item_vars, &e->lists, &e->band,
                       &e->phase_timers, &e->var_off, &e->var_S, &e->var_lo, &e->var_hi, &e->mle_counts,
                       &e->mle_pot, &e->mle_meta, &e->wide, &e->wide_items, &e->tune, &e->wave_ctl,
-                      &e->tune_obs, &e->res_adj_d, &e->res_key, &e->res_idx, &e->res_removed_d, &e->res_cnt,
+                      &e->tune_obs, &e->ovf, &e->res_adj_d, &e->res_key, &e->res_idx, &e->res_removed_d, &e->res_cnt,
                       &e->res_vars_d};
     for (DevBuf *b : bufs) b->release();
     gram_destroy(e->gram);
@@ -963,6 +970,7 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t ite
         }
         a.tune = e->tune_loaded ? e->tune.as<int8_t>() : nullptr;
         a.tune_obs = (e->tune_online && !e->tune_loaded) ? e->tune_obs.as<unsigned long long>() : nullptr;
+        a.ovf = e->ovf_on ? e->ovf.as<unsigned long long>() : nullptr;
         a.part_min_samples = e->part_min_samples;
     }
     a.part_max_log = e->part_max_log;
@@ -1182,6 +1190,9 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
             CK(cudaMemsetAsync(a.dbg, 0, sizeof h, e->stream));
             CK(cudaStreamSynchronize(e->stream));
             if (h[23]) fprintf(stderr, "partition-parallel d=%d tests=%llu\n", d, h[23]);
+            if (h[27])
+                fprintf(stderr, "staged d=%llu records=%llu re-split=%llu big strata=%llu holding %llu samples\n",
+                        (unsigned long long)d, h[27], h[24], h[25], h[26]);
             if (h[13])
                 fprintf(stderr,
                         "partitioned d=%d tests=%llu strata/test=%.0f partitions/test=%.1f us/test: records=%.1f "
