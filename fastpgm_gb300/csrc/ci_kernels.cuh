@@ -662,6 +662,17 @@ __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gor
             if (collect) big[atomicAdd(n_big, 1)] = k;
             continue;
         }
+        if (m == 2 && !want_hash) {
+            // two samples add one degree of freedom and two cells of 2 ln 2 when they differ in
+            // both x and y, and nothing otherwise
+            const uint32_t dif = (uint32_t)gord[o0] ^ (uint32_t)gord[o0 + 1];
+            if ((dif >> 8) != 0 && (dif & 0xffu) != 0) {
+                acc.df += 1;
+                ta.add(1, 1, 1, 2);
+                ta.add(1, 1, 1, 2);
+            }
+            continue;
+        }
         // one register per sample: (x << 8) | y; equal cells <=> equal words
         uint32_t pk[kLaneStratum];
 #pragma unroll
