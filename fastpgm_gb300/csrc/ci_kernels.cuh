@@ -540,6 +540,29 @@ __device__ inline int zinsert(K *keys, Id *ids, uint32_t cap, uint64_t zz, int *
     return -1;
 }
 
+// As zinsert, without the id: *claimed is set when this call took an empty slot for z (the
+// caller hands out the ids of a warp's claims together).  Returns the slot, or -1 after
+// max_probe probes.
+template <class K>
+__device__ __forceinline__ int zclaim(K *keys, uint32_t cap, uint64_t zz, uint32_t max_probe, bool *claimed) {
+    const K z = (K)zz, empty = (K)kEmptyKey;
+    uint32_t h = zhash(zz, cap);
+    for (uint32_t p = 0; p < max_probe; ++p) {
+        const K k = keys[h];
+        if (k == z) return (int)h;
+        if (k == empty) {
+            const K old = key_cas(&keys[h], empty, z);
+            if (old == empty) {
+                *claimed = true;
+                return (int)h;
+            }
+            if (old == z) return (int)h;
+        }
+        h = (h + 1) & (cap - 1);
+    }
+    return -1;
+}
+
 // Stratum codes of 16 consecutive samples (vector v) from the d Z columns, four column
 // loads in flight at a time.  K = uint32_t when every code is below 2^32 (so is every
 // prefix of the mixed-radix code).
@@ -1936,43 +1959,74 @@ __global__ void __launch_bounds__(kThreads, 2) ci_compact_kernel(WaveArgs a) {
             __syncthreads();
             const int limit = global ? (int)(cap / 2) : zlimit;
             const uint32_t max_probe = global ? cap : 64u;
-            for (int64_t v = tid; v < nvec; v += kThreads) {
-                if (*(volatile int *)&s_over) break;
-                uint64_t z[16];
-                zcodes16(z, s_col, s_dim, d, v);
-                // first probes of all 16 codes in flight at once; a code found there (the common
-                // case) is done, the others take the inserting path (a stale empty slot read
-                // here is resolved by its compare-and-swap)
+            // every lane runs every round (the ids of a warp's new strata are handed out together)
+            const int64_t vrounds = (nvec + kThreads - 1) / kThreads;
+            for (int64_t rd = 0; rd < vrounds; ++rd) {
+                if (*(volatile int *)&s_over) break;  // one load per warp: the same for its lanes
+                const int64_t v = rd * kThreads + tid;
+                const bool have = v < nvec;
                 int hs[16];
+                unsigned claimed = 0;
                 bool ok = true;
+                if (have) {
+                    uint64_t z[16];
+                    zcodes16(z, s_col, s_dim, d, v);
+                    // first probes of all 16 codes in flight at once; a code found there (the
+                    // common case) is done, the others take the inserting path (a stale empty
+                    // slot read here is resolved by its compare-and-swap)
 #pragma unroll
-                for (int b0 = 0; b0 < 16; b0 += 8) {  // eight at a time (register budget)
-                    uint64_t kk[8];
+                    for (int b0 = 0; b0 < 16; b0 += 8) {  // eight at a time (register budget)
+                        uint64_t kk[8];
 #pragma unroll
-                    for (int b = 0; b < 8; ++b) {
-                        hs[b0 + b] = (int)zhash(z[b0 + b], cap);
-                        kk[b] = k32 ? (uint64_t)hkeys32[hs[b0 + b]] : keys[hs[b0 + b]];
+                        for (int b = 0; b < 8; ++b) {
+                            hs[b0 + b] = (int)zhash(z[b0 + b], cap);
+                            kk[b] = k32 ? (uint64_t)hkeys32[hs[b0 + b]] : keys[hs[b0 + b]];
+                        }
+#pragma unroll
+                        for (int b = 0; b < 8; ++b) {
+                            if (!ok || kk[b] == z[b0 + b]) continue;
+                            bool cl = false;
+                            hs[b0 + b] = k32 ? zclaim(hkeys32, cap, z[b0 + b], max_probe, &cl)
+                                             : zclaim(keys, cap, z[b0 + b], max_probe, &cl);
+                            if (cl) claimed |= 1u << (b0 + b);
+                            ok = hs[b0 + b] >= 0;
+                        }
                     }
+                }
+                // ids of the warp's new strata: one atomic per warp
+                const int c = __popc(claimed);
+                int incl = c;
 #pragma unroll
-                    for (int b = 0; b < 8; ++b) {
-                        if (!ok || kk[b] == z[b0 + b]) continue;
-                        hs[b0 + b] = global ? zinsert(keys, gids, cap, z[b0 + b], &s_distinct, limit, max_probe, zk)
-                                     : k32  ? zinsert(hkeys32, hids, cap, z[b0 + b], &s_distinct, limit, max_probe, zk)
-                                            : zinsert(keys, hids, cap, z[b0 + b], &s_distinct, limit, max_probe, zk);
-                        ok = hs[b0 + b] >= 0;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if ((tid & 31) >= o) incl += t;
+                }
+                int first = 0;
+                if ((tid & 31) == 31 && incl > 0) first = atomicAdd(&s_distinct, incl);
+                first = __shfl_sync(0xffffffffu, first, 31) + incl - c;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    if (!(claimed >> j & 1u)) continue;
+                    if (first < limit) {
+                        if (global) gids[hs[j]] = first;
+                        else hids[hs[j]] = (uint16_t)first;
+                        if (zk) zk[first] = k32 ? (uint64_t)hkeys32[hs[j]] : keys[hs[j]];  // the slot holds the code
+                    } else {
+                        ok = false;
                     }
+                    ++first;
                 }
                 if (!ok) {
                     s_over = 1;
                     s_seen = (int)v + 1;
-                    break;
+                } else if (have) {
+                    // one 64-byte run per thread, written after the inserts
+                    int4 *dst = reinterpret_cast<int4 *>(gsid + v * 16);
+                    dst[0] = make_int4(hs[0], hs[1], hs[2], hs[3]);
+                    dst[1] = make_int4(hs[4], hs[5], hs[6], hs[7]);
+                    dst[2] = make_int4(hs[8], hs[9], hs[10], hs[11]);
+                    dst[3] = make_int4(hs[12], hs[13], hs[14], hs[15]);
                 }
-                // one 64-byte run per thread, written after the inserts
-                int4 *dst = reinterpret_cast<int4 *>(gsid + v * 16);
-                dst[0] = make_int4(hs[0], hs[1], hs[2], hs[3]);
-                dst[1] = make_int4(hs[4], hs[5], hs[6], hs[7]);
-                dst[2] = make_int4(hs[8], hs[9], hs[10], hs[11]);
-                dst[3] = make_int4(hs[12], hs[13], hs[14], hs[15]);
             }
             for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
                 if (*(volatile int *)&s_over) break;
