@@ -807,12 +807,20 @@ __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const ui
             }
         } else {
             const int o1 = o0 + m;
-            for (int i = o0 + lane; i < o1; i += 32) {
-                const int p = gord[i];
-                const int x = p >> 8, y = p & 0xff;
-                atomicAdd(&wt[x * dy + y], 1);
-                ax += atomicAdd(&wni[x], 1) == 0;
-                ay += atomicAdd(&wnj[y], 1) == 0;
+            // counts: four codes per lane loaded together, so a stratum in global memory costs
+            // one load round trip per 128 samples
+            for (int i0 = o0 + lane; i0 < o1; i0 += 128) {
+                int q[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) q[u] = i0 + 32 * u < o1 ? (int)gord[i0 + 32 * u] : -1;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (q[u] < 0) break;
+                    const int x = q[u] >> 8, y = q[u] & 0xff;
+                    atomicAdd(&wt[x * dy + y], 1);
+                    ax += atomicAdd(&wni[x], 1) == 0;
+                    ay += atomicAdd(&wnj[y], 1) == 0;
+                }
             }
             __syncwarp();
 #pragma unroll
