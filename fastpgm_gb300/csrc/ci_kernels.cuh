@@ -113,6 +113,7 @@ struct WaveArgs {
     unsigned long long *ovf;
     int32_t warp_ints;             // ints of the warp tier's per-warp slice (its table limit)
     int32_t dense_rows;            // compact kernel's dense strata table: a thread per stratum (else lane groups)
+    int32_t stage_rec;             // records staged in shared memory at most (0: as many as fit; tests lower it)
     int64_t part_min_samples;
 };
 
@@ -1727,8 +1728,8 @@ template <bool kFp64, class K>
 __device__ inline Partial part_super(int lp, const K *rec_z, const uint16_t *rec_xy, const int *pcnt, const int *poff,
                                      int b0, int b1, int dx, int dy, unsigned char *smem, uint16_t *gord, int *gwt,
                                      uint64_t *gzk, bool want_hash, int *s_w, int *s_over, int *s_nbig, int *s_nocc,
-                                     int *s_bin, int &claims, unsigned long long *dbg = nullptr) {
-    constexpr int R = StagePlan<K>::rec;
+                                     int *s_bin, int &claims, int rstage, unsigned long long *dbg = nullptr) {
+    const int R = rstage > 0 && rstage < StagePlan<K>::rec ? rstage : StagePlan<K>::rec;
     const int n = poff[b1] - poff[b0];
     if (n == 0) return Partial{0, 0.0, 0.0, 0.0, 0ull};
     if (n <= R) {
@@ -1766,12 +1767,13 @@ __device__ __noinline__ Partial part_run(int lp, const K *rec_z, const uint16_t 
                                          const int *s_poff, const int *sp, int n_sp, int dx, int dy,
                                          unsigned char *smem, uint16_t *gord, int *gwt, uint64_t *gzk, bool want_hash,
                                          int *s_w, int *s_over, int *s_nbig, int *s_nocc, int *s_bin, int &claims,
-                                         unsigned long long *dbg) {
+                                         int rstage, unsigned long long *dbg) {
     Partial acc{0, 0.0, 0.0, 0.0, 0ull};
     if (dbg && threadIdx.x == 0) atomicAdd(&dbg[22], (unsigned long long)n_sp);
     for (int i = 0; i < n_sp; ++i) {
         const Partial q = part_super<kFp64, K>(lp, rec_z, rec_xy, s_pcnt, s_poff, sp[i], sp[i + 1], dx, dy, smem, gord,
-                                               gwt, gzk, want_hash, s_w, s_over, s_nbig, s_nocc, s_bin, claims, dbg);
+                                               gwt, gzk, want_hash, s_w, s_over, s_nbig, s_nocc, s_bin, claims, rstage,
+                                               dbg);
         if (*s_over) break;  // read after part_super's closing barrier, same in every thread
         partial_add(acc, q);
     }
@@ -2275,7 +2277,8 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
         // Super-partitions of at most rmax records (the staged shared-memory plan), few enough
         // that their strata -- est per sample, which errs high -- fill at most 70% of a table;
         // partitions of about a quarter of that, so that runs of them pack well.
-        const int rstage = code32 ? StagePlan<uint32_t>::rec : StagePlan<uint64_t>::rec;
+        int rstage = code32 ? StagePlan<uint32_t>::rec : StagePlan<uint64_t>::rec;
+        if (a.stage_rec > 0 && a.stage_rec < rstage) rstage = a.stage_rec;
         const int lim = code32 ? StagePlan<uint32_t>::lim : StagePlan<uint64_t>::lim;
         const double ratio = fmax(est / (double)(S > 0 ? S : 1), 1e-6);
         int rmax = (int)fmin((double)rstage, 0.7 * lim / ratio) & ~7;
@@ -2354,11 +2357,11 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
             if (code32)
                 acc = part_run<false>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, s_pcnt, s_poff, s_sp, s_nsp, dx,
                                       dy, smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
-                                      s_bin, claims, a.dbg);
+                                      s_bin, claims, a.stage_rec, a.dbg);
             else
                 acc = part_run<false>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, s_pcnt, s_poff, s_sp, s_nsp, dx,
                                       dy, smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
-                                      s_bin, claims, a.dbg);
+                                      s_bin, claims, a.stage_rec, a.dbg);
             atomicAdd(&s_distinct, claims);
             __syncthreads();
             over = s_over != 0;
@@ -2383,10 +2386,10 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
                 int claims = 0;
                 return code32 ? part_run<true>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, s_pcnt, s_poff, s_sp,
                                                s_nsp, dx, dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over,
-                                               &s_nbig, &s_nocc, s_bin, claims, nullptr)
+                                               &s_nbig, &s_nocc, s_bin, claims, a.stage_rec, nullptr)
                               : part_run<true>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, s_pcnt, s_poff, s_sp,
                                                s_nsp, dx, dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over,
-                                               &s_nbig, &s_nocc, s_bin, claims, nullptr);
+                                               &s_nbig, &s_nocc, s_bin, claims, a.stage_rec, nullptr);
             });
         }
         if (tid == 0 && a.tune_obs && !a.tune) {  // the partition path's time for the online autotuner
@@ -2440,10 +2443,12 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_wide_kernel(WaveArgs a) {
         const Partial q =
             code32 ? part_super<false, uint32_t>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, w->pcnt, w->poff,
                                                  w->sp[p], w->sp[p + 1], dx, dy, smem_raw, gord, gwt, zk,
-                                                 a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc, s_bin, claims)
+                                                 a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc, s_bin, claims,
+                                                 a.stage_rec)
                    : part_super<false, uint64_t>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, w->pcnt, w->poff,
                                                  w->sp[p], w->sp[p + 1], dx, dy, smem_raw, gord, gwt, zk,
-                                                 a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc, s_bin, claims);
+                                                 a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc, s_bin, claims,
+                                                 a.stage_rec);
         const bool over = s_over != 0;  // read after part_super's closing barrier
         const Partial r = block_sum(q, scratch);
         if (tid == 0) {
@@ -2485,10 +2490,10 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_wide_kernel(WaveArgs a) {
                     int cl = 0;
                     return code32 ? part_run<true>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, w->pcnt, w->poff,
                                                    w->sp, w->n_items, dx, dy, smem_raw, gord, gwt, nullptr, false, s_w,
-                                                   &s_over, &s_nbig, &s_nocc, s_bin, cl, nullptr)
+                                                   &s_over, &s_nbig, &s_nocc, s_bin, cl, a.stage_rec, nullptr)
                                   : part_run<true>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, w->pcnt, w->poff,
                                                    w->sp, w->n_items, dx, dy, smem_raw, gord, gwt, nullptr, false, s_w,
-                                                   &s_over, &s_nbig, &s_nocc, s_bin, cl, nullptr);
+                                                   &s_over, &s_nbig, &s_nocc, s_bin, cl, a.stage_rec, nullptr);
                 });
             }
         }

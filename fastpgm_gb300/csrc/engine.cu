@@ -191,6 +191,7 @@ struct fpgm_engine {
     DevBuf tune, tune_obs;  // a fixed table (FPGM_TUNE_TABLE) / the online autotuner's timings
     DevBuf ovf;             // per bucket: how often tier-2 tests overflowed the shared strata hash
     bool ovf_on = true;     // FPGM_OVF_SKIP=0: every tier-2 test tries the shared hash first
+    int stage_rec = 0;      // FPGM_STAGE_REC=n (tests): at most n records per staged super-partition
     bool tune_loaded = false, tune_online = true;
     std::string tune_source;
     // result
@@ -746,6 +747,7 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
         CK(cudaMemset(e->tune_obs.p, 0, (size_t)kTuneBuckets * 8 * 8));
     }
     if (const char *w = getenv("FPGM_OVF_SKIP")) e->ovf_on = atoi(w) != 0;
+    if (const char *w = getenv("FPGM_STAGE_REC")) e->stage_rec = std::max(0, atoi(w)) & ~7;
     if (e->ovf_on) {
         RET(e->ovf.ensure((size_t)kTuneBuckets * 8 * 8));
         CK(cudaMemset(e->ovf.p, 0, (size_t)kTuneBuckets * 8 * 8));
@@ -976,6 +978,7 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t ite
     a.part_max_log = e->part_max_log;
     a.warp_ints = e->warp_small ? kWarpIntsSmall : kWarpInts;
     a.dense_rows = e->dense_rows;
+    a.stage_rec = e->stage_rec;
     return FPGM_OK;
 }
 

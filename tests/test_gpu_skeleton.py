@@ -364,3 +364,25 @@ def test_large_warp_slices_match_reference(monkeypatch, tmp_path, name):
     assert res["sepsets"] == read_sepsets(os.path.join(GOLDEN, name + "_sepsets"))
     n = raw.shape[0]
     assert struct_of(tmp_path, ["V%d" % i for i in range(n)], res) == open(os.path.join(GOLDEN, name + "_struct")).read()
+
+
+@pytest.mark.parametrize("env", [{}, {"FPGM_OVF_SKIP": "0"}, {"FPGM_STAGE_REC": "64"}, {"FPGM_STAGE_REC": "1024"}])
+def test_tier2_paths_match_oracle_over_repeated_skeletons(monkeypatch, env):
+    """Tier 2 on a 70,000-sample dataset with 6-9 states, three skeletons on one engine (the
+    autotuner and the shared-hash overflow record carry over from one to the next, so later
+    skeletons skip the shared-hash attempt where it overflowed before): the default, the
+    attempt never skipped (FPGM_OVF_SKIP=0), and the staged super-partitions capped at 64 or
+    1,024 records (FPGM_STAGE_REC; at 64 nearly every partition is counted from its records
+    in global memory instead).  Every skeleton equals the oracle's, test counts included."""
+    raw, _, _ = F.generate(n_nodes=12, n_samples=70000, seed=72, n_edges=30, max_indegree=5, card=(6, 10))
+    cols, card = O.relabel(raw)
+    ref = O.pc_skeleton(cols, card, threads=16)
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    with F.Engine(0) as e:
+        e.upload(raw)
+        for _ in range(3):
+            st = e.pc_skeleton().to_dict()
+            res = e.result()
+            assert np.array_equal(res["adj"], ref["adj"]) and res["sepsets"] == ref["sepsets"]
+            assert st["tests"] == ref["stats"]["tests"]
