@@ -53,7 +53,69 @@ struct WideTest {
     int32_t pcnt[kPartMax];      // records per partition
     int32_t poff[kPartMax + 1];  // first record of each partition (runs padded to 8 records)
     int32_t sp[kPartMax + 1];    // super-partitions (queue items): partitions sp[i] .. sp[i + 1] - 1
+    uint32_t *bmw;               // the test's contributing-sample bitmap being written (null: none)
+    int32_t bm_slot, bm_bad;     // its pool slot; set when a partition could not write it
 };
+
+// Contributing-sample bitmaps.  A stratum adds a degree of freedom and a G^2 term only when
+// its samples take at least two values of x and at least two of y; every other stratum adds
+// exactly zero, and so does every stratum that refines it.  A test (x, y | Z) counted by the
+// partition kernels records, one bit per sample, which samples lie in strata that do add
+// something; at the next level the test (x, y | Z + v), whose strata refine those of Z (v
+// past Z's last variable), counts only those samples.  An edge that reaches a level ran every
+// test of the level before, so the parent exists whenever the edge is still tested; it has a
+// bitmap when the partition kernels counted it in full (no partition from global memory).
+// Tests are keyed by (min(x, y), max(x, y), Z ascending).
+struct LiveKey {
+    unsigned long long h;      // 0: empty; else the key's hash (never 0)
+    int32_t slot;              // bitmap in the pool
+    int32_t nz;                // |Z|
+    uint16_t v[2 + kMaxCond];  // min(x, y), max(x, y), Z ascending
+};
+__device__ inline unsigned long long live_hash(const uint16_t *v, int n) {
+    unsigned long long h = 0x9E3779B97F4A7C15ull ^ (unsigned long long)n;
+    for (int i = 0; i < n; ++i) {
+        h = (h ^ v[i]) * 0x100000001B3ull;
+        h ^= h >> 29;
+    }
+    return h | 1ull;
+}
+// key of a test from its item variables (z1 .. zd ascending, x, y), its first nz Z variables
+__device__ inline int live_key(const uint16_t *iv, int d, int nz, uint16_t *v) {
+    const uint16_t x = iv[d], y = iv[d + 1];
+    v[0] = x < y ? x : y;
+    v[1] = x < y ? y : x;
+    for (int k = 0; k < nz; ++k) v[2 + k] = iv[k];
+    return nz + 2;
+}
+__device__ inline void live_insert(LiveKey *tab, int cap, const uint16_t *v, int n, int slot) {
+    const unsigned long long h = live_hash(v, n);
+    uint32_t i = (uint32_t)(h >> 7) & (uint32_t)(cap - 1);
+    for (int p = 0; p < cap; ++p) {
+        if (atomicCAS(&tab[i].h, 0ull, h) == 0ull) {
+            tab[i].slot = slot;
+            tab[i].nz = n - 2;
+            for (int k = 0; k < n; ++k) tab[i].v[k] = v[k];
+            return;
+        }
+        i = (i + 1) & (uint32_t)(cap - 1);
+    }
+}
+__device__ inline int live_find(const LiveKey *tab, int cap, const uint16_t *v, int n) {
+    const unsigned long long h = live_hash(v, n);
+    uint32_t i = (uint32_t)(h >> 7) & (uint32_t)(cap - 1);
+    for (int p = 0; p < cap; ++p) {
+        const unsigned long long e = tab[i].h;
+        if (e == 0ull) return -1;
+        if (e == h && tab[i].nz == n - 2) {
+            bool eq = true;
+            for (int k = 0; k < n && eq; ++k) eq = tab[i].v[k] == v[k];
+            if (eq) return tab[i].slot;
+        }
+        i = (i + 1) & (uint32_t)(cap - 1);
+    }
+    return -1;
+}
 
 struct WaveArgs {
     const uint8_t *cols;
@@ -114,6 +176,17 @@ struct WaveArgs {
     int32_t warp_ints;             // ints of the warp tier's per-warp slice (its table limit)
     int32_t dense_rows;            // compact kernel's dense strata table: a thread per stratum (else lane groups)
     int32_t stage_rec;             // records staged in shared memory at most (0: as many as fit; tests lower it)
+    // contributing-sample bitmaps (null: off): written by this level's partition-path tests
+    // into bm_pool (bm_cap bitmaps of bm_words words, keys in bm_tab), read from the previous
+    // level's (bm_prev_*)
+    uint32_t *bm_pool;
+    LiveKey *bm_tab;
+    int32_t *bm_count;
+    int32_t bm_cap, bm_tab_cap, bm_words;
+    const uint32_t *bm_prev_pool;
+    const LiveKey *bm_prev_tab;
+    int32_t bm_prev_tab_cap;
+    unsigned long long *live_stat;  // [0] samples in contributing strata, [1] samples scored (partition path)
     int64_t part_min_samples;
 };
 
@@ -590,7 +663,7 @@ __device__ __forceinline__ void zcodes16(K (&z)[16], const uint8_t *const *col, 
 
 // Byte offsets of one compact-tier global slot, every region 256-byte aligned.
 struct SlotLayout {
-    int64_t keys, zk, ids, cnt, cur, sid, wt, ord, tab, total;
+    int64_t keys, zk, ids, cnt, cur, sid, wt, ord, tab, rs, total;
 };
 __host__ __device__ inline int64_t align256(int64_t x) { return (x + 255) & ~(int64_t)255; }
 __host__ __device__ inline SlotLayout slot_layout(int64_t S, int64_t cap) {
@@ -605,6 +678,7 @@ __host__ __device__ inline SlotLayout slot_layout(int64_t S, int64_t cap) {
     L.wt = o;   o = align256(o + (int64_t)kWarps * kGlobalWarpTab * 4);  // wide x,y tables, kept zeroed
     L.ord = o;  o = align256(o + (S + 2048) * 2);  // (x << 8) | y codes sorted by stratum (+ partition padding)
     L.tab = o;  o = align256(o + ((int64_t)kDenseMul * S + 64) * 4);  // dense strata x cells counts, kept zeroed
+    L.rs = o;   o = align256(o + (S + 2048) * 4);  // partition records: sample index (contributing-sample bitmaps)
     L.total = o;
     return L;
 }
@@ -674,9 +748,11 @@ struct TermAcc {
 
 // Strata of at most kLaneStratum samples, one thread each, pairwise in registers.
 // Larger strata are appended to big[] when collect.
+// live (optional): live[k] = 1 when stratum k has two or more values of x and of y.
 template <bool kFp64>
 __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gord, int n_obs, int dx, int dy, int *big,
-                                             int *n_big, const uint64_t *gzk, bool want_hash, bool collect) {
+                                             int *n_big, const uint64_t *gzk, bool want_hash, bool collect,
+                                             uint8_t *live = nullptr) {
     Partial acc{0, 0.0, 0.0, 0.0, 0ull};
     TermAcc<kFp64> ta;
     for (int k = threadIdx.x; k < n_obs; k += kThreads) {
@@ -690,11 +766,13 @@ __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gor
             // two samples add one degree of freedom and two cells of 2 ln 2 when they differ in
             // both x and y, and nothing otherwise
             const uint32_t dif = (uint32_t)gord[o0] ^ (uint32_t)gord[o0 + 1];
-            if ((dif >> 8) != 0 && (dif & 0xffu) != 0) {
+            const bool both = (dif >> 8) != 0 && (dif & 0xffu) != 0;
+            if (both) {
                 acc.df += 1;
                 ta.add(1, 1, 1, 2);
                 ta.add(1, 1, 1, 2);
             }
+            if (live) live[k] = both;
             continue;
         }
         // one register per sample: (x << 8) | y; equal cells <=> equal words
@@ -731,6 +809,7 @@ __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gor
             }
         }
         acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
+        if (live) live[k] = ax >= 2 && ay >= 2;
     }
     ta.into(acc);
     return acc;
@@ -743,7 +822,7 @@ __device__ inline Partial score_small_strata(const int *cnt, const uint16_t *gor
 template <bool kFp64>
 __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const uint16_t *gord, const int *big, int n_big,
                                            int dx, int dy, int *wt, const uint64_t *gzk, bool want_hash,
-                                           int k_first = 0) {
+                                           int k_first = 0, uint8_t *live = nullptr) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int dxy = dx * dy;
@@ -846,7 +925,10 @@ __device__ inline Partial score_big_strata(Partial acc, const int *cnt, const ui
             }
         }
         __syncwarp();
-        if (lane == 0) acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
+        if (lane == 0) {
+            acc.df += (long long)(max(ax, 1) - 1) * (max(ay, 1) - 1);
+            if (live) live[k] = ax >= 2 && ay >= 2;
+        }
         k = kn;
         m = mn;
         o0 = on;
@@ -1081,18 +1163,25 @@ __device__ __forceinline__ void load8(K (&z)[8], const K *src) {
 // chunk's records by partition in shared memory (smem, dead at this point) and copies each
 // partition's run out to consecutive records, so the global stores are coalesced.
 constexpr int kScatterChunk = kThreads * 16;
+// bmr (optional): the parent test's contributing-sample bitmap; samples whose bit is clear get
+// no record.  rec_s (optional): each record's sample index, written beside its code.
 template <class K>
 __device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint32_t *dim, int d, int64_t S, int lp,
                                           K *rec_z, uint16_t *rec_xy, int *s_pcnt, int *s_poff, int *s_pcur, K *zbuf,
-                                          unsigned char *smem) {
+                                          unsigned char *smem, const uint32_t *bmr, uint32_t *rec_s) {
     const int tid = threadIdx.x, P = 1 << lp;
     const int64_t nvec = S >> 4;
     const uint8_t *colx = col[d], *coly = col[d + 1];
     K *cz = reinterpret_cast<K *>(smem);
     uint16_t *cxy = reinterpret_cast<uint16_t *>(smem + kScatterChunk * sizeof(K));
     uint8_t *cp = reinterpret_cast<uint8_t *>(smem + kScatterChunk * (sizeof(K) + 2));
-    int *lcnt = reinterpret_cast<int *>(smem + kScatterChunk * (sizeof(K) + 3));
-    int *lstart = lcnt + kPartMax, *gbase = lstart + kPartMax;
+    uint32_t *cs = reinterpret_cast<uint32_t *>(smem + kScatterChunk * (sizeof(K) + 3));
+    int *lcnt = reinterpret_cast<int *>(smem + kScatterChunk * (sizeof(K) + 7));
+    int *lstart = lcnt + kPartMax, *gbase = lstart + kPartMax, *s_ctot = gbase + kPartMax;
+    auto live16 = [&](int64_t v) -> uint32_t {
+        return bmr ? (__ldcg(bmr + (v >> 1)) >> (16 * (int)(v & 1))) & 0xffffu : 0xffffu;
+    };
+    auto live1 = [&](int64_t s) -> bool { return !bmr || ((__ldcg(bmr + (s >> 5)) >> (int)(s & 31)) & 1u); };
     for (int i = tid; i < P; i += kThreads) s_pcnt[i] = 0;
     __syncthreads();
     for (int64_t v = tid; v < nvec; v += kThreads) {
@@ -1108,14 +1197,15 @@ __device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint3
                 dst[q] = make_uint4((uint32_t)z[2 * q], (uint32_t)(z[2 * q] >> 32), (uint32_t)z[2 * q + 1],
                                     (uint32_t)(z[2 * q + 1] >> 32));
         }
+        const uint32_t lv = live16(v);
 #pragma unroll
-        for (int b = 0; b < 16; ++b) atomicAdd(&s_pcnt[part_of(z[b], lp)], 1);
+        for (int b = 0; b < 16; ++b) atomicAdd(&s_pcnt[part_of(z[b], lp)], (int)((lv >> b) & 1u));  // no branch
     }
     for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
         K z = 0;
         for (int j = 0; j < d; ++j) z = z * (K)dim[j] + col[j][s];
         zbuf[s] = z;
-        atomicAdd(&s_pcnt[part_of(z, lp)], 1);
+        if (live1(s)) atomicAdd(&s_pcnt[part_of(z, lp)], 1);
     }
     __syncthreads();
     if (tid < 32) {  // padded exclusive scan, eight partitions per lane at most
@@ -1175,8 +1265,12 @@ __device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint3
             const uint4 wy = __ldg(reinterpret_cast<const uint4 *>(coly) + v);
             xx[0] = wx.x; xx[1] = wx.y; xx[2] = wx.z; xx[3] = wx.w;
             yy[0] = wy.x; yy[1] = wy.y; yy[2] = wy.z; yy[3] = wy.w;
+            const uint32_t lv = live16(v);
 #pragma unroll
-            for (int b = 0; b < 16; ++b) rk[b] = atomicAdd(&lcnt[part_of(z[b], lp)], 1);
+            for (int b = 0; b < 16; ++b) {  // no branch: a left-out sample adds 0 and keeps no rank
+                rk[b] = atomicAdd(&lcnt[part_of(z[b], lp)], (int)((lv >> b) & 1u));
+                if (!((lv >> b) & 1u)) rk[b] = -1;
+            }
         }
         __syncthreads();
         if (tid < 32) {  // chunk offsets per partition, and each run's place in the records
@@ -1201,33 +1295,38 @@ __device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint3
                     run += lcnt[p];
                 }
             }
+            if (tid == 31) *s_ctot = incl;  // records of this chunk
         }
         __syncthreads();
         if (have) {
 #pragma unroll
             for (int b = 0; b < 16; ++b) {
+                if (rk[b] < 0) continue;
                 const int p = part_of(z[b], lp), pos = lstart[p] + rk[b], sh = 8 * (b & 3);
                 cz[pos] = z[b];
                 cxy[pos] = (uint16_t)((((xx[b >> 2] >> sh) & 0xffu) << 8) | ((yy[b >> 2] >> sh) & 0xffu));
                 cp[pos] = (uint8_t)p;
+                if (rec_s) cs[pos] = (uint32_t)(16 * v + b);
             }
         }
         __syncthreads();
-        const int64_t left = 16 * (nvec - c * kThreads);
-        const int n_in = left < kScatterChunk ? (int)left : kScatterChunk;
+        const int n_in = *s_ctot;
         for (int i = tid; i < n_in; i += kThreads) {
             const int p = cp[i];
             const int g = gbase[p] + (i - lstart[p]);
             rec_z[g] = cz[i];
             rec_xy[g] = cxy[i];
+            if (rec_s) rec_s[g] = cs[i];
         }
         __syncthreads();
     }
     for (int64_t s = (S & ~(int64_t)15) + tid; s < S; s += kThreads) {
+        if (!live1(s)) continue;
         const K z = zbuf[s];
         const int pos = atomicAdd(&s_pcur[part_of(z, lp)], 1);
         rec_z[pos] = z;
         rec_xy[pos] = (uint16_t)((colx[s] << 8) | coly[s]);
+        if (rec_s) rec_s[pos] = (uint32_t)s;
     }
     // padding records carry the empty key (never a stratum code), so a run of partitions
     // can be read as one
@@ -1235,7 +1334,7 @@ __device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint3
         for (int i = s_poff[p] + s_pcnt[p]; i < s_poff[p + 1]; ++i) rec_z[i] = (K)kEmptyKey;
     __syncthreads();
 }
-static_assert(kScatterChunk * (8 + 3) + 3 * kPartMax * 4 <= kSmemBytes, "scatter chunk in shared memory");
+static_assert(kScatterChunk * (8 + 7) + 3 * kPartMax * 4 + 4 <= kSmemBytes, "scatter chunk in shared memory");
 
 // Counts and scores one partition (n records from rec_z/rec_xy + base) in shared memory;
 // returns this thread's share of the statistic.  *s_over is set when the partition's codes
@@ -1403,6 +1502,7 @@ struct StagePlan {
     static constexpr int rec = (kSmemBytes - rec_off) / ((int)sizeof(K) + 2) / 8 * 8;  // records at most
     static constexpr int xy_off = rec_off + rec * (int)sizeof(K);
     static constexpr int wtab = (rec * ((int)sizeof(K) + 2)) / 4 / kWarps;  // ints per warp over the records
+    static constexpr int wtab_z = rec * (int)sizeof(K) / 4 / kWarps;         // ... over the codes alone
 };
 static_assert(StagePlan<uint32_t>::rec * 2 <= StagePlan<uint32_t>::a_off, "sorted codes over the u32 keys");
 static_assert(StagePlan<uint64_t>::rec * 2 <= StagePlan<uint64_t>::a_off, "sorted codes over the u64 keys");
@@ -1448,6 +1548,10 @@ __device__ __forceinline__ void slot_store8(K *dst, const int (&sl)[8]) {
     }
 }
 template <class K>
+__device__ __forceinline__ int stage_slot(const K *zr, int i) {
+    return reinterpret_cast<const int *>(zr)[i * (int)(sizeof(K) / 4)];
+}
+template <class K>
 __device__ __forceinline__ void slot_load8(int (&sl)[8], const K *src) {
     const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
     if constexpr (sizeof(K) == 4) {
@@ -1468,11 +1572,16 @@ __device__ __forceinline__ void slot_load8(int (&sl)[8], const K *src) {
 // memory; n <= StagePlan<K>::rec.  As part_partition: *s_over is set when the strata
 // overflow the table (first pass only), claims gets the strata seen, and it ends on a
 // barrier.  s_bin: 16 ints of shared scratch.
+// bmw / rec_s (optional, first pass only): the test's contributing-sample bitmap, set here for
+// the samples of strata with two or more values of x and of y, and the records' sample
+// indices (the per-warp x,y tables then live in global memory, so the records' slots survive
+// the scoring).
 template <bool kFp64, class K>
 __device__ __noinline__ Partial part_staged(int lp, const K *rec_z, const uint16_t *rec_xy, int base, int n, int dx,
                                             int dy, unsigned char *smem, int *gwt, uint64_t *gzk, bool want_hash,
                                             int *s_w, int *s_over, int *s_nocc, int *s_bin, int &claims,
-                                            unsigned long long *dbg) {
+                                            unsigned long long *dbg, uint32_t *bmw = nullptr,
+                                            const uint32_t *rec_s = nullptr, unsigned long long *lstat = nullptr) {
     using Plan = StagePlan<K>;
     constexpr uint32_t cap = Plan::cap;
     const unsigned full = 0xffffffffu;
@@ -1485,9 +1594,15 @@ __device__ __noinline__ Partial part_staged(int lp, const K *rec_z, const uint16
     uint16_t *xyr = reinterpret_cast<uint16_t *>(smem + Plan::xy_off);
     uint16_t *sorted = reinterpret_cast<uint16_t *>(smem);  // over the keys once they are dead
     const int dxy = dx * dy;
-    const bool wsmem = dxy + dx + dy <= Plan::wtab;
-    int *wt = wsmem ? reinterpret_cast<int *>(smem + Plan::rec_off) + warp * Plan::wtab
+    const bool bits = !kFp64 && bmw != nullptr;
+    // with a bitmap to write, the records' ranks are kept over their x,y codes, so the per-warp
+    // tables use the codes' part of the records region only
+    const int wtab = bits ? Plan::wtab_z : Plan::wtab;
+    const bool wsmem = dxy + dx + dy <= wtab;
+    int *wt = wsmem ? reinterpret_cast<int *>(smem + Plan::rec_off) + warp * wtab
                     : gwt + (int64_t)warp * kGlobalWarpTab;
+    uint8_t *live = (bits || (!kFp64 && lstat)) ? reinterpret_cast<uint8_t *>(occ) : nullptr;  // per ranked stratum
+                                                                                        // (occ is dead then)
     const int max_probe = kFp64 ? (int)cap : kPartProbe;
     const K empty = (K)kEmptyKey;
     Partial acc{0, 0.0, 0.0, 0.0, 0ull};
@@ -1677,15 +1792,22 @@ __device__ __noinline__ Partial part_staged(int lp, const K *rec_z, const uint16
 #pragma unroll
                 for (int j = 0; j < 8; ++j)
                     if (r[j] >= 0) sorted[atomicAdd(&E[1 + r[j]], 1)] = (uint16_t)(cw[j >> 1] >> (16 * (j & 1)));
+                if (bits)  // each record's rank (0xffff: not scored) over its dead x,y code
+                    reinterpret_cast<uint4 *>(xyr)[g] =
+                        make_uint4(((uint32_t)r[0] & 0xffffu) | ((uint32_t)r[1] << 16),
+                                   ((uint32_t)r[2] & 0xffffu) | ((uint32_t)r[3] << 16),
+                                   ((uint32_t)r[4] & 0xffffu) | ((uint32_t)r[5] << 16),
+                                   ((uint32_t)r[6] & 0xffffu) | ((uint32_t)r[7] << 16));
             }
         }
         __syncthreads();
         if (wsmem)  // the records are dead: per-warp x,y tables
-            for (int i = tid; i < kWarps * Plan::wtab; i += kThreads)
+            for (int i = tid; i < kWarps * wtab; i += kThreads)
                 reinterpret_cast<int *>(smem + Plan::rec_off)[i] = 0;
         __syncthreads();
         lap(19);
-        Partial q = score_small_strata<kFp64>(E, sorted, first_big, dx, dy, nullptr, nullptr, gzk, want_hash, false);
+        Partial q = score_small_strata<kFp64>(E, sorted, first_big, dx, dy, nullptr, nullptr, gzk, want_hash, false,
+                                              live);
         if (dbg) {
             __syncthreads();
             lap(20);
@@ -1696,7 +1818,25 @@ __device__ __noinline__ Partial part_staged(int lp, const K *rec_z, const uint16
             }
         }
         acc = score_big_strata<kFp64>(q, E, sorted, nullptr, n_live - first_big, dx, dy, wt, gzk, want_hash,
-                                      first_big);
+                                      first_big, live);
+        if (live && lstat) {  // how many of the scored samples lie in contributing strata
+            __syncthreads();
+            unsigned long long in = 0;
+            for (int k = tid; k < n_live; k += kThreads)
+                if (live[k]) in += (unsigned long long)(E[k + 1] - E[k]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) in += __shfl_xor_sync(full, in, o);
+            if (lane == 0 && in) atomicAdd(&lstat[0], in);
+        }
+        if (bits) {  // the samples of contributing strata into the test's bitmap
+            __syncthreads();
+            for (int i = tid; i < n; i += kThreads) {
+                const uint32_t r = xyr[i];
+                if (r == 0xffffu || !live[r]) continue;
+                const uint32_t si = __ldcg(rec_s + base + i);
+                atomicOr(&bmw[si >> 5], 1u << (si & 31));
+            }
+        }
     }
     __syncthreads();  // before the next super-partition reuses shared memory
     lap(21);
@@ -1728,13 +1868,15 @@ template <bool kFp64, class K>
 __device__ inline Partial part_super(int lp, const K *rec_z, const uint16_t *rec_xy, const int *pcnt, const int *poff,
                                      int b0, int b1, int dx, int dy, unsigned char *smem, uint16_t *gord, int *gwt,
                                      uint64_t *gzk, bool want_hash, int *s_w, int *s_over, int *s_nbig, int *s_nocc,
-                                     int *s_bin, int &claims, int rstage, unsigned long long *dbg = nullptr) {
+                                     int *s_bin, int &claims, int rstage, unsigned long long *dbg = nullptr,
+                                     uint32_t *bmw = nullptr, const uint32_t *rec_s = nullptr,
+                                     int *s_bmbad = nullptr, unsigned long long *lstat = nullptr) {
     const int R = rstage > 0 && rstage < StagePlan<K>::rec ? rstage : StagePlan<K>::rec;
     const int n = poff[b1] - poff[b0];
     if (n == 0) return Partial{0, 0.0, 0.0, 0.0, 0ull};
     if (n <= R) {
         const Partial q = part_staged<kFp64, K>(lp, rec_z, rec_xy, poff[b0], n, dx, dy, smem, gwt, gzk, want_hash, s_w,
-                                                s_over, s_nocc, s_bin, claims, dbg);
+                                                s_over, s_nocc, s_bin, claims, dbg, bmw, rec_s, lstat);
         if (*s_over == 0 || b1 - b0 == 1) return q;  // read after part_staged's closing barrier
         __syncthreads();  // every thread has read s_over
         if (threadIdx.x == 0) {
@@ -1747,9 +1889,10 @@ __device__ inline Partial part_super(int lp, const K *rec_z, const uint16_t *rec
     for (int b = b0; b < b1; ++b) {
         if (pcnt[b] == 0) continue;
         const int nb = poff[b + 1] - poff[b];
+        if (nb > R && bmw && s_bmbad && threadIdx.x == 0) *s_bmbad = 1;  // counted unstaged: no bitmap
         const Partial q =
             nb <= R ? part_staged<kFp64, K>(lp, rec_z, rec_xy, poff[b], nb, dx, dy, smem, gwt, gzk, want_hash, s_w,
-                                            s_over, s_nocc, s_bin, claims, dbg)
+                                            s_over, s_nocc, s_bin, claims, dbg, bmw, rec_s, lstat)
                     : part_partition<kFp64, K>(lp, rec_z, rec_xy, pcnt[b], poff[b], dx, dy, smem, gord, gwt, gzk,
                                                want_hash, s_w, s_over, s_nbig, s_nocc, s_bin, claims, dbg);
         if (*s_over) return acc;
@@ -1767,13 +1910,15 @@ __device__ __noinline__ Partial part_run(int lp, const K *rec_z, const uint16_t 
                                          const int *s_poff, const int *sp, int n_sp, int dx, int dy,
                                          unsigned char *smem, uint16_t *gord, int *gwt, uint64_t *gzk, bool want_hash,
                                          int *s_w, int *s_over, int *s_nbig, int *s_nocc, int *s_bin, int &claims,
-                                         int rstage, unsigned long long *dbg) {
+                                         int rstage, unsigned long long *dbg, uint32_t *bmw = nullptr,
+                                         const uint32_t *rec_s = nullptr, int *s_bmbad = nullptr,
+                                         unsigned long long *lstat = nullptr) {
     Partial acc{0, 0.0, 0.0, 0.0, 0ull};
     if (dbg && threadIdx.x == 0) atomicAdd(&dbg[22], (unsigned long long)n_sp);
     for (int i = 0; i < n_sp; ++i) {
         const Partial q = part_super<kFp64, K>(lp, rec_z, rec_xy, s_pcnt, s_poff, sp[i], sp[i + 1], dx, dy, smem, gord,
                                                gwt, gzk, want_hash, s_w, s_over, s_nbig, s_nocc, s_bin, claims, rstage,
-                                               dbg);
+                                               dbg, bmw, rec_s, s_bmbad, lstat);
         if (*s_over) break;  // read after part_super's closing barrier, same in every thread
         partial_add(acc, q);
     }
@@ -2234,11 +2379,15 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
     __shared__ int s_w[kWarps];
     __shared__ Partial scratch[kWarps];
     __shared__ int s_pcnt[kPartMax], s_poff[kPartMax + 1], s_pcur[kPartMax], s_sp[kPartMax + 1], s_nsp;
+    __shared__ const uint32_t *s_bmr;  // parent's contributing-sample bitmap (null: every sample)
+    __shared__ uint32_t *s_bmw;        // this test's, being written (null: none)
+    __shared__ int s_bmslot, s_bmbad;
     const int tid = threadIdx.x;
     char *slot = a.slot_mem + (int64_t)blockIdx.x * a.slot_bytes;
     const SlotLayout L = slot_layout(a.slot_S, (uint32_t)a.hash_cap_global);
     char *rz = slot + L.keys;  // record codes (u32 or u64), S + padding
     uint16_t *rxy = reinterpret_cast<uint16_t *>(slot + L.ids);  // record (x << 8) | y
+    uint32_t *rs = reinterpret_cast<uint32_t *>(slot + L.rs);    // record sample index (bitmaps only)
     uint64_t *gzk = reinterpret_cast<uint64_t *>(slot + L.zk);
     int *gwt = reinterpret_cast<int *>(slot + L.wt);
     uint16_t *gord = reinterpret_cast<uint16_t *>(slot + L.ord);
@@ -2269,7 +2418,29 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
             s_dim[tid] = a.card[var];
             s_col[tid] = a.cols + a.var_off[var];
         }
+        if (tid == 0) {  // contributing-sample bitmaps: the parent's (Z minus its last variable), and one to write
+            s_bmr = nullptr;
+            s_bmw = nullptr;
+            s_bmslot = -1;
+            s_bmbad = 0;
+            if (a.bm_prev_tab && d >= 1) {
+                uint16_t v[2 + kMaxCond];
+                const int nv = live_key(a.item_vars + (int64_t)item * ncols, d, d - 1, v);
+                const int sl = live_find(a.bm_prev_tab, a.bm_prev_tab_cap, v, nv);
+                if (sl >= 0) s_bmr = a.bm_prev_pool + (int64_t)sl * a.bm_words;
+            }
+            if (a.bm_pool) {
+                const int sl = atomicAdd(a.bm_count, 1);
+                if (sl < a.bm_cap) {
+                    s_bmslot = sl;
+                    s_bmw = a.bm_pool + (int64_t)sl * a.bm_words;
+                }
+            }
+            if (a.live_stat) atomicAdd(&a.live_stat[1], (unsigned long long)S);  // the test's samples
+        }
         __syncthreads();
+        if (s_bmw)  // cleared before any bit is set (part_scatter's barriers come first)
+            for (int64_t i = tid; i < ((S + 31) >> 5); i += kThreads) s_bmw[i] = 0u;
         uint64_t dz = 1;
         for (int j = 0; j < d; ++j) dz *= s_dim[j];
         const bool code32 = dz <= 0xFFFFFFFFull;
@@ -2299,10 +2470,10 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
             while ((S >> lw) > rw / 4 && lw < maxlog) ++lw;
             if (code32)
                 part_scatter(s_col, s_dim, d, S, lw, reinterpret_cast<uint32_t *>(rz), rxy, s_pcnt, s_poff, s_pcur,
-                             reinterpret_cast<uint32_t *>(gzk), smem_raw);
+                             reinterpret_cast<uint32_t *>(gzk), smem_raw, s_bmr, s_bmw ? rs : nullptr);
             else
                 part_scatter(s_col, s_dim, d, S, lw, reinterpret_cast<uint64_t *>(rz), rxy, s_pcnt, s_poff, s_pcur,
-                             reinterpret_cast<uint64_t *>(gzk), smem_raw);
+                             reinterpret_cast<uint64_t *>(gzk), smem_raw, s_bmr, s_bmw ? rs : nullptr);
             FPGM_PHASE(14);
             if (tid == 0) s_idx = atomicAdd(&a.counters[C_WIDET], 1);
             __syncthreads();
@@ -2314,7 +2485,10 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
             }
             if (tid == 0) {
                 w->poff[P] = s_poff[P];
-                const int nne = plan_super(s_pcnt, P, rw, w->sp);
+                int kept = 0;  // as in the per-CTA path: fewer records per super-partition with a bitmap
+                for (int i = 0; i < P; ++i) kept += s_pcnt[i];
+                int rk = (int)fmin((double)rw, 0.7 * lim * (double)kept / fmax(est, 1.0)) & ~7;
+                const int nne = plan_super(s_pcnt, P, rk < 64 ? 64 : rk, w->sp);
                 w->item = item;
                 w->owner = blockIdx.x;
                 w->lp = lw;
@@ -2330,6 +2504,9 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
                 w->err = 0.0;
                 w->abs_g2 = 0.0;
                 w->hash = 0ull;
+                w->bmw = s_bmw;
+                w->bm_slot = s_bmslot;
+                w->bm_bad = 0;
                 const int q0 = atomicAdd(&a.counters[C_WIDEQ], nne);
                 for (int i = 0; i < nne; ++i) a.wide_items[q0 + i] = (s_idx << 8) | i;
                 if (a.dbg) atomicAdd(&a.dbg[23], 1ull);
@@ -2347,21 +2524,34 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
             int claims = 0;
             if (code32)
                 part_scatter(s_col, s_dim, d, S, lp, reinterpret_cast<uint32_t *>(rz), rxy, s_pcnt, s_poff, s_pcur,
-                             reinterpret_cast<uint32_t *>(gzk), smem_raw);
+                             reinterpret_cast<uint32_t *>(gzk), smem_raw, s_bmr, s_bmw ? rs : nullptr);
             else
                 part_scatter(s_col, s_dim, d, S, lp, reinterpret_cast<uint64_t *>(rz), rxy, s_pcnt, s_poff, s_pcur,
-                             reinterpret_cast<uint64_t *>(gzk), smem_raw);
-            if (tid == 0) s_nsp = plan_super(s_pcnt, 1 << lp, rmax, s_sp);
+                             reinterpret_cast<uint64_t *>(gzk), smem_raw, s_bmr, s_bmw ? rs : nullptr);
+            if (tid == 0) {
+                // strata are at most est whichever samples were kept: with a parent's bitmap, as
+                // many strata fall on fewer records, so the super-partitions hold fewer records
+                int kept = 0;
+                for (int i = 0; i < (1 << lp); ++i) kept += s_pcnt[i];
+                int rk = (int)fmin((double)rmax, 0.7 * lim * (double)kept / fmax(est, 1.0)) & ~7;
+                s_nsp = plan_super(s_pcnt, 1 << lp, rk < 64 ? 64 : rk, s_sp);
+                if (a.dbg) {  // contributing-sample bitmaps: tests with a parent's, samples, records kept
+                    atomicAdd(&a.dbg[28], s_bmr ? 1ull : 0ull);
+                    atomicAdd(&a.dbg[29], (unsigned long long)S);
+                    atomicAdd(&a.dbg[30], (unsigned long long)kept);
+                    atomicAdd(&a.dbg[31], s_bmw ? 1ull : 0ull);
+                }
+            }
             __syncthreads();
             FPGM_PHASE(14);
             if (code32)
                 acc = part_run<false>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, s_pcnt, s_poff, s_sp, s_nsp, dx,
                                       dy, smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
-                                      s_bin, claims, a.stage_rec, a.dbg);
+                                      s_bin, claims, a.stage_rec, a.dbg, s_bmw, rs, &s_bmbad, a.live_stat);
             else
                 acc = part_run<false>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, s_pcnt, s_poff, s_sp, s_nsp, dx,
                                       dy, smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
-                                      s_bin, claims, a.stage_rec, a.dbg);
+                                      s_bin, claims, a.stage_rec, a.dbg, s_bmw, rs, &s_bmbad, a.live_stat);
             atomicAdd(&s_distinct, claims);
             __syncthreads();
             over = s_over != 0;
@@ -2391,6 +2581,11 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
                                                s_nsp, dx, dy, smem_raw, gord, gwt, nullptr, false, s_w, &s_over,
                                                &s_nbig, &s_nocc, s_bin, claims, a.stage_rec, nullptr);
             });
+            if (tid == 0 && s_bmw && !s_bmbad) {  // the bitmap is complete: the next level may use it
+                uint16_t v[2 + kMaxCond];
+                const int nv = live_key(a.item_vars + (int64_t)item * ncols, d, d, v);
+                live_insert(a.bm_tab, a.bm_tab_cap, v, nv, s_bmslot);
+            }
         }
         if (tid == 0 && a.tune_obs && !a.tune) {  // the partition path's time for the online autotuner
             const int b = tune_index(S, d, (double)dz * dx * dy);
@@ -2411,7 +2606,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
 // test to the compact kernel's global hash (retry list, ci_compact_kernel<true>).
 __global__ void __launch_bounds__(kThreads, 2) ci_part_wide_kernel(WaveArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ int s_idx, s_over, s_flag, s_nbig, s_nocc, s_last;
+    __shared__ int s_idx, s_over, s_flag, s_nbig, s_nocc, s_last, s_bmbad;
     __shared__ int s_bin[16];
     __shared__ int s_w[kWarps];
     __shared__ Partial scratch[kWarps];
@@ -2435,23 +2630,29 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_wide_kernel(WaveArgs a) {
         const char *own = a.slot_mem + (int64_t)w->owner * a.slot_bytes;
         const char *rz = own + L.keys;
         const uint16_t *rxy = reinterpret_cast<const uint16_t *>(own + L.ids);
+        const uint32_t *rs = reinterpret_cast<const uint32_t *>(own + L.rs);
         const int lp = w->lp, dx = w->dx, dy = w->dy;
         const bool code32 = w->code32 != 0;
-        if (tid == 0) s_over = 0;
+        uint32_t *bmw = w->bmw;
+        if (tid == 0) {
+            s_over = 0;
+            s_bmbad = 0;
+        }
         __syncthreads();
         int claims = 0;
         const Partial q =
             code32 ? part_super<false, uint32_t>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, w->pcnt, w->poff,
                                                  w->sp[p], w->sp[p + 1], dx, dy, smem_raw, gord, gwt, zk,
                                                  a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc, s_bin, claims,
-                                                 a.stage_rec)
+                                                 a.stage_rec, nullptr, bmw, rs, &s_bmbad, a.live_stat)
                    : part_super<false, uint64_t>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, w->pcnt, w->poff,
                                                  w->sp[p], w->sp[p + 1], dx, dy, smem_raw, gord, gwt, zk,
                                                  a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc, s_bin, claims,
-                                                 a.stage_rec);
+                                                 a.stage_rec, nullptr, bmw, rs, &s_bmbad, a.live_stat);
         const bool over = s_over != 0;  // read after part_super's closing barrier
         const Partial r = block_sum(q, scratch);
         if (tid == 0) {
+            if (s_bmbad) atomicExch(&w->bm_bad, 1);
             if (over) {
                 atomicExch(&w->over, 1);
             } else {
@@ -2495,6 +2696,11 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_wide_kernel(WaveArgs a) {
                                                    w->sp, w->n_items, dx, dy, smem_raw, gord, gwt, nullptr, false, s_w,
                                                    &s_over, &s_nbig, &s_nocc, s_bin, cl, a.stage_rec, nullptr);
                 });
+                if (tid == 0 && bmw && !__ldcg(&w->bm_bad)) {  // complete: the next level may use it
+                    uint16_t v[2 + kMaxCond];
+                    const int nv = live_key(a.item_vars + (int64_t)item * (a.d + 2), a.d, a.d, v);
+                    live_insert(a.bm_tab, a.bm_tab_cap, v, nv, w->bm_slot);
+                }
             }
         }
         __syncthreads();

@@ -192,6 +192,20 @@ struct fpgm_engine {
     DevBuf ovf;             // per bucket: how often tier-2 tests overflowed the shared strata hash
     bool ovf_on = true;     // FPGM_OVF_SKIP=0: every tier-2 test tries the shared hash first
     int stage_rec = 0;      // FPGM_STAGE_REC=n (tests): at most n records per staged super-partition
+    // contributing-sample bitmaps of the partition path (FPGM_LIVE=0: off), two pools used by
+    // alternate levels: level d writes pool d & 1 and reads pool (d - 1) & 1
+    bool live_on = true;
+    int live_min_level = 3;             // FPGM_LIVE_MIN_LEVEL: first level that writes bitmaps
+    DevBuf live_pool[2], live_tab[2], live_cnt;
+    int64_t live_cap = 0;               // bitmaps per pool
+    int32_t live_tab_cap = 0, live_words = 0;
+    int live_level[2] = {-1, -1};       // the level whose bitmaps each pool holds
+    bool live_write = false;            // this level writes (set per level)
+    bool live_in_skeleton = false;      // bitmaps are used only by a batched skeleton's waves
+    DevBuf live_stat;                   // samples in contributing strata, samples counted (partition path)
+    unsigned long long live_prev[2] = {0ull, 0ull};
+    bool live_next = false;             // the level just measured had few enough contributing samples
+    double live_frac = 0.55;            // FPGM_LIVE_FRAC: write bitmaps below this contributing fraction
     bool tune_loaded = false, tune_online = true;
     std::string tune_source;
     // result
@@ -748,6 +762,9 @@ extern "C" int fpgm_engine_create(int32_t device, fpgm_engine **out) {
     }
     if (const char *w = getenv("FPGM_OVF_SKIP")) e->ovf_on = atoi(w) != 0;
     if (const char *w = getenv("FPGM_STAGE_REC")) e->stage_rec = std::max(0, atoi(w)) & ~7;
+    if (const char *w = getenv("FPGM_LIVE")) e->live_on = atoi(w) != 0;
+    if (const char *w = getenv("FPGM_LIVE_MIN_LEVEL")) e->live_min_level = std::max(1, atoi(w));
+    if (const char *w = getenv("FPGM_LIVE_FRAC")) e->live_frac = atof(w);
     if (e->ovf_on) {
         RET(e->ovf.ensure((size_t)kTuneBuckets * 8 * 8));
         CK(cudaMemset(e->ovf.p, 0, (size_t)kTuneBuckets * 8 * 8));
@@ -770,7 +787,8 @@ extern "C" int fpgm_engine_destroy(fpgm_engine *e) {
                       &e->tests_buf, &e->detail_buf, &e->item_vars, &e->lists, &e->band,
                       &e->phase_timers, &e->var_off, &e->var_S, &e->var_lo, &e->var_hi, &e->mle_counts,
                       &e->mle_pot, &e->mle_meta, &e->wide, &e->wide_items, &e->tune, &e->wave_ctl,
-                      &e->tune_obs, &e->ovf, &e->res_adj_d, &e->res_key, &e->res_idx, &e->res_removed_d, &e->res_cnt,
+                      &e->tune_obs, &e->ovf, &e->live_pool[0], &e->live_pool[1], &e->live_tab[0], &e->live_tab[1],
+                      &e->live_cnt, &e->live_stat, &e->res_adj_d, &e->res_key, &e->res_idx, &e->res_removed_d, &e->res_cnt,
                       &e->res_vars_d};
     for (DevBuf *b : bufs) b->release();
     gram_destroy(e->gram);
@@ -934,6 +952,50 @@ int ensure_slots(fpgm_engine *e) {
     return FPGM_OK;
 }
 
+// Contributing-sample bitmaps for level d: the pools are made once (up to 32 GB or 30%
+// of the free device memory; none when that fails), the pool of this level's parity gets an
+// empty key table, and the other keeps the previous level's bitmaps for the readers.
+int live_setup(fpgm_engine *e, int d) {
+    e->live_write = false;
+    if (!e->live_on || !e->live_next || d < e->live_min_level || max_table_ints(e->h_card, d) <= kCtaInts - 64)
+        return FPGM_OK;
+    if (e->live_cap == 0) {
+        const int64_t words = (e->S + 31) / 32;
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return FPGM_OK;
+        const double budget = std::min(32.0e9, 0.3 * (double)free_b);
+        int64_t cap = (int64_t)(budget / 2.0 / (double)(words * 4));
+        cap = std::min<int64_t>(cap, (int64_t)1 << 21);
+        if (cap < 1024) {
+            e->live_on = false;
+            return FPGM_OK;
+        }
+        int32_t tcap = 1024;
+        while (tcap < 2 * cap) tcap <<= 1;
+        for (int par = 0; par < 2; ++par) {
+            if (e->live_pool[par].ensure((size_t)cap * words * 4) != FPGM_OK ||
+                e->live_tab[par].ensure((size_t)tcap * sizeof(LiveKey)) != FPGM_OK) {
+                for (int q = 0; q < 2; ++q) {
+                    e->live_pool[q].release();
+                    e->live_tab[q].release();
+                }
+                e->live_on = false;  // no room: every test counts all of its samples
+                return FPGM_OK;
+            }
+        }
+        RET(e->live_cnt.ensure(16));
+        e->live_cap = cap;
+        e->live_tab_cap = tcap;
+        e->live_words = (int32_t)words;
+    }
+    const int par = d & 1;
+    CK(cudaMemsetAsync(e->live_tab[par].p, 0, (size_t)e->live_tab_cap * sizeof(LiveKey), e->stream));
+    CK(cudaMemsetAsync(e->live_cnt.as<int32_t>() + par, 0, 4, e->stream));
+    e->live_level[par] = d;
+    e->live_write = true;
+    return FPGM_OK;
+}
+
 int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t items) {
     memset(&a, 0, sizeof a);
     a.cols = e->cols.as<uint8_t>();
@@ -974,6 +1036,23 @@ int wave_args_base(fpgm_engine *e, WaveArgs &a, double alpha, int d, int64_t ite
         a.tune_obs = (e->tune_online && !e->tune_loaded) ? e->tune_obs.as<unsigned long long>() : nullptr;
         a.ovf = e->ovf_on ? e->ovf.as<unsigned long long>() : nullptr;
         a.part_min_samples = e->part_min_samples;
+        if (e->live_on && e->live_in_skeleton && e->live_stat.p) a.live_stat = e->live_stat.as<unsigned long long>();
+        if (e->live_on && e->live_in_skeleton && e->live_cap > 0 && d >= 1) {
+            const int par = d & 1, prev = (d - 1) & 1;
+            a.bm_words = e->live_words;
+            if (e->live_write && e->live_level[par] == d) {
+                a.bm_pool = e->live_pool[par].as<uint32_t>();
+                a.bm_tab = e->live_tab[par].as<LiveKey>();
+                a.bm_count = e->live_cnt.as<int32_t>() + par;
+                a.bm_cap = (int32_t)e->live_cap;
+                a.bm_tab_cap = e->live_tab_cap;
+            }
+            if (e->live_level[prev] == d - 1) {
+                a.bm_prev_pool = e->live_pool[prev].as<uint32_t>();
+                a.bm_prev_tab = e->live_tab[prev].as<LiveKey>();
+                a.bm_prev_tab_cap = e->live_tab_cap;
+            }
+        }
     }
     a.part_max_log = e->part_max_log;
     a.warp_ints = e->warp_small ? kWarpIntsSmall : kWarpInts;
@@ -1196,6 +1275,9 @@ int run_waves_and_count(fpgm_engine *e, double alpha, int d, int64_t n_active, f
             if (h[27])
                 fprintf(stderr, "staged d=%llu records=%llu re-split=%llu big strata=%llu holding %llu samples\n",
                         (unsigned long long)d, h[27], h[24], h[25], h[26]);
+            if (h[29])
+                fprintf(stderr, "bitmaps d=%llu tests-with-parent=%llu writing=%llu samples=%llu kept=%llu (%.3f)\n",
+                        (unsigned long long)d, h[28], h[31], h[29], h[30], (double)h[30] / (double)h[29]);
             if (h[13])
                 fprintf(stderr,
                         "partitioned d=%d tests=%llu strata/test=%.0f partitions/test=%.1f us/test: records=%.1f "
@@ -1265,6 +1347,26 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
     const int64_t E = e->E;  // level-0 pairs (within each dataset)
     unsigned long long *dstat = e->stats.as<unsigned long long>();
     CK(cudaMemsetAsync(dstat, 0, ST_COUNT * 8, e->stream));
+    // bitmaps live only inside this skeleton: none carries over to a later call (the data may change)
+    struct LiveScope {
+        fpgm_engine *e;
+        explicit LiveScope(fpgm_engine *x) : e(x) {
+            e->live_level[0] = e->live_level[1] = -1;
+            e->live_write = false;
+            e->live_in_skeleton = true;
+        }
+        ~LiveScope() {
+            e->live_level[0] = e->live_level[1] = -1;
+            e->live_write = false;
+            e->live_in_skeleton = false;
+        }
+    } live_scope(e);
+    if (e->live_on) {  // contributing-sample counts, measured level by level
+        RET(e->live_stat.ensure(16));
+        CK(cudaMemsetAsync(e->live_stat.p, 0, 16, e->stream));
+        e->live_prev[0] = e->live_prev[1] = 0ull;
+        e->live_next = false;
+    }
     RET(e->bits.ensure((size_t)n * W * 4));
     init_bits_kernel<<<blocks_for((int64_t)n * W, 256), 256, 0, e->stream>>>(
         e->bits.as<uint32_t>(), n, W, e->var_lo.as<int32_t>(), e->var_hi.as<int32_t>());
@@ -1372,7 +1474,23 @@ int run_batched(fpgm_engine *e, double alpha, int depth, fpgm_pc_stats *st) {
                 }
                 gram = e->gram_ok;
             }
+            if (!gram) RET(live_setup(e, d));
             RET(run_waves_and_count(e, alpha, d, n_active, st, st->n_levels, a, gram));
+            if (e->live_on && e->live_stat.p) {
+                // Bitmaps pay for themselves when the next level can leave enough samples out:
+                // the next level writes them when this one's partition-path tests had fewer than
+                // live_frac of their samples in contributing strata (the fraction falls with |Z|).
+                unsigned long long ls[2];
+                CK(cudaMemcpyAsync(ls, e->live_stat.p, 16, cudaMemcpyDeviceToHost, e->stream));
+                CK(cudaStreamSynchronize(e->stream));
+                const unsigned long long din = ls[0] - e->live_prev[0], dall = ls[1] - e->live_prev[1];
+                e->live_prev[0] = ls[0];
+                e->live_prev[1] = ls[1];
+                e->live_next = dall > 0 && (double)din < e->live_frac * (double)dall;
+                if (e->wave_log && dall > 0)
+                    fprintf(stderr, "live level=%d contributing=%.3f wrote=%d next_writes=%d\n", d,
+                            (double)din / (double)dall, (int)e->live_write, (int)e->live_next);
+            }
         }
         // finalize: removals into the bitset and the removal log
         RET(e->log_vars.ensure((size_t)(var_count + std::max<int64_t>(n_active, 1) * std::max(d, 1)) * 4 + 16, true,

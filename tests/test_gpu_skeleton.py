@@ -366,14 +366,19 @@ def test_large_warp_slices_match_reference(monkeypatch, tmp_path, name):
     assert struct_of(tmp_path, ["V%d" % i for i in range(n)], res) == open(os.path.join(GOLDEN, name + "_struct")).read()
 
 
-@pytest.mark.parametrize("env", [{}, {"FPGM_OVF_SKIP": "0"}, {"FPGM_STAGE_REC": "64"}, {"FPGM_STAGE_REC": "1024"}])
+@pytest.mark.parametrize("env", [{}, {"FPGM_OVF_SKIP": "0"}, {"FPGM_STAGE_REC": "64"}, {"FPGM_STAGE_REC": "1024"},
+                                 {"FPGM_LIVE": "0"}, {"FPGM_LIVE_FRAC": "1.01", "FPGM_LIVE_MIN_LEVEL": "2"},
+                                 {"FPGM_LIVE_FRAC": "1.01", "FPGM_LIVE_MIN_LEVEL": "2", "FPGM_STAGE_REC": "512"}])
 def test_tier2_paths_match_oracle_over_repeated_skeletons(monkeypatch, env):
     """Tier 2 on a 70,000-sample dataset with 6-9 states, three skeletons on one engine (the
     autotuner and the shared-hash overflow record carry over from one to the next, so later
     skeletons skip the shared-hash attempt where it overflowed before): the default, the
-    attempt never skipped (FPGM_OVF_SKIP=0), and the staged super-partitions capped at 64 or
+    attempt never skipped (FPGM_OVF_SKIP=0), the staged super-partitions capped at 64 or
     1,024 records (FPGM_STAGE_REC; at 64 nearly every partition is counted from its records
-    in global memory instead).  Every skeleton equals the oracle's, test counts included."""
+    in global memory instead), no contributing-sample bitmaps (FPGM_LIVE=0), and bitmaps
+    written at every level from level 2 (FPGM_LIVE_FRAC above 1), also with partitions
+    beyond the staged cap (whose tests then leave their bitmaps out).  Every skeleton equals
+    the oracle's, test counts included."""
     raw, _, _ = F.generate(n_nodes=12, n_samples=70000, seed=72, n_edges=30, max_indegree=5, card=(6, 10))
     cols, card = O.relabel(raw)
     ref = O.pc_skeleton(cols, card, threads=16)
