@@ -1165,10 +1165,14 @@ __device__ __forceinline__ void load8(K (&z)[8], const K *src) {
 constexpr int kScatterChunk = kThreads * 16;
 // bmr (optional): the parent test's contributing-sample bitmap; samples whose bit is clear get
 // no record.  rec_s (optional): each record's sample index, written beside its code.
-template <class K>
-__device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint32_t *dim, int d, int64_t S, int lp,
-                                          K *rec_z, uint16_t *rec_xy, int *s_pcnt, int *s_poff, int *s_pcur, K *zbuf,
-                                          unsigned char *smem, const uint32_t *bmr, uint32_t *rec_s) {
+template <class K, bool kBits>
+__device__ __noinline__ void part_scatter_t(const uint8_t *const *col, const uint32_t *dim, int d, int64_t S, int lp,
+                                            K *rec_z, uint16_t *rec_xy, int *s_pcnt, int *s_poff, int *s_pcur, K *zbuf,
+                                            unsigned char *smem, const uint32_t *bmr, uint32_t *rec_s) {
+    if constexpr (!kBits) {
+        bmr = nullptr;
+        rec_s = nullptr;
+    }
     const int tid = threadIdx.x, P = 1 << lp;
     const int64_t nvec = S >> 4;
     const uint8_t *colx = col[d], *coly = col[d + 1];
@@ -1179,9 +1183,13 @@ __device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint3
     int *lcnt = reinterpret_cast<int *>(smem + kScatterChunk * (sizeof(K) + 7));
     int *lstart = lcnt + kPartMax, *gbase = lstart + kPartMax, *s_ctot = gbase + kPartMax;
     auto live16 = [&](int64_t v) -> uint32_t {
+        if constexpr (!kBits) return 0xffffu;
         return bmr ? (__ldcg(bmr + (v >> 1)) >> (16 * (int)(v & 1))) & 0xffffu : 0xffffu;
     };
-    auto live1 = [&](int64_t s) -> bool { return !bmr || ((__ldcg(bmr + (s >> 5)) >> (int)(s & 31)) & 1u); };
+    auto live1 = [&](int64_t s) -> bool {
+        if constexpr (!kBits) return true;
+        return !bmr || ((__ldcg(bmr + (s >> 5)) >> (int)(s & 31)) & 1u);
+    };
     for (int i = tid; i < P; i += kThreads) s_pcnt[i] = 0;
     __syncthreads();
     for (int64_t v = tid; v < nvec; v += kThreads) {
@@ -1335,6 +1343,17 @@ __device__ __noinline__ void part_scatter(const uint8_t *const *col, const uint3
     __syncthreads();
 }
 static_assert(kScatterChunk * (8 + 7) + 3 * kPartMax * 4 + 4 <= kSmemBytes, "scatter chunk in shared memory");
+// without a bitmap to read or write, the plain instance (no per-sample checks)
+template <class K>
+__device__ inline void part_scatter(const uint8_t *const *col, const uint32_t *dim, int d, int64_t S, int lp, K *rec_z,
+                                    uint16_t *rec_xy, int *s_pcnt, int *s_poff, int *s_pcur, K *zbuf, unsigned char *smem,
+                                    const uint32_t *bmr, uint32_t *rec_s) {
+    if (bmr || rec_s)
+        part_scatter_t<K, true>(col, dim, d, S, lp, rec_z, rec_xy, s_pcnt, s_poff, s_pcur, zbuf, smem, bmr, rec_s);
+    else
+        part_scatter_t<K, false>(col, dim, d, S, lp, rec_z, rec_xy, s_pcnt, s_poff, s_pcur, zbuf, smem, nullptr,
+                                 nullptr);
+}
 
 // Counts and scores one partition (n records from rec_z/rec_xy + base) in shared memory;
 // returns this thread's share of the statistic.  *s_over is set when the partition's codes
@@ -2382,6 +2401,7 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
     __shared__ const uint32_t *s_bmr;  // parent's contributing-sample bitmap (null: every sample)
     __shared__ uint32_t *s_bmw;        // this test's, being written (null: none)
     __shared__ int s_bmslot, s_bmbad;
+    __shared__ unsigned long long *s_lstat;  // this test measures the contributing fraction (null: no)
     const int tid = threadIdx.x;
     char *slot = a.slot_mem + (int64_t)blockIdx.x * a.slot_bytes;
     const SlotLayout L = slot_layout(a.slot_S, (uint32_t)a.hash_cap_global);
@@ -2436,7 +2456,11 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
                     s_bmw = a.bm_pool + (int64_t)sl * a.bm_words;
                 }
             }
-            if (a.live_stat) atomicAdd(&a.live_stat[1], (unsigned long long)S);  // the test's samples
+            // one test in eight (and none of the partition-parallel ones) measures the contributing fraction
+            s_lstat = (a.live_stat && (idx & 7) == 0 && !(a.wide != nullptr && idx >= np - (int)gridDim.x))
+                          ? a.live_stat
+                          : nullptr;
+            if (s_lstat) atomicAdd(&s_lstat[1], (unsigned long long)S);  // the test's samples
         }
         __syncthreads();
         if (s_bmw)  // cleared before any bit is set (part_scatter's barriers come first)
@@ -2485,10 +2509,14 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
             }
             if (tid == 0) {
                 w->poff[P] = s_poff[P];
-                int kept = 0;  // as in the per-CTA path: fewer records per super-partition with a bitmap
-                for (int i = 0; i < P; ++i) kept += s_pcnt[i];
-                int rk = (int)fmin((double)rw, 0.7 * lim * (double)kept / fmax(est, 1.0)) & ~7;
-                const int nne = plan_super(s_pcnt, P, rk < 64 ? 64 : rk, w->sp);
+                int rk = rw;
+                if (s_bmr) {  // as in the per-CTA path: fewer records per super-partition with a bitmap
+                    int kept = 0;
+                    for (int i = 0; i < P; ++i) kept += s_pcnt[i];
+                    rk = (int)fmin((double)rw, 0.7 * lim * (double)kept / fmax(est, 1.0)) & ~7;
+                    if (rk < 64) rk = 64;
+                }
+                const int nne = plan_super(s_pcnt, P, rk, w->sp);
                 w->item = item;
                 w->owner = blockIdx.x;
                 w->lp = lw;
@@ -2531,13 +2559,19 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
             if (tid == 0) {
                 // strata are at most est whichever samples were kept: with a parent's bitmap, as
                 // many strata fall on fewer records, so the super-partitions hold fewer records
-                int kept = 0;
-                for (int i = 0; i < (1 << lp); ++i) kept += s_pcnt[i];
-                int rk = (int)fmin((double)rmax, 0.7 * lim * (double)kept / fmax(est, 1.0)) & ~7;
-                s_nsp = plan_super(s_pcnt, 1 << lp, rk < 64 ? 64 : rk, s_sp);
+                int rk = rmax;
+                if (s_bmr) {
+                    int kept = 0;
+                    for (int i = 0; i < (1 << lp); ++i) kept += s_pcnt[i];
+                    rk = (int)fmin((double)rmax, 0.7 * lim * (double)kept / fmax(est, 1.0)) & ~7;
+                    if (rk < 64) rk = 64;
+                }
+                s_nsp = plan_super(s_pcnt, 1 << lp, rk, s_sp);
                 if (a.dbg) {  // contributing-sample bitmaps: tests with a parent's, samples, records kept
                     atomicAdd(&a.dbg[28], s_bmr ? 1ull : 0ull);
                     atomicAdd(&a.dbg[29], (unsigned long long)S);
+                    int kept = 0;
+                    for (int i = 0; i < (1 << lp); ++i) kept += s_pcnt[i];
                     atomicAdd(&a.dbg[30], (unsigned long long)kept);
                     atomicAdd(&a.dbg[31], s_bmw ? 1ull : 0ull);
                 }
@@ -2547,11 +2581,11 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_kernel(WaveArgs a) {
             if (code32)
                 acc = part_run<false>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, s_pcnt, s_poff, s_sp, s_nsp, dx,
                                       dy, smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
-                                      s_bin, claims, a.stage_rec, a.dbg, s_bmw, rs, &s_bmbad, a.live_stat);
+                                      s_bin, claims, a.stage_rec, a.dbg, s_bmw, rs, &s_bmbad, s_lstat);
             else
                 acc = part_run<false>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, s_pcnt, s_poff, s_sp, s_nsp, dx,
                                       dy, smem_raw, gord, gwt, zk, a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc,
-                                      s_bin, claims, a.stage_rec, a.dbg, s_bmw, rs, &s_bmbad, a.live_stat);
+                                      s_bin, claims, a.stage_rec, a.dbg, s_bmw, rs, &s_bmbad, s_lstat);
             atomicAdd(&s_distinct, claims);
             __syncthreads();
             over = s_over != 0;
@@ -2644,11 +2678,11 @@ __global__ void __launch_bounds__(kThreads, 2) ci_part_wide_kernel(WaveArgs a) {
             code32 ? part_super<false, uint32_t>(lp, reinterpret_cast<const uint32_t *>(rz), rxy, w->pcnt, w->poff,
                                                  w->sp[p], w->sp[p + 1], dx, dy, smem_raw, gord, gwt, zk,
                                                  a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc, s_bin, claims,
-                                                 a.stage_rec, nullptr, bmw, rs, &s_bmbad, a.live_stat)
+                                                 a.stage_rec, nullptr, bmw, rs, &s_bmbad, nullptr)
                    : part_super<false, uint64_t>(lp, reinterpret_cast<const uint64_t *>(rz), rxy, w->pcnt, w->poff,
                                                  w->sp[p], w->sp[p + 1], dx, dy, smem_raw, gord, gwt, zk,
                                                  a.want_hash != 0, s_w, &s_over, &s_nbig, &s_nocc, s_bin, claims,
-                                                 a.stage_rec, nullptr, bmw, rs, &s_bmbad, a.live_stat);
+                                                 a.stage_rec, nullptr, bmw, rs, &s_bmbad, nullptr);
         const bool over = s_over != 0;  // read after part_super's closing barrier
         const Partial r = block_sum(q, scratch);
         if (tid == 0) {
