@@ -959,6 +959,13 @@ int live_setup(fpgm_engine *e, int d) {
     e->live_write = false;
     if (!e->live_on || !e->live_next || d < e->live_min_level || max_table_ints(e->h_card, d) <= kCtaInts - 64)
         return FPGM_OK;
+    if (e->live_cap > 0 && (e->S + 31) / 32 > e->live_words) {  // a larger dataset since: bigger bitmaps
+        for (int q = 0; q < 2; ++q) {
+            e->live_pool[q].release();
+            e->live_tab[q].release();
+        }
+        e->live_cap = 0;
+    }
     if (e->live_cap == 0) {
         const int64_t words = (e->S + 31) / 32;
         size_t free_b = 0, total_b = 0;

@@ -391,3 +391,22 @@ def test_tier2_paths_match_oracle_over_repeated_skeletons(monkeypatch, env):
             res = e.result()
             assert np.array_equal(res["adj"], ref["adj"]) and res["sepsets"] == ref["sepsets"]
             assert st["tests"] == ref["stats"]["tests"]
+
+
+def test_bitmaps_follow_a_larger_dataset_in_the_same_engine(monkeypatch):
+    """Contributing-sample bitmaps written at every level from level 2 (FPGM_LIVE_FRAC above
+    1), in one engine that learns a 20,000-sample dataset and then a 70,000-sample one: the
+    bitmap pools are remade for the larger sample count, and both skeletons equal the oracle's."""
+    monkeypatch.setenv("FPGM_LIVE_FRAC", "1.01")
+    monkeypatch.setenv("FPGM_LIVE_MIN_LEVEL", "2")
+    with F.Engine(0) as e:
+        for S, seed in ((20000, 73), (70000, 72)):
+            raw, _, _ = F.generate(n_nodes=12, n_samples=S, seed=seed, n_edges=30, max_indegree=5, card=(6, 10))
+            cols, card = O.relabel(raw)
+            ref = O.pc_skeleton(cols, card, threads=16)
+            e.upload(raw)
+            for _ in range(2):
+                st = e.pc_skeleton().to_dict()
+                res = e.result()
+                assert np.array_equal(res["adj"], ref["adj"]) and res["sepsets"] == ref["sepsets"], S
+                assert st["tests"] == ref["stats"]["tests"], S
